@@ -1,0 +1,917 @@
+// Spin-orbital CISD / CID residual on the GPU: block builders, per-iteration
+// amplitude layouts, the residual as a sequence of complex GEMMs plus one
+// packed assembly kernel, the amplitude update, DIIS dot products and the
+// fused DIIS combination / energy / norm reduction.
+//
+// Amplitudes are kept packed: t2p[p(i<j)][p(a<b)] = t2[i,j,a,b].  Every
+// quantity of the reference with full (i,j,a,b) ranges is recovered through
+// the antisymmetry t2[i,j,a,b] = -t2[j,i,a,b] = -t2[i,j,b,a]; the full-vector
+// sums of the reference (energy, DIIS Gram, rms) equal 4x the packed sums.
+#include <vector>
+#include <string>
+#include <mutex>
+#include <atomic>
+
+#include "cisd_plan.h"
+
+namespace agb {
+
+agb_status zgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                    const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                    void* scratch, size_t scratch_bytes, cudaStream_t stream);
+agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
+                 cudaStream_t stream);
+agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
+                        int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                        void* scratch, size_t scratch_bytes, cudaStream_t stream);
+size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
+
+namespace {
+
+// ----------------------------------------------------------------- blocks --
+
+enum BlockId { B_R0p = 0, B_Wop, B_VT, B_Wvovv, B_Wooov, B_Wovoo, B_Wvvvo, B_Woooo, B_Wvvvv, B_COUNT };
+// Orbital-range letters of each block's <PQ||RS> (o = occupied, v = virtual).
+const char* kBlockRanges[B_COUNT] = {"vvoo", "oovv", "ovvo", "vovv", "ooov", "ovoo", "vvvo", "oooo", "vvvv"};
+
+struct Dims {
+  int o, v;
+  int64_t ov, po, pv;
+  const int2* opairs;
+  const int2* vpairs;
+};
+
+// Output element e of block id -> spin-orbital indices (P,Q,R,S) of <PQ||RS>.
+__device__ __forceinline__ void block_indices(int id, int64_t e, const Dims& d, int& P, int& Q, int& R, int& S) {
+  const int o = d.o, v = d.v;
+  switch (id) {
+    case B_R0p: {  // [p(ij)][p(ab)] <ab||ij>
+      int2 ij = d.opairs[e / d.pv], ab = d.vpairs[e % d.pv];
+      P = o + ab.x; Q = o + ab.y; R = ij.x; S = ij.y; break;
+    }
+    case B_Wop: {  // [p(ij)][p(ab)] <ij||ab>
+      int2 ij = d.opairs[e / d.pv], ab = d.vpairs[e % d.pv];
+      P = ij.x; Q = ij.y; R = o + ab.x; S = o + ab.y; break;
+    }
+    case B_VT: {  // [(j,b)][(k,c)] <kb||cj>
+      int64_t row = e / d.ov, col = e % d.ov;
+      int j = (int)(row / v), b = (int)(row % v), k = (int)(col / v), c = (int)(col % v);
+      P = k; Q = o + b; R = o + c; S = j; break;
+    }
+    case B_Wvovv: {  // [a][j][p(cb)] <aj||cb>
+      int2 cb = d.vpairs[e % d.pv];
+      int64_t rest = e / d.pv;
+      int j = (int)(rest % o), a = (int)(rest / o);
+      P = o + a; Q = j; R = o + cb.x; S = o + cb.y; break;
+    }
+    case B_Wooov: {  // [i][p(kj)][b] <kj||ib>
+      int b = (int)(e % v);
+      int64_t rest = e / v;
+      int2 kj = d.opairs[rest % d.po];
+      int i = (int)(rest / d.po);
+      P = kj.x; Q = kj.y; R = i; S = o + b; break;
+    }
+    case B_Wovoo: {  // [p(ij)][b][k] <kb||ij>
+      int k = (int)(e % o);
+      int64_t rest = e / o;
+      int b = (int)(rest % v);
+      int2 ij = d.opairs[rest / v];
+      P = k; Q = o + b; R = ij.x; S = ij.y; break;
+    }
+    case B_Wvvvo: {  // [c][j][p(ab)] <ab||cj>
+      int2 ab = d.vpairs[e % d.pv];
+      int64_t rest = e / d.pv;
+      int j = (int)(rest % o), c = (int)(rest / o);
+      P = o + ab.x; Q = o + ab.y; R = o + c; S = j; break;
+    }
+    case B_Woooo: {  // [p(ij)][p(kl)] <kl||ij>
+      int2 ij = d.opairs[e / d.po], kl = d.opairs[e % d.po];
+      P = kl.x; Q = kl.y; R = ij.x; S = ij.y; break;
+    }
+    default: {  // B_Wvvvv [p(ab)][p(cd)] <ab||cd>
+      int2 ab = d.vpairs[e / d.pv], cd = d.vpairs[e % d.pv];
+      P = o + ab.x; Q = o + ab.y; R = o + cd.x; S = o + cd.y; break;
+    }
+  }
+}
+
+int64_t block_elems(int id, const agb_cisd_plan* p) {
+  switch (id) {
+    case B_R0p: case B_Wop: return p->po * p->pv;
+    case B_VT: return p->ov * p->ov;
+    case B_Wvovv: return (int64_t)p->v * p->o * p->pv;
+    case B_Wooov: return (int64_t)p->o * p->po * p->v;
+    case B_Wovoo: return p->po * p->v * p->o;
+    case B_Wvvvo: return (int64_t)p->v * p->o * p->pv;
+    case B_Woooo: return p->po * p->po;
+    default: return p->pv * p->pv;
+  }
+}
+
+// Chemist sources (pq|rs) in spin orbitals.
+struct SrcMO {  // spatial ERI_MO[n^4] with the spin integration of compute_ERI_SO
+  const z64* g; int64_t n;
+  __device__ __forceinline__ z64 chem(int p, int q, int r, int s) const {
+    if (((p ^ q) & 1) || ((r ^ s) & 1)) return zmk(0, 0);
+    return g[(((int64_t)(p >> 1) * n + (q >> 1)) * n + (r >> 1)) * n + (s >> 1)];
+  }
+};
+struct SrcSO {  // full spin-orbital chemist tensor
+  const z64* g; int64_t n;
+  __device__ __forceinline__ z64 chem(int p, int q, int r, int s) const {
+    return g[(((int64_t)p * n + q) * n + r) * n + s];
+  }
+};
+struct SrcChem {  // chemist sub-block over index ranges [off_i, off_i + len_i)
+  const z64* g; int off0, off1, off2, off3; int64_t len1, len2, len3;
+  __device__ __forceinline__ z64 chem(int p, int q, int r, int s) const {
+    return g[((((int64_t)(p - off0)) * len1 + (q - off1)) * len2 + (r - off2)) * len3 + (s - off3)];
+  }
+};
+
+template <class SD, class SE>
+__global__ void build_block_kernel(int id, Dims d, int64_t total, SD sd, SE se, z64* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int P, Q, R, S;
+    block_indices(id, e, d, P, Q, R, S);
+    // <PQ||RS> = (PR|QS) - (PS|QR)
+    out[e] = zsub(sd.chem(P, R, Q, S), se.chem(P, S, Q, R));
+  }
+}
+
+// Bsub[(x,y)][L] = Bf[L][x0+x][y0+y]
+__global__ void extract_factor_kernel(const z64* __restrict__ Bf, int64_t naux, int64_t nso, int x0, int nx, int y0,
+                                      int ny, z64* __restrict__ out) {
+  int64_t total = (int64_t)nx * ny * naux;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t L = e % naux, xy = e / naux;
+    int64_t x = xy / ny, y = xy % ny;
+    out[e] = Bf[(L * nso + x0 + x) * nso + y0 + y];
+  }
+}
+
+// ------------------------------------------------------- Fock and tables --
+
+__global__ void fock_extract_kernel(const z64* __restrict__ F, const double* __restrict__ eps_in, int o, int v,
+                                    z64* FvoT, z64* Foo, z64* Fvv, z64* Fov, double* eps, int* offdiag) {
+  int nso = o + v;
+  int64_t total = (int64_t)nso * nso;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int p = (int)(e / nso), q = (int)(e % nso);
+    z64 f = F[e];
+    if (p < o && q < o) {
+      Foo[p * o + q] = f;
+      if (p != q && (f.x != 0.0 || f.y != 0.0)) atomicOr(offdiag, 1);
+    } else if (p >= o && q >= o) {
+      Fvv[(p - o) * v + (q - o)] = f;
+      if (p != q && (f.x != 0.0 || f.y != 0.0)) atomicOr(offdiag, 1);
+    } else if (p < o) {
+      if (Fov) Fov[p * v + (q - o)] = f;
+    } else {
+      if (FvoT) FvoT[q * v + (p - o)] = f;  // F[a,i] at [i][a]
+    }
+    if (e < nso) eps[e] = eps_in[e];
+  }
+}
+
+// ------------------------------------------------- per-iteration layouts --
+
+__device__ __forceinline__ int sgn_pair(int x, int y) { return x < y ? 1 : (x > y ? -1 : 0); }
+
+// Tring[(i,a)][(k,c)] = t2[i,k,a,c]
+__global__ void unpack_ring_kernel(const z64* __restrict__ t2p, int o, int v, int64_t pv, z64* __restrict__ out) {
+  int64_t ov = (int64_t)o * v, total = ov * ov;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t row = e / ov, col = e % ov;
+    int i = (int)(row / v), a = (int)(row % v), k = (int)(col / v), c = (int)(col % v);
+    int s = sgn_pair(i, k) * sgn_pair(a, c);
+    z64 val = zmk(0, 0);
+    if (s != 0) {
+      int64_t p = pair_index(min(i, k), max(i, k), o), q = pair_index(min(a, c), max(a, c), v);
+      val = t2p[p * pv + q];
+      if (s < 0) val = zneg(val);
+    }
+    out[e] = val;
+  }
+}
+
+// t2h[i][j][q] = t2[i,j,(a<b)_q]
+__global__ void unpack_h_kernel(const z64* __restrict__ t2p, int o, int64_t pv, z64* __restrict__ out) {
+  int64_t total = (int64_t)o * o * pv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t q = e % pv, ij = e / pv;
+    int i = (int)(ij / o), j = (int)(ij % o);
+    int s = sgn_pair(i, j);
+    z64 val = zmk(0, 0);
+    if (s != 0) {
+      val = t2p[pair_index(min(i, j), max(i, j), o) * pv + q];
+      if (s < 0) val = zneg(val);
+    }
+    out[e] = val;
+  }
+}
+
+// t2q[p][a][b] = t2[(i<j)_p, a, b]
+__global__ void unpack_q_kernel(const z64* __restrict__ t2p, int64_t po, int v, int64_t pv, z64* __restrict__ out) {
+  int64_t vv = (int64_t)v * v, total = po * vv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p = e / vv, ab = e % vv;
+    int a = (int)(ab / v), b = (int)(ab % v);
+    int s = sgn_pair(a, b);
+    z64 val = zmk(0, 0);
+    if (s != 0) {
+      val = t2p[p * pv + pair_index(min(a, b), max(a, b), v)];
+      if (s < 0) val = zneg(val);
+    }
+    out[e] = val;
+  }
+}
+
+// y = x (or 0) , optionally y -= E*t
+__global__ void r1_init_kernel(const z64* __restrict__ src, int64_t n, z64* __restrict__ r) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    r[e] = src ? src[e] : zmk(0, 0);
+}
+__global__ void axpy_kernel(int64_t n, z64 alpha, const z64* __restrict__ x, z64* __restrict__ y) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    z64 t = y[e];
+    zfma(t, alpha, x[e]);
+    y[e] = t;
+  }
+}
+
+// ------------------------------------------------------------- assembly --
+
+struct AsmArgs {
+  int o, v;
+  int64_t ov, po, pv;
+  const int2* opairs;
+  const z64 *R0p, *PQ, *X, *Zq, *Yh, *Gq, *H2h, *t2p;
+  const double* eps;     // SO energies (for the diagonal-Fock fast path)
+  const z64 *Foo, *Fvv;  // diagonal-Fock fast path reads F[p,p]
+  z64 E;
+  int use_const, use_e, singles, f_diag;
+  z64* r2p;
+};
+
+constexpr int TS = 32;  // (a,b) tile edge
+
+// One CTA per (pair p(ij), upper-triangle tile of (a,b)).  Terms whose source
+// is indexed [b][a] are summed first along a (coalesced) into shared memory
+// and read transposed; the rest are read along b.
+__global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
+  __shared__ z64 tr[TS][TS + 1];
+  const int ntile = (A.v + TS - 1) / TS;
+  // decode tile pair (ta <= tb) from blockIdx.x
+  int tp = blockIdx.x, ta = 0;
+  while (tp >= ntile - ta) { tp -= ntile - ta; ++ta; }
+  const int tb = ta + tp;
+  const int64_t p = blockIdx.y;
+  const int2 ij = A.opairs[p];
+  const int i = ij.x, j = ij.y;
+  const int a0 = ta * TS, b0 = tb * TS;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const int v = A.v;
+  const int64_t vv = (int64_t)v * v;
+  // Phase 1: transposed terms T[b][a] for b in tile tb, a in tile ta (coalesced along a).
+  for (int rb = ty; rb < TS; rb += 8) {
+    int b = b0 + rb, a = a0 + tx;
+    z64 s = zmk(0, 0);
+    if (a < v && b < v) {
+      // -X[(i,b),(j,a)] + X[(j,b),(i,a)]
+      s = zneg(A.X[((int64_t)i * v + b) * A.ov + (int64_t)j * v + a]);
+      s = zadd(s, A.X[((int64_t)j * v + b) * A.ov + (int64_t)i * v + a]);
+      if (A.singles) s = zsub(s, A.Zq[p * vv + (int64_t)b * v + a]);      // -Zq[p][b][a]
+      if (!A.f_diag) s = zsub(s, A.Gq[p * vv + (int64_t)b * v + a]);      // -Gq[p][b][a]
+    }
+    tr[rb][tx] = s;
+  }
+  __syncthreads();
+  // Phase 2: direct terms along b, plus tr[b][a].
+  for (int ra = ty; ra < TS; ra += 8) {
+    int a = a0 + ra, b = b0 + tx;
+    if (a >= v || b >= v || b <= a) continue;
+    int64_t q = pair_index(a, b, v);
+    int64_t pq = p * A.pv + q;
+    z64 s = tr[tx][ra];
+    s = zadd(s, A.PQ[pq]);
+    s = zadd(s, A.X[((int64_t)i * v + a) * A.ov + (int64_t)j * v + b]);
+    s = zsub(s, A.X[((int64_t)j * v + a) * A.ov + (int64_t)i * v + b]);
+    if (A.singles) {
+      s = zadd(s, A.Zq[p * vv + (int64_t)a * v + b]);
+      s = zadd(s, A.Yh[((int64_t)i * A.o + j) * A.pv + q]);
+      s = zsub(s, A.Yh[((int64_t)j * A.o + i) * A.pv + q]);
+    }
+    z64 t = A.t2p[pq];
+    if (A.f_diag) {
+      // sum_c F[b,c] t2[ijac] + F[a,c] t2[ijcb] - F[k,j] t2[ikab] - F[k,i] t2[kjab] with F diagonal
+      z64 fs = zadd(zadd(A.Fvv[(int64_t)a * v + a], A.Fvv[(int64_t)b * v + b]),
+                    zneg(zadd(A.Foo[(int64_t)i * A.o + i], A.Foo[(int64_t)j * A.o + j])));
+      s = zadd(s, zmul(fs, t));
+    } else {
+      s = zadd(s, A.Gq[p * vv + (int64_t)a * v + b]);
+      s = zadd(s, A.H2h[((int64_t)j * A.o + i) * A.pv + q]);
+      s = zsub(s, A.H2h[((int64_t)i * A.o + j) * A.pv + q]);
+    }
+    if (A.use_const) s = zadd(s, A.R0p[pq]);
+    if (A.use_e) s = zsub(s, zmul(A.E, t));
+    A.r2p[pq] = s;
+  }
+}
+
+// ------------------------------------------------------- update / guess --
+
+struct VecDims {
+  int o, v;
+  int64_t n1, pv;
+  const int2* opairs;
+  const int2* vpairs;
+  const double* eps;
+};
+
+__device__ __forceinline__ double denom_at(const VecDims& d, int64_t k) {
+  if (k < d.n1) {
+    int i = (int)(k / d.v), a = (int)(k % d.v);
+    return d.eps[i] - d.eps[d.o + a];
+  }
+  int64_t e = k - d.n1;
+  int2 ij = d.opairs[e / d.pv], ab = d.vpairs[e % d.pv];
+  return d.eps[ij.x] + d.eps[ij.y] - d.eps[d.o + ab.x] - d.eps[d.o + ab.y];
+}
+
+// t_out = t + r * (1/D), the exact operation numpy performs for complex / real.
+__global__ void update_kernel(VecDims d, int64_t n, const z64* __restrict__ t, const z64* __restrict__ r,
+                              z64* __restrict__ t_out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    double inv = 1.0 / denom_at(d, k);
+    z64 rr = r[k], tt = t[k];
+    t_out[k] = zmk(tt.x + rr.x * inv, tt.y + rr.y * inv);
+  }
+}
+
+// guess: t1 = F_ai / D_ia, t2p = <ab||ij> / D
+__global__ void guess_kernel(VecDims d, int64_t n, const z64* __restrict__ FvoT, const z64* __restrict__ R0p,
+                             z64* __restrict__ t) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    double inv = 1.0 / denom_at(d, k);
+    z64 num = k < d.n1 ? FvoT[k] : R0p[k - d.n1];
+    t[k] = zmk(num.x * inv, num.y * inv);
+  }
+}
+
+// ------------------------------------------------------------ reductions --
+
+__device__ __forceinline__ z64 warp_sum(z64 s) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, off);
+    s.y += __shfl_xor_sync(0xffffffffu, s.y, off);
+  }
+  return s;
+}
+
+// Block-reduce NV complex accumulators; thread 0 writes them to out[blockIdx.x*NV + k].
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(z64 (&acc)[NV], z64* out) {
+  __shared__ z64 sh[NV][32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    z64 s = warp_sum(acc[k]);
+    if (lane == 0) sh[k][w] = s;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      z64 s = lane < nw ? sh[k][lane] : zmk(0, 0);
+      s = warp_sum(s);
+      if (lane == 0) out[(int64_t)blockIdx.x * NV + k] = s;
+    }
+  }
+}
+
+// out[k] = sum over blocks of partial[b*nv + k], fixed order (deterministic)
+__global__ void finish_partials_kernel(const z64* __restrict__ partial, int nblocks, int nv, z64* out) {
+  int k = threadIdx.x;
+  if (k >= nv) return;
+  z64 s = zmk(0, 0);
+  for (int b = 0; b < nblocks; ++b) s = zadd(s, partial[(int64_t)b * nv + k]);
+  out[k] = s;
+}
+
+constexpr int kRedBlocks = 152 * 4;
+constexpr int kMaxVec = 16;
+
+struct DotArgs {
+  int64_t n1, n2;
+  double w1, w2;
+  const z64* x;
+  const z64* ys[kMaxVec];
+  int ny;
+};
+
+template <int NY>
+__global__ void __launch_bounds__(256) dots_kernel(DotArgs A, z64* partial) {
+  z64 acc[NY];
+#pragma unroll
+  for (int j = 0; j < NY; ++j) acc[j] = zmk(0, 0);
+  int64_t n = A.n1 + A.n2;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    z64 x = A.x[k];
+    double w = k < A.n1 ? A.w1 : A.w2;
+#pragma unroll
+    for (int j = 0; j < NY; ++j) {
+      if (j < A.ny) {
+        z64 y = A.ys[j][k];
+        // conj(y) * x
+        acc[j].x += w * (y.x * x.x + y.y * x.y);
+        acc[j].y += w * (y.x * x.y - y.y * x.x);
+      }
+    }
+  }
+  block_reduce_store<NY>(acc, partial);
+}
+
+struct CombArgs {
+  int64_t n1, n2;
+  const z64* ys[kMaxVec];
+  double c[2 * kMaxVec];
+  int ny;
+  const z64* t_old;
+  z64* t_new;
+  const z64* ew;   // energy weights [F_ov | <ij||ab>_p]
+};
+
+__global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) {
+  z64 acc[3] = {zmk(0, 0), zmk(0, 0), zmk(0, 0)};  // E, s1, s2
+  int64_t n = A.n1 + A.n2;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    z64 t = zmk(0, 0);
+    for (int j = 0; j < A.ny; ++j) zfma(t, zmk(A.c[2 * j], A.c[2 * j + 1]), A.ys[j][k]);
+    z64 old = A.t_old[k];
+    A.t_new[k] = t;
+    z64 dlt = zsub(old, t);
+    z64 d2 = zmul(dlt, dlt);
+    z64 e = zmul(t, A.ew[k]);
+    acc[0] = zadd(acc[0], e);
+    if (k < A.n1) acc[1] = zadd(acc[1], d2); else acc[2] = zadd(acc[2], d2);
+  }
+  acc[2] = zscale(acc[2], 4.0);
+  block_reduce_store<3>(acc, partial);
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+}  // namespace agb
+
+using namespace agb;
+
+// =================================================================== plan ==
+
+static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char* {
+    char* ptr = base ? base + off : nullptr;
+    off += align256(bytes);
+    return ptr;
+  };
+  const size_t Z = sizeof(z64);
+  const int64_t o = P->o, v = P->v, ov = P->ov, po = P->po, pv = P->pv;
+  P->FvoT = (z64*)take(Z * ov);
+  P->Foo = (z64*)take(Z * o * o);
+  P->Fvv = (z64*)take(Z * v * v);
+  P->EW = (z64*)take(Z * (P->n1 + P->n2));
+  P->eps = (double*)take(sizeof(double) * P->nso);
+  P->opairs = (int2*)take(sizeof(int2) * (po > 0 ? po : 1));
+  P->vpairs = (int2*)take(sizeof(int2) * (pv > 0 ? pv : 1));
+  P->R0p = (z64*)take(Z * po * pv);
+  if (P->mp2_only) {
+    P->VT = P->WooooT = P->Wvp = P->Tring = P->X = P->PQ = P->t2h = P->t2q = P->Gq = P->H2h = nullptr;
+    P->WvovvH = P->WooovP = P->WovooP = P->WvvvoP = P->Zq = P->Yh = nullptr;
+    P->gemm_scratch = take(4096);
+    P->gemm_scratch_bytes = 4096;
+    *total = off;
+    return;
+  }
+  P->VT = (z64*)take(Z * ov * ov);
+  P->WooooT = (z64*)take(Z * po * po);
+  P->Wvp = (z64*)take(Z * pv * pv);
+  P->Tring = (z64*)take(Z * ov * ov);
+  P->X = (z64*)take(Z * ov * ov);
+  P->PQ = (z64*)take(Z * po * pv);
+  // t2h/t2q serve the singles terms and the non-diagonal Fock terms
+  P->t2h = (z64*)take(Z * o * o * pv);
+  P->t2q = (z64*)take(Z * po * v * v);
+  P->Gq = (z64*)take(Z * po * v * v);
+  P->H2h = (z64*)take(Z * o * o * pv);
+  if (P->singles) {
+    P->WvovvH = (z64*)take(Z * v * o * pv);
+    P->WooovP = (z64*)take(Z * o * po * v);
+    P->WovooP = (z64*)take(Z * po * v * o);
+    P->WvvvoP = (z64*)take(Z * v * o * pv);
+    P->Zq = (z64*)take(Z * po * v * v);
+    P->Yh = (z64*)take(Z * o * o * pv);
+  } else {
+    P->WvovvH = P->WooovP = P->WovooP = P->WvvvoP = P->Zq = P->Yh = nullptr;
+  }
+  // GEMM scratch: split-K partials (FP64) or 3xTF32 operand planes.
+  size_t gs = (size_t)64 << 20;
+  if (P->mixed) {
+    auto upd = [&](int64_t M, int64_t N, int64_t K) {
+      size_t s = agb::cgemm_tf32x3_scratch(M, N, K);
+      if (s > gs) gs = s;
+    };
+    upd(ov, ov, ov);
+    upd(po, pv, pv);
+    upd(po, pv, po);
+    upd(po * v, v, v);
+    upd(o, o * pv, o);
+    if (P->singles) {
+      upd(o, v, o * pv);
+      upd(o, v, po * v);
+      upd(po * v, v, o);
+      upd(o, o * pv, v);
+    }
+  }
+  P->gemm_scratch = take(gs);
+  P->gemm_scratch_bytes = gs;
+  *total = off;
+}
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void agb_set_error_message(const char* msg, const char* file, int line) {
+  g_last_error = std::string(msg) + " (" + file + ":" + std::to_string(line) + ")";
+}
+
+static std::atomic<unsigned long long> g_launches{0};
+void agb_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+extern "C" unsigned long long agb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+namespace agb {
+namespace {
+
+// GEMM on the selected backend.  conj flags are never needed on the hot path.
+agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm,
+                int64_t sAk, const z64* B, int64_t sBk, int64_t sBn, z64 beta, z64* C, int64_t ldc,
+                cudaStream_t st) {
+  if (prec == AGB_PREC_TF32X3)
+    return cgemm_tf32x3(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, P->gemm_scratch,
+                        P->gemm_scratch_bytes, st);
+  // FP64 split-K partials start past the 256-byte status header of the scratch.
+  return zgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, (char*)P->gemm_scratch + 256,
+                  P->gemm_scratch_bytes - 256, st);
+}
+
+Dims dims_of(const agb_cisd_plan* P) { return Dims{P->o, P->v, P->ov, P->po, P->pv, P->opairs, P->vpairs}; }
+VecDims vdims_of(const agb_cisd_plan* P) { return VecDims{P->o, P->v, P->n1, P->pv, P->opairs, P->vpairs, P->eps}; }
+
+z64* block_ptr(agb_cisd_plan* P, int id) {
+  switch (id) {
+    case B_R0p: return P->R0p;
+    case B_Wop: return P->EW + P->n1;
+    case B_VT: return P->VT;
+    case B_Wvovv: return P->WvovvH;
+    case B_Wooov: return P->WooovP;
+    case B_Wovoo: return P->WovooP;
+    case B_Wvvvo: return P->WvvvoP;
+    case B_Woooo: return P->WooooT;
+    default: return P->Wvp;
+  }
+}
+
+bool block_needed(const agb_cisd_plan* P, int id) {
+  if (P->mp2_only) return id == B_R0p || id == B_Wop;
+  if (P->singles) return true;
+  return id == B_R0p || id == B_Wop || id == B_VT || id == B_Woooo || id == B_Wvvvv;
+}
+
+template <class SD, class SE>
+agb_status launch_build(agb_cisd_plan* P, int id, SD sd, SE se, cudaStream_t st) {
+  int64_t n = block_elems(id, P);
+  if (n == 0) return AGB_OK;
+  build_block_kernel<SD, SE><<<grid_for(n, 256), 256, 0, st>>>(id, dims_of(P), n, sd, se, block_ptr(P, id));
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+}  // namespace
+}  // namespace agb
+
+extern "C" {
+
+int agb_version(void) { return 100; }
+const char* agb_last_error(void) { return g_last_error.c_str(); }
+
+agb_status agb_cisd_plan_create(int o, int v, int flags, agb_cisd_plan** plan) {
+  AGB_ARG_CHECK(plan != nullptr, "plan_create: null output");
+  AGB_ARG_CHECK(o >= 2 && v >= 2 && o % 2 == 0 && v % 2 == 0, "plan_create: o, v must be even and >= 2");
+  agb_cisd_plan* P = new agb_cisd_plan();
+  P->o = o; P->v = v; P->flags = flags;
+  P->nso = o + v; P->ov = (int64_t)o * v; P->po = npairs(o); P->pv = npairs(v);
+  P->mp2_only = (flags & AGB_PLAN_MP2) != 0;
+  P->singles = !(flags & (AGB_PLAN_NO_SINGLES | AGB_PLAN_MP2));
+  P->mixed = (flags & AGB_PLAN_MIXED) != 0;
+  P->n1 = P->singles ? P->ov : 0;
+  P->n2 = P->po * P->pv;
+  P->f_diag = true;
+  P->ws = nullptr;
+  plan_layout(P, nullptr, &P->ws_bytes);
+  *plan = P;
+  return AGB_OK;
+}
+
+agb_status agb_cisd_plan_destroy(agb_cisd_plan* plan) {
+  delete plan;
+  return AGB_OK;
+}
+
+agb_status agb_cisd_plan_workspace_bytes(const agb_cisd_plan* plan, size_t* bytes) {
+  AGB_ARG_CHECK(plan && bytes, "workspace_bytes: null argument");
+  *bytes = plan->ws_bytes;
+  return AGB_OK;
+}
+
+agb_status agb_cisd_plan_sizes(const agb_cisd_plan* plan, int64_t* n1, int64_t* n2) {
+  AGB_ARG_CHECK(plan && n1 && n2, "plan_sizes: null argument");
+  *n1 = plan->n1;
+  *n2 = plan->n2;
+  return AGB_OK;
+}
+
+agb_status agb_cisd_plan_set_workspace(agb_cisd_plan* P, void* workspace, size_t bytes) {
+  AGB_ARG_CHECK(P != nullptr, "set_workspace: null plan");
+  if (workspace == nullptr || bytes < P->ws_bytes) {
+    agb_set_error_message("set_workspace: workspace missing or smaller than agb_cisd_plan_workspace_bytes",
+                          __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  AGB_ARG_CHECK(((uintptr_t)workspace & 255) == 0, "set_workspace: workspace must be 256-byte aligned");
+  size_t total;
+  P->ws = workspace;
+  plan_layout(P, (char*)workspace, &total);
+  // pair tables
+  std::vector<int2> op(P->po > 0 ? P->po : 1), vp(P->pv > 0 ? P->pv : 1);
+  for (int p = 0, k = 0; p < P->o; ++p)
+    for (int q = p + 1; q < P->o; ++q) op[k++] = make_int2(p, q);
+  for (int p = 0, k = 0; p < P->v; ++p)
+    for (int q = p + 1; q < P->v; ++q) vp[k++] = make_int2(p, q);
+  AGB_CUDA_TRY(cudaMemcpy(P->opairs, op.data(), sizeof(int2) * op.size(), cudaMemcpyHostToDevice));
+  AGB_CUDA_TRY(cudaMemcpy(P->vpairs, vp.data(), sizeof(int2) * vp.size(), cudaMemcpyHostToDevice));
+  AGB_CUDA_TRY(cudaMemset(P->gemm_scratch, 0, 256));  // error word of the tcgen05 GEMM
+  return AGB_OK;
+}
+
+agb_status agb_cisd_set_fock(agb_cisd_plan* P, const void* F_SO, const double* eps_so, void* stream) {
+  AGB_ARG_CHECK(P && P->ws, "set_fock: plan without workspace");
+  AGB_ARG_CHECK(F_SO && eps_so, "set_fock: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  int* flag = (int*)((char*)P->gemm_scratch + 128);  // scratch word, consumed synchronously below
+  AGB_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+  int64_t nn = P->nso * P->nso;
+  fock_extract_kernel<<<grid_for(nn, 256), 256, 0, st>>>((const z64*)F_SO, eps_so, P->o, P->v,
+                                                          P->singles ? P->FvoT : nullptr, P->Foo, P->Fvv,
+                                                          P->singles ? P->EW : nullptr, P->eps, flag);
+  AGB_LAUNCH_CHECK();
+  int h = 0;
+  AGB_CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  AGB_CUDA_TRY(cudaStreamSynchronize(st));
+  P->f_diag = (h == 0);
+  return AGB_OK;
+}
+
+agb_status agb_cisd_blocks_from_mo(agb_cisd_plan* P, const void* ERI_MO, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && ERI_MO, "blocks_from_mo: bad argument");
+  SrcMO s{(const z64*)ERI_MO, P->nso / 2};
+  for (int id = 0; id < B_COUNT; ++id)
+    if (block_needed(P, id)) AGB_STATUS_TRY(launch_build(P, id, s, s, (cudaStream_t)stream));
+  return AGB_OK;
+}
+
+agb_status agb_cisd_blocks_from_so(agb_cisd_plan* P, const void* ERI_SO, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && ERI_SO, "blocks_from_so: bad argument");
+  SrcSO s{(const z64*)ERI_SO, P->nso};
+  for (int id = 0; id < B_COUNT; ++id)
+    if (block_needed(P, id)) AGB_STATUS_TRY(launch_build(P, id, s, s, (cudaStream_t)stream));
+  return AGB_OK;
+}
+
+static int64_t rlen(const agb_cisd_plan* P, char c) { return c == 'o' ? P->o : P->v; }
+static int roff(const agb_cisd_plan* P, char c) { return c == 'o' ? 0 : P->o; }
+
+size_t agb_cisd_factor_scratch_bytes(const agb_cisd_plan* P, int64_t naux) {
+  size_t fac = sizeof(z64) * (size_t)(P->nso * P->nso * naux) + 4 * 256;
+  size_t best = 0;
+  for (int id = 0; id < B_COUNT; ++id) {
+    if (!block_needed(P, id)) continue;
+    const char* r = kBlockRanges[id];
+    // direct (X Z | Y W), exchange (X W | Y Z)
+    size_t d = align256(sizeof(z64) * rlen(P, r[0]) * rlen(P, r[2]) * rlen(P, r[1]) * rlen(P, r[3]));
+    bool same = (r[2] == r[3]);
+    size_t e = same ? 0 : align256(sizeof(z64) * rlen(P, r[0]) * rlen(P, r[3]) * rlen(P, r[1]) * rlen(P, r[2]));
+    if (d + e > best) best = d + e;
+  }
+  return fac + best + 256;
+}
+
+agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* P, const void* Bf, int64_t naux, void* scratch,
+                                        size_t scratch_bytes, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && Bf && naux > 0, "blocks_from_factors: bad argument");
+  if (!scratch || scratch_bytes < agb_cisd_factor_scratch_bytes(P, naux)) {
+    agb_set_error_message("blocks_from_factors: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  // sub-factors Bsub_XY[(x,y)][L] for XY in {oo, ov, vo, vv}
+  z64* sub[2][2];
+  size_t off = 0;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      char ca = a ? 'v' : 'o', cb = b ? 'v' : 'o';
+      int64_t nx = rlen(P, ca), ny = rlen(P, cb);
+      sub[a][b] = (z64*)(base + off);
+      off += align256(sizeof(z64) * nx * ny * naux);
+      extract_factor_kernel<<<grid_for(nx * ny * naux, 256), 256, 0, st>>>(
+          (const z64*)Bf, naux, P->nso, roff(P, ca), (int)nx, roff(P, cb), (int)ny, sub[a][b]);
+      AGB_LAUNCH_CHECK();
+    }
+  char* chem_base = base + off;
+  auto chem_block = [&](char c0, char c1, char c2, char c3, z64* out) -> agb_status {
+    // (c0 c1 | c2 c3) = sum_L Bsub_{c0c1}[(x,y)][L] * Bsub_{c2c3}[(z,w)][L]
+    const z64* A = sub[c0 == 'v'][c1 == 'v'];
+    const z64* B = sub[c2 == 'v'][c3 == 'v'];
+    int64_t M = rlen(P, c0) * rlen(P, c1), N = rlen(P, c2) * rlen(P, c3);
+    return zgemm_ex(M, N, naux, zmk(1, 0), A, naux, 1, 0, B, 1, naux, 0, zmk(0, 0), out, N,
+                    (char*)P->gemm_scratch + 256, P->gemm_scratch_bytes - 256, st);
+  };
+  for (int id = 0; id < B_COUNT; ++id) {
+    if (!block_needed(P, id)) continue;
+    const char* r = kBlockRanges[id];
+    z64* cd = (z64*)chem_base;
+    AGB_STATUS_TRY(chem_block(r[0], r[2], r[1], r[3], cd));
+    SrcChem sd{cd, roff(P, r[0]), roff(P, r[2]), roff(P, r[1]), roff(P, r[3]),
+               rlen(P, r[2]), rlen(P, r[1]), rlen(P, r[3])};
+    SrcChem se = sd;
+    if (r[2] != r[3]) {
+      z64* ce = (z64*)(chem_base + align256(sizeof(z64) * rlen(P, r[0]) * rlen(P, r[2]) * rlen(P, r[1]) *
+                                            rlen(P, r[3])));
+      AGB_STATUS_TRY(chem_block(r[0], r[3], r[1], r[2], ce));
+      se = SrcChem{ce, roff(P, r[0]), roff(P, r[3]), roff(P, r[1]), roff(P, r[2]),
+                   rlen(P, r[3]), rlen(P, r[1]), rlen(P, r[2])};
+    }
+    AGB_STATUS_TRY(launch_build(P, id, sd, se, st));
+  }
+  return AGB_OK;
+}
+
+agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double E_re, double E_im, int flags, void* rv,
+                             void* stream) {
+  AGB_ARG_CHECK(P && P->ws && tv && rv, "residual: bad argument");
+  AGB_ARG_CHECK(!P->mp2_only, "residual: plan created with AGB_PLAN_MP2");
+  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || prec == AGB_PREC_TF32X3, "residual: unknown precision");
+  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || P->mixed, "residual: plan created without AGB_PLAN_MIXED");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int o = P->o, v = P->v;
+  const int64_t ov = P->ov, po = P->po, pv = P->pv, n1 = P->n1;
+  const z64* t1 = (const z64*)tv;
+  const z64* t2p = t1 + n1;
+  z64* r1 = (z64*)rv;
+  z64* r2p = r1 + n1;
+  const z64 one = zmk(1, 0), zero = zmk(0, 0);
+  const z64 E = zmk(E_re, E_im);
+  const bool need_hq = P->singles || !P->f_diag;
+
+  unpack_ring_kernel<<<grid_for(ov * ov, 256), 256, 0, st>>>(t2p, o, v, pv, P->Tring);
+  AGB_LAUNCH_CHECK();
+  if (need_hq) {
+    unpack_h_kernel<<<grid_for((int64_t)o * o * pv, 256), 256, 0, st>>>(t2p, o, pv, P->t2h);
+    AGB_LAUNCH_CHECK();
+    unpack_q_kernel<<<grid_for(po * v * v, 256), 256, 0, st>>>(t2p, po, v, pv, P->t2q);
+    AGB_LAUNCH_CHECK();
+  }
+
+  if (P->singles) {
+    // r1 = F_ai - F_ji t1_ja + F_ab t1_ib + <ja||bi> t1_jb + F_jb t2_ijab + 1/2 <aj||cb> t2_ijcb
+    //      - 1/2 <kj||ib> t2_kjab - E t1                                    (apyib/ci_wfn.py:309-316)
+    r1_init_kernel<<<grid_for(n1, 256), 256, 0, st>>>((flags & AGB_RES_CONST) ? P->FvoT : nullptr, n1, r1);
+    AGB_LAUNCH_CHECK();
+    AGB_STATUS_TRY(gemm(P, prec, o, v, o, zmk(-1, 0), P->Foo, 1, o, t1, v, 1, one, r1, v, st));
+    AGB_STATUS_TRY(gemm(P, prec, o, v, v, one, t1, v, 1, P->Fvv, 1, v, one, r1, v, st));
+    AGB_STATUS_TRY(zgemv(ov, ov, one, P->VT, ov, t1, one, r1, st));
+    AGB_STATUS_TRY(zgemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
+    AGB_STATUS_TRY(gemm(P, prec, o, v, (int64_t)o * pv, one, P->t2h, (int64_t)o * pv, 1, P->WvovvH, 1,
+                        (int64_t)o * pv, one, r1, v, st));
+    AGB_STATUS_TRY(gemm(P, prec, o, v, po * v, one, P->WooovP, po * v, 1, P->t2q, v, 1, one, r1, v, st));
+    if (flags & AGB_RES_ETERM) {
+      axpy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(n1, zneg(E), t1, r1);
+      AGB_LAUNCH_CHECK();
+    }
+    // Zq[p(ij)][b][a] = sum_k <kb||ij> t1[k,a];  Yh[i][j][p(ab)] = sum_c t1[i,c] <ab||cj>
+    AGB_STATUS_TRY(gemm(P, prec, po * v, v, o, one, P->WovooP, o, 1, t1, v, 1, zero, P->Zq, v, st));
+    AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, v, one, t1, v, 1, P->WvvvoP, (int64_t)o * pv, 1, zero, P->Yh,
+                        (int64_t)o * pv, st));
+  }
+  // ladders: PQ = sum_{k<l} <kl||ij> t2p[kl,ab] + sum_{c<d} t2p[ij,cd] <ab||cd>
+  AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st));
+  AGB_STATUS_TRY(gemm(P, prec, po, pv, pv, one, t2p, pv, 1, P->Wvp, 1, pv, one, P->PQ, pv, st));
+  // rings: X[(i,a),(j,b)] = sum_(k,c) t2[i,k,a,c] <kb||cj>
+  AGB_STATUS_TRY(gemm(P, prec, ov, ov, ov, one, P->Tring, ov, 1, P->VT, 1, ov, zero, P->X, ov, st));
+  if (!P->f_diag) {
+    AGB_STATUS_TRY(gemm(P, prec, po * v, v, v, one, P->t2q, v, 1, P->Fvv, 1, v, zero, P->Gq, v, st));
+    AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, o, one, P->Foo, 1, o, P->t2h, (int64_t)o * pv, 1, zero, P->H2h,
+                        (int64_t)o * pv, st));
+  }
+  if (po > 0 && pv > 0) {
+    AsmArgs A;
+    A.o = o; A.v = v; A.ov = ov; A.po = po; A.pv = pv; A.opairs = P->opairs;
+    A.R0p = P->R0p; A.PQ = P->PQ; A.X = P->X; A.Zq = P->Zq; A.Yh = P->Yh; A.Gq = P->Gq; A.H2h = P->H2h;
+    A.t2p = t2p; A.eps = P->eps; A.Foo = P->Foo; A.Fvv = P->Fvv; A.E = E;
+    A.use_const = (flags & AGB_RES_CONST) != 0; A.use_e = (flags & AGB_RES_ETERM) != 0;
+    A.singles = P->singles; A.f_diag = P->f_diag; A.r2p = r2p;
+    int nt = (v + TS - 1) / TS;
+    dim3 grid(nt * (nt + 1) / 2, (unsigned)po);
+    assemble_r2_kernel<<<grid, 256, 0, st>>>(A);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+agb_status agb_scratch_status(void* scratch, void* stream);
+
+agb_status agb_cisd_status(agb_cisd_plan* P, void* stream) {
+  AGB_ARG_CHECK(P && P->ws, "status: plan without workspace");
+  return agb_scratch_status(P->gemm_scratch, stream);
+}
+
+agb_status agb_cisd_update(agb_cisd_plan* P, const void* t, const void* r, void* t_out, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && t && r && t_out, "update: bad argument");
+  int64_t n = P->n1 + P->n2;
+  update_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(vdims_of(P), n, (const z64*)t, (const z64*)r,
+                                                                    (z64*)t_out);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status agb_cisd_guess(agb_cisd_plan* P, void* t, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && t, "guess: bad argument");
+  int64_t n = P->n1 + P->n2;
+  guess_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(vdims_of(P), n, P->FvoT, P->R0p, (z64*)t);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+size_t agb_vec_partials_bytes(int ny) { return sizeof(z64) * (size_t)kRedBlocks * (ny > 3 ? ny : 3); }
+
+agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x, const void* const* ys, int ny,
+                        void* out, void* partials, size_t partials_bytes, void* stream) {
+  AGB_ARG_CHECK(x && ys && out && ny >= 1 && ny <= kMaxVec, "vec_dots: bad argument");
+  if (!partials || partials_bytes < agb_vec_partials_bytes(ny)) {
+    agb_set_error_message("vec_dots: partials buffer too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  DotArgs A;
+  A.n1 = n1; A.n2 = n2; A.w1 = w1; A.w2 = w2; A.x = (const z64*)x; A.ny = ny;
+  for (int j = 0; j < kMaxVec; ++j) A.ys[j] = j < ny ? (const z64*)ys[j] : nullptr;
+  z64* part = (z64*)partials;
+  if (ny <= 4) dots_kernel<4><<<kRedBlocks, 256, 0, st>>>(A, part);
+  else if (ny <= 8) dots_kernel<8><<<kRedBlocks, 256, 0, st>>>(A, part);
+  else dots_kernel<16><<<kRedBlocks, 256, 0, st>>>(A, part);
+  AGB_LAUNCH_CHECK();
+  int nv = ny <= 4 ? 4 : (ny <= 8 ? 8 : 16);
+  // finish only the first ny of the nv slots (stride nv)
+  finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, (z64*)out);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status agb_cisd_combine(agb_cisd_plan* P, const void* const* ys, const double* coefs, int ny, const void* t_old,
+                            void* t_new, void* out3, void* partials, size_t partials_bytes, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && ys && coefs && t_old && t_new && out3, "combine: bad argument");
+  AGB_ARG_CHECK(ny >= 1 && ny <= kMaxVec, "combine: 1 <= ny <= 16");
+  if (!partials || partials_bytes < agb_vec_partials_bytes(3)) {
+    agb_set_error_message("combine: partials buffer too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  CombArgs A;
+  A.n1 = P->n1; A.n2 = P->n2; A.ny = ny;
+  for (int j = 0; j < kMaxVec; ++j) {
+    A.ys[j] = j < ny ? (const z64*)ys[j] : nullptr;
+    A.c[2 * j] = j < ny ? coefs[2 * j] : 0.0;
+    A.c[2 * j + 1] = j < ny ? coefs[2 * j + 1] : 0.0;
+  }
+  A.t_old = (const z64*)t_old; A.t_new = (z64*)t_new; A.ew = P->EW;
+  combine_kernel<<<kRedBlocks, 256, 0, st>>>(A, (z64*)partials);
+  AGB_LAUNCH_CHECK();
+  finish_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kRedBlocks, 3, (z64*)out3);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,374 @@
+// Spin-orbital expansion, amplitude pack/unpack, MP2_SO, the AO->MO
+// four-index transform and the one-pass J/K Fock build.
+#include "cisd_plan.h"
+
+namespace agb {
+
+agb_status zgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                    const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                    void* scratch, size_t scratch_bytes, cudaStream_t stream);
+agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
+                        int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                        void* scratch, size_t scratch_bytes, cudaStream_t stream);
+size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
+
+namespace {
+
+__global__ void f_so_kernel(const z64* __restrict__ F, int64_t n, z64* __restrict__ out) {
+  int64_t m = 2 * n, total = m * m;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p = e / m, q = e % m;
+    out[e] = ((p ^ q) & 1) ? zmk(0, 0) : F[(p >> 1) * n + (q >> 1)];
+  }
+}
+
+__global__ void eri_so_kernel(const z64* __restrict__ g, int64_t n0, int64_t n1, int64_t n2, int64_t n3,
+                              z64* __restrict__ out) {
+  int64_t m1 = 2 * n1, m2 = 2 * n2, m3 = 2 * n3;
+  int64_t total = 2 * n0 * m1 * m2 * m3;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t s = e % m3, rest = e / m3;
+    int64_t r = rest % m2; rest /= m2;
+    int64_t q = rest % m1, p = rest / m1;
+    z64 val = zmk(0, 0);
+    if (!((p ^ q) & 1) && !((r ^ s) & 1)) val = g[(((p >> 1) * n1 + (q >> 1)) * n2 + (r >> 1)) * n3 + (s >> 1)];
+    out[e] = val;
+  }
+}
+
+__device__ __forceinline__ int sgnp(int x, int y) { return x < y ? 1 : (x > y ? -1 : 0); }
+
+// full t2[i][j][a][b] from packed
+__global__ void unpack_full_kernel(const z64* __restrict__ t2p, int o, int v, int64_t pv, z64* __restrict__ t2) {
+  int64_t vv = (int64_t)v * v, total = (int64_t)o * o * vv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ij = e / vv, ab = e % vv;
+    int i = (int)(ij / o), j = (int)(ij % o), a = (int)(ab / v), b = (int)(ab % v);
+    int s = sgnp(i, j) * sgnp(a, b);
+    z64 val = zmk(0, 0);
+    if (s) {
+      val = t2p[pair_index(min(i, j), max(i, j), o) * pv + pair_index(min(a, b), max(a, b), v)];
+      if (s < 0) val = zneg(val);
+    }
+    t2[e] = val;
+  }
+}
+
+__global__ void pack_kernel(const z64* __restrict__ t2, int o, int v, int64_t po, int64_t pv,
+                            const int2* __restrict__ opairs, const int2* __restrict__ vpairs, z64* __restrict__ t2p) {
+  int64_t total = po * pv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int2 ij = opairs[e / pv], ab = vpairs[e % pv];
+    t2p[e] = t2[(((int64_t)ij.x * o + ij.y) * v + ab.x) * v + ab.y];
+  }
+}
+
+__global__ void copy_kernel(const z64* __restrict__ src, int64_t n, z64* __restrict__ dst) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    dst[e] = src[e];
+}
+
+__device__ __forceinline__ z64 warp_sum(z64 s) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, off);
+    s.y += __shfl_xor_sync(0xffffffffu, s.y, off);
+  }
+  return s;
+}
+
+constexpr int kMp2Blocks = 152 * 4;
+
+// t2p = <ab||ij>_p * (1/D), partial[b] = sum t2p * <ij||ab>_p
+__global__ void __launch_bounds__(256) mp2_kernel(const z64* __restrict__ R0p, const z64* __restrict__ Wop,
+                                                  const double* __restrict__ eps, const int2* __restrict__ opairs,
+                                                  const int2* __restrict__ vpairs, int o, int64_t pv, int64_t n2,
+                                                  z64* __restrict__ t2p, z64* __restrict__ partial) {
+  z64 acc = zmk(0, 0);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n2; e += (int64_t)gridDim.x * blockDim.x) {
+    int2 ij = opairs[e / pv], ab = vpairs[e % pv];
+    double inv = 1.0 / (eps[ij.x] + eps[ij.y] - eps[o + ab.x] - eps[o + ab.y]);
+    z64 num = R0p[e];
+    z64 t = zmk(num.x * inv, num.y * inv);
+    t2p[e] = t;
+    acc = zadd(acc, zmul(Wop[e], t));
+  }
+  __shared__ z64 sh[32];
+  acc = warp_sum(acc);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = acc;
+  __syncthreads();
+  if (w == 0) {
+    acc = lane < (int)(blockDim.x >> 5) ? sh[lane] : zmk(0, 0);
+    acc = warp_sum(acc);
+    if (lane == 0) partial[blockIdx.x] = acc;
+  }
+}
+
+__global__ void sum_partials_kernel(const z64* __restrict__ partial, int n, z64* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    z64 s = zmk(0, 0);
+    for (int b = 0; b < n; ++b) s = zadd(s, partial[b]);
+    *out = s;
+  }
+}
+
+// ---- real FP64 GEMM (first AO->MO quarter step: real ERIs x interleaved complex C)
+constexpr int DBM = 64, DBN = 64, DBK = 16;
+__global__ void __launch_bounds__(256) dgemm_kernel(int64_t M, int64_t N, int64_t K, const double* __restrict__ A,
+                                                    int64_t sAm, int64_t sAk, const double* __restrict__ B,
+                                                    int64_t sBk, int64_t sBn, double* __restrict__ C, int64_t ldc) {
+  __shared__ double As[DBK][DBM + 1];
+  __shared__ double Bs[DBK][DBN + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, tid = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.y * DBM, n0 = (int64_t)blockIdx.x * DBN;
+  double acc[4][4] = {};
+  const bool a_kfast = (sAk == 1), b_nfast = (sBn == 1);
+  for (int64_t k0 = 0; k0 < K; k0 += DBK) {
+#pragma unroll
+    for (int r = 0; r < (DBM * DBK) / 256; ++r) {
+      int idx = tid + 256 * r, m, k;
+      if (a_kfast) { k = idx % DBK; m = idx / DBK; } else { m = idx % DBM; k = idx / DBM; }
+      int64_t gm = m0 + m, gk = k0 + k;
+      As[k][m] = (gm < M && gk < K) ? A[gm * sAm + gk * sAk] : 0.0;
+    }
+#pragma unroll
+    for (int r = 0; r < (DBN * DBK) / 256; ++r) {
+      int idx = tid + 256 * r, n, k;
+      if (b_nfast) { n = idx % DBN; k = idx / DBN; } else { k = idx % DBK; n = idx / DBK; }
+      int64_t gn = n0 + n, gk = k0 + k;
+      Bs[k][n] = (gn < N && gk < K) ? B[gk * sBk + gn * sBn] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < DBK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int64_t gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t gn = n0 + tx + 16 * j;
+      if (gn < N) C[gm * ldc + gn] = acc[i][j];
+    }
+  }
+}
+
+__global__ void conj_kernel(const z64* __restrict__ src, int64_t n, z64* __restrict__ dst) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    dst[e] = zconj(src[e]);
+}
+
+// ---- J/K: one pass over real (mn|ls).  CTA per m; for each x the plane e[x][y][z] = (mx|yz)
+// contributes J[m][x] += sum_yz e D[y][z] and K[m][y] += sum_z e D[x][z].
+constexpr int JK_THREADS = 512;
+__global__ void __launch_bounds__(JK_THREADS) jk_kernel(const double* __restrict__ eri, int n,
+                                                        const z64* __restrict__ D, const z64* __restrict__ h,
+                                                        double scale, z64* __restrict__ F) {
+  extern __shared__ z64 ksh[];  // K[m][y], n entries
+  __shared__ z64 red[JK_THREADS / 32];
+  const int m = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = JK_THREADS / 32;
+  for (int y = threadIdx.x; y < n; y += JK_THREADS) ksh[y] = zmk(0, 0);
+  __syncthreads();
+  const int64_t nn = (int64_t)n * n;
+  const double* base = eri + (int64_t)m * n * nn;
+  for (int x = 0; x < n; ++x) {
+    const double* plane = base + (int64_t)x * nn;
+    z64 jacc = zmk(0, 0);
+    for (int y = w; y < n; y += nw) {
+      z64 kacc = zmk(0, 0);
+      const double* row = plane + (int64_t)y * n;
+      for (int z = lane; z < n; z += 32) {
+        double e = row[z];
+        z64 dyz = D[(int64_t)y * n + z], dxz = D[(int64_t)x * n + z];
+        jacc.x = fma(e, dyz.x, jacc.x); jacc.y = fma(e, dyz.y, jacc.y);
+        kacc.x = fma(e, dxz.x, kacc.x); kacc.y = fma(e, dxz.y, kacc.y);
+      }
+      kacc = warp_sum(kacc);
+      if (lane == 0) ksh[y] = zadd(ksh[y], kacc);
+    }
+    jacc = warp_sum(jacc);
+    if (lane == 0) red[w] = jacc;
+    __syncthreads();
+    if (w == 0) {
+      z64 s = lane < nw ? red[lane] : zmk(0, 0);
+      s = warp_sum(s);
+      if (lane == 0) {
+        // F[m][x] = h + scale*(2J - K) ; K added after the loop
+        z64 hv = h ? h[(int64_t)m * n + x] : zmk(0, 0);
+        F[(int64_t)m * n + x] = zmk(hv.x + 2.0 * scale * s.x, hv.y + 2.0 * scale * s.y);
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  for (int y = threadIdx.x; y < n; y += JK_THREADS) {
+    z64 f = F[(int64_t)m * n + y];
+    F[(int64_t)m * n + y] = zmk(f.x - scale * ksh[y].x, f.y - scale * ksh[y].y);
+  }
+}
+
+}  // namespace
+}  // namespace agb
+
+using namespace agb;
+
+extern "C" {
+
+agb_status agb_compute_f_so(const void* F_MO, int64_t n, void* F_SO, void* stream) {
+  AGB_ARG_CHECK(F_MO && F_SO && n >= 0, "compute_f_so: bad argument");
+  if (n == 0) return AGB_OK;
+  f_so_kernel<<<grid_for(4 * n * n, 256), 256, 0, (cudaStream_t)stream>>>((const z64*)F_MO, n, (z64*)F_SO);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status agb_compute_eri_so(const void* ERI_MO, int64_t n0, int64_t n1, int64_t n2, int64_t n3, void* ERI_SO,
+                              void* stream) {
+  AGB_ARG_CHECK(ERI_MO && ERI_SO && n0 >= 0 && n1 >= 0 && n2 >= 0 && n3 >= 0, "compute_eri_so: bad argument");
+  int64_t total = 16 * n0 * n1 * n2 * n3;
+  if (total == 0) return AGB_OK;
+  eri_so_kernel<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>((const z64*)ERI_MO, n0, n1, n2, n3,
+                                                                        (z64*)ERI_SO);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status agb_cisd_unpack(agb_cisd_plan* P, const void* t, void* t1, void* t2, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && t, "unpack: bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (t1 && P->n1) {
+    copy_kernel<<<grid_for(P->n1, 256), 256, 0, st>>>((const z64*)t, P->n1, (z64*)t1);
+    AGB_LAUNCH_CHECK();
+  }
+  if (t2) {
+    int64_t total = (int64_t)P->o * P->o * P->v * P->v;
+    unpack_full_kernel<<<grid_for(total, 256), 256, 0, st>>>((const z64*)t + P->n1, P->o, P->v, P->pv, (z64*)t2);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+agb_status agb_cisd_pack(agb_cisd_plan* P, const void* t1, const void* t2, void* t, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && t && t2 && (t1 || P->n1 == 0), "pack: bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (P->n1) {
+    copy_kernel<<<grid_for(P->n1, 256), 256, 0, st>>>((const z64*)t1, P->n1, (z64*)t);
+    AGB_LAUNCH_CHECK();
+  }
+  if (P->n2) {
+    pack_kernel<<<grid_for(P->n2, 256), 256, 0, st>>>((const z64*)t2, P->o, P->v, P->po, P->pv, P->opairs, P->vpairs,
+                                                      (z64*)t + P->n1);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+agb_status agb_mp2_so(agb_cisd_plan* P, void* t, void* E_out, void* partials, size_t partials_bytes, void* stream) {
+  AGB_ARG_CHECK(P && P->ws && t && E_out, "mp2_so: bad argument");
+  if (!partials || partials_bytes < sizeof(z64) * kMp2Blocks) {
+    agb_set_error_message("mp2_so: partials buffer too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (P->n1) {
+    AGB_CUDA_TRY(cudaMemsetAsync(t, 0, sizeof(z64) * P->n1, st));
+  }
+  mp2_kernel<<<kMp2Blocks, 256, 0, st>>>(P->R0p, P->EW + P->n1, P->eps, P->opairs, P->vpairs, P->o, P->pv, P->n2,
+                                         (z64*)t + P->n1, (z64*)partials);
+  AGB_LAUNCH_CHECK();
+  sum_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo) {
+  int64_t big = nbf * nbf * nbf * nmo;
+  int64_t mid = nbf * nbf * nmo * nmo;
+  int64_t a = big > mid ? big : mid;
+  size_t s = sizeof(z64) * (size_t)a;
+  s = (s + 255) & ~(size_t)255;
+  size_t gs = (size_t)64 << 20;
+  size_t t1 = cgemm_tf32x3_scratch(nbf * nbf * nmo, nmo, nbf);
+  size_t t2 = cgemm_tf32x3_scratch(nbf * nmo * nmo, nmo, nbf);
+  size_t t3 = cgemm_tf32x3_scratch(nmo * nmo * nmo, nmo, nbf);
+  if (t1 > gs) gs = t1;
+  if (t2 > gs) gs = t2;
+  if (t3 > gs) gs = t3;
+  return 2 * s + sizeof(z64) * (size_t)(nbf * nmo) + 256 + gs + 256;
+}
+
+// Each quarter step contracts the leading AO index and appends the new MO index
+// last: (m n l s) -> (n l s p) -> (l s p q) -> (s p q r) -> (p q r s).
+agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t nmo, void* ERI_MO, void* scratch,
+                     size_t scratch_bytes, int precision, void* stream) {
+  AGB_ARG_CHECK(ERI_AO && C && ERI_MO && nbf > 0 && nmo > 0, "ao2mo: bad argument");
+  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_TF32X3, "ao2mo: unknown precision");
+  if (!scratch || scratch_bytes < agb_ao2mo_scratch_bytes(nbf, nmo)) {
+    agb_set_error_message("ao2mo: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int64_t big = nbf * nbf * nbf * nmo, mid = nbf * nbf * nmo * nmo;
+  size_t s = sizeof(z64) * (size_t)(big > mid ? big : mid);
+  s = (s + 255) & ~(size_t)255;
+  char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  z64* Y1 = (z64*)base;
+  z64* Y2 = (z64*)(base + s);
+  z64* Cc = (z64*)(base + 2 * s);
+  char* gs = base + 2 * s + ((sizeof(z64) * nbf * nmo + 255) & ~(size_t)255);
+  size_t gs_bytes = scratch_bytes - (size_t)(gs - (char*)scratch);
+  if (precision == AGB_PREC_TF32X3) AGB_CUDA_TRY(cudaMemsetAsync(gs, 0, 256, st));  // GEMM status word
+  conj_kernel<<<grid_for(nbf * nmo, 256), 256, 0, st>>>((const z64*)C, nbf * nmo, Cc);
+  AGB_LAUNCH_CHECK();
+  // step 1 (real x complex as a real GEMM on interleaved columns): Y1[(n l s)][p] = sum_m (mn|ls) C*[m,p]
+  {
+    int64_t M = nbf * nbf * nbf, N = 2 * nmo, K = nbf;
+    dim3 grid((unsigned)((N + DBN - 1) / DBN), (unsigned)((M + DBM - 1) / DBM));
+    AGB_ARG_CHECK((M + DBM - 1) / DBM <= 65535, "ao2mo: nbf too large");
+    dgemm_kernel<<<grid, 256, 0, st>>>(M, N, K, ERI_AO, 1, M, (const double*)Cc, N, 1, (double*)Y1, N);
+    AGB_LAUNCH_CHECK();
+  }
+  auto step = [&](const z64* T, int64_t Mrest, const z64* Cop, z64* out) -> agb_status {
+    // out[(rest)][q] = sum_k T[k][(rest)] Cop[k][q]
+    if (precision == AGB_PREC_TF32X3)
+      return cgemm_tf32x3(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, 0, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
+                          gs_bytes, st);
+    return zgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, 0, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs, gs_bytes,
+                    st);
+  };
+  // step 2: Y2[(l s p)][q] = sum_n Y1[n][(l s p)] C[n,q]
+  AGB_STATUS_TRY(step(Y1, nbf * nbf * nmo, (const z64*)C, Y2));
+  // step 3: Y1[(s p q)][r] = sum_l Y2[l][(s p q)] C*[l,r]
+  AGB_STATUS_TRY(step(Y2, nbf * nmo * nmo, Cc, Y1));
+  // step 4: ERI_MO[(p q r)][s] = sum_s' Y1[s'][(p q r)] C[s',s]
+  AGB_STATUS_TRY(step(Y1, nmo * nmo * nmo, (const z64*)C, (z64*)ERI_MO));
+  return AGB_OK;
+}
+
+agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale, void* F,
+                       void* stream) {
+  AGB_ARG_CHECK(ERI_AO && D && F && nbf > 0 && nbf < 65536, "jk_fock: bad argument");
+  size_t sh = sizeof(z64) * (size_t)nbf;
+  AGB_ARG_CHECK(sh <= 200 * 1024, "jk_fock: nbf too large for the shared K row");
+  if (sh > 48 * 1024) AGB_CUDA_TRY(cudaFuncSetAttribute(jk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  jk_kernel<<<(unsigned)nbf, JK_THREADS, sh, (cudaStream_t)stream>>>(ERI_AO, (int)nbf, (const z64*)D,
+                                                                     (const z64*)h, scale, (z64*)F);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+}  // extern "C"

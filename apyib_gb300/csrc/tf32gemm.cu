@@ -1,0 +1,509 @@
+// Complex GEMM as complex-FP32 with 3xTF32 split products on the sm_103a
+// tensor cores (tcgen05.mma kind::tf32, accumulators in TMEM, operands staged
+// by TMA with 64-byte swizzle).
+//
+//   x = x_hi + x_lo,  x_hi = tf32(x), x_lo = tf32(x - x_hi)   (|x - x_hi - x_lo| ~ 2^-22 |x|)
+//   a*b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi
+//   Re(C) += Ar Br - Ai Bi,  Im(C) += Ar Bi + Ai Br   (4M; the minus via the MMA negate-A bit)
+//
+// Operands arrive in FP64 (complex128, arbitrary strides); a prep kernel
+// writes four K-major FP32 planes per operand (re_hi, re_lo, im_hi, im_lo),
+// zero-padded to the tile grid.  One CTA per 128x128 output tile (or per
+// tile and K split): warp 0 issues TMA loads, warp 1 issues the MMAs from one
+// thread, warps 2-5 drain the two TMEM accumulators (Re in columns 0-127, Im
+// in 128-255) and write FP64 results.  Every mbarrier wait is bounded; on
+// timeout the kernel records an error word and returns after releasing TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "common.cuh"
+
+namespace agb {
+
+agb_status zgemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                 const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                 cudaStream_t stream);
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 16;   // BK in fp32 elements (64 bytes)
+constexpr int STAGES = 3;
+constexpr int PLANE_TILE_BYTES = 128 * BK * 4;               // 8 KB
+constexpr int STAGE_BYTES = 8 * PLANE_TILE_BYTES;            // 4 A planes + 4 B planes = 64 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 192;
+constexpr unsigned TMEM_COLS = 256;
+constexpr long long kWaitCycles = 8000000000LL;  // ~4 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: returns false (and flags the error) when the deadline passes.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, volatile int* abort_flag,
+                                          int code) {
+  long long start = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort_flag) return false;
+    if (clock64() - start > kWaitCycles) {
+      atomicExch(err, code);
+      *abort_flag = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);          // start address
+  d |= (uint64_t)1 << 16;                           // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;                  // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                           // descriptor version
+  d |= (uint64_t)4 << 61;                           // SWIZZLE_64B
+  return d;
+}
+
+// Instruction descriptor: D=F32, A=B=TF32, K-major both, N=128, M=128.
+__host__ __device__ constexpr uint32_t make_idesc(bool negA) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct GemmParams {
+  int64_t M, N;
+  int nkb;          // k-blocks per split
+  int nkb_total;
+  z64 alpha, beta;
+  z64* C;
+  int64_t ldc;
+  z64* partial;     // split-K partials [splits][M][N] or null
+  int* err;
+  int64_t rowsA, rowsB;  // padded rows per plane
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   GemmParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty_bar = full_bar + STAGES;
+  uint64_t* tmem_bar = empty_bar + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(tmem_bar + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile_n = blockIdx.x, tile_m = blockIdx.y, split = blockIdx.z;
+  const int kb0 = split * p.nkb;
+  int nk = p.nkb_total - kb0;
+  if (nk > p.nkb) nk = p.nkb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(tmem_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        int s = kb % STAGES;
+        uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+        int kx = (kb0 + kb) * BK;
+        for (int pl = 0; pl < 4; ++pl) {
+          tma_load_2d(st + pl * PLANE_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
+          tma_load_2d(st + (4 + pl) * PLANE_TILE_BYTES, &mapB, &full_bar[s], kx,
+                      (int)(pl * p.rowsB + tile_n * BN));
+        }
+        issued = kb + 1;
+      }
+      // On abort, wait (bounded) for loads still in flight before the CTA exits.
+      if (*abort_flag) {
+        for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb) {
+          long long t0 = clock64();
+          while (!mbar_try_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u) &&
+                 clock64() - t0 < kWaitCycles) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t id_pos = make_idesc(false), id_neg = make_idesc(true);
+      const uint32_t d_re = tmem_base, d_im = tmem_base + BN;
+      bool ok = true;
+      for (int kb = 0; kb < nk; ++kb) {
+        int s = kb % STAGES;
+        uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        // planes: 0 Ar_hi 1 Ar_lo 2 Ai_hi 3 Ai_lo | 4 Br_hi 5 Br_lo 6 Bi_hi 7 Bi_lo
+#pragma unroll
+        for (int ks = 0; ks < BK / 8; ++ks) {
+          uint64_t a[4], b[4];
+#pragma unroll
+          for (int pl = 0; pl < 4; ++pl) {
+            a[pl] = make_desc(st + pl * PLANE_TILE_BYTES + ks * 32);
+            b[pl] = make_desc(st + (4 + pl) * PLANE_TILE_BYTES + ks * 32);
+          }
+          uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
+          // Re: Ar Br - Ai Bi
+          mma_tf32(d_re, a[1], b[0], id_pos, acc0);
+          mma_tf32(d_re, a[0], b[1], id_pos, 1u);
+          mma_tf32(d_re, a[0], b[0], id_pos, 1u);
+          mma_tf32(d_re, a[3], b[2], id_neg, 1u);
+          mma_tf32(d_re, a[2], b[3], id_neg, 1u);
+          mma_tf32(d_re, a[2], b[2], id_neg, 1u);
+          // Im: Ar Bi + Ai Br
+          mma_tf32(d_im, a[1], b[2], id_pos, acc0);
+          mma_tf32(d_im, a[0], b[3], id_pos, 1u);
+          mma_tf32(d_im, a[0], b[2], id_pos, 1u);
+          mma_tf32(d_im, a[3], b[0], id_pos, 1u);
+          mma_tf32(d_im, a[2], b[1], id_pos, 1u);
+          mma_tf32(d_im, a[2], b[0], id_pos, 1u);
+        }
+        mma_commit(&empty_bar[s]);   // frees the stage once these MMAs finish
+      }
+      if (ok) mma_commit(tmem_bar);
+    }
+  } else {
+    // Epilogue warps 2..5: TMEM lane quadrant = warp % 4
+    const int q = warp & 3;
+    int okw = 0;
+    if (lane == 0) okw = mbar_wait(tmem_bar, 0, p.err, abort_flag, 3) ? 1 : 0;
+    const bool ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && nk > 0) {
+      const int64_t m = (int64_t)tile_m * BM + q * 32 + lane;
+      const bool use_beta = (p.beta.x != 0.0 || p.beta.y != 0.0);
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        float vr[32], vi[32];
+        uint32_t tl = tmem_base + ((uint32_t)(q * 32) << 16) + c * 32;
+        tmem_ld32(tl, vr);
+        tmem_ld32(tl + BN, vi);
+        if (m < p.M) {
+          int64_t n0 = (int64_t)tile_n * BN + c * 32;
+          if (p.partial) {
+            z64* dst = p.partial + ((int64_t)split * p.M + m) * p.N + n0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (n0 + j < p.N) dst[j] = zmk((double)vr[j], (double)vi[j]);
+          } else {
+            z64* dst = p.C + m * p.ldc + n0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (n0 + j < p.N) {
+                z64 out = zmul(p.alpha, zmk((double)vr[j], (double)vi[j]));
+                if (use_beta) out = zadd(out, zmul(p.beta, dst[j]));
+                dst[j] = out;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS));
+  }
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// planes[4][rows][Kp]: re_hi, re_lo, im_hi, im_lo of X(row, k) = src[row*s_row + k*s_k], zero padded.
+__global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t K, int64_t s_row, int64_t s_k,
+                            int conj, int64_t rows_pad, int64_t Kp, float* __restrict__ planes) {
+  __shared__ z64 tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
+  for (int i = ty; i < 32; i += 8) {
+    int64_t r, k;
+    if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
+    z64 v = zmk(0, 0);
+    if (r < nrows && k < K) v = src[r * s_row + k * s_k];
+    if (conj) v.y = -v.y;
+    if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
+  }
+  __syncthreads();
+  const int64_t plane = rows_pad * Kp;
+  for (int i = ty; i < 32; i += 8) {
+    int64_t r = r0 + i, k = k0 + tx;
+    if (r >= rows_pad || k >= Kp) continue;
+    z64 v = tile[i][tx];
+    float rh = tf32_rna(__double2float_rn(v.x));
+    float rl = tf32_rna(__double2float_rn(v.x - (double)rh));
+    float ih = tf32_rna(__double2float_rn(v.y));
+    float il = tf32_rna(__double2float_rn(v.y - (double)ih));
+    int64_t off = r * Kp + k;
+    planes[off] = rh;
+    planes[plane + off] = rl;
+    planes[2 * plane + off] = ih;
+    planes[3 * plane + off] = il;
+  }
+}
+
+__global__ void splitk_sum_kernel(const z64* __restrict__ partial, int splits, int64_t M, int64_t N, z64 alpha,
+                                  z64 beta, z64* C, int64_t ldc) {
+  int64_t total = M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    z64 s = zmk(0, 0);
+    for (int z = 0; z < splits; ++z) s = zadd(s, partial[(int64_t)z * total + e]);
+    int64_t m = e / N, n = e % N;
+    z64* c = C + m * ldc + n;
+    z64 out = zmul(alpha, s);
+    if (beta.x != 0.0 || beta.y != 0.0) out = zadd(out, zmul(beta, *c));
+    *c = out;
+  }
+}
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* ptr = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+  }
+  return fn;
+}
+
+bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
+  cuuint64_t strides[1] = {(cuuint64_t)(Kp * sizeof(float))};
+  cuuint32_t box[2] = {(cuuint32_t)BK, 128u};
+  cuuint32_t estr[2] = {1u, 1u};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+struct Layout {
+  int64_t Mp, Np, Kp, nkb;
+  int splits, nkb_split;
+  size_t offA, offB, offP, total;
+};
+
+Layout plan_layout(int64_t M, int64_t N, int64_t K, size_t cap) {
+  Layout L;
+  L.Mp = round_up(M, BM);
+  L.Np = round_up(N, BN);
+  L.Kp = round_up(K, BK);
+  L.nkb = L.Kp / BK;
+  L.offA = 256;
+  L.offB = L.offA + round_up((int64_t)(4 * L.Mp * L.Kp * sizeof(float)), 256);
+  size_t base_total = L.offB + round_up((int64_t)(4 * L.Np * L.Kp * sizeof(float)), 256);
+  L.offP = base_total;
+  // split K when the tile grid cannot fill the GPU
+  int64_t tiles = (L.Mp / BM) * (L.Np / BN);
+  int splits = 1;
+  if (tiles < 152 && L.nkb >= 16) {
+    int64_t want = (2 * 152 + tiles - 1) / tiles;
+    int64_t kmax = L.nkb / 8;
+    if (want > kmax) want = kmax;
+    if (want > 128) want = 128;
+    if (want < 1) want = 1;
+    splits = (int)want;
+  }
+  L.nkb_split = (int)((L.nkb + splits - 1) / splits);
+  L.splits = (int)((L.nkb + L.nkb_split - 1) / L.nkb_split);
+  size_t part = L.splits > 1 ? (size_t)L.splits * M * N * sizeof(z64) : 0;
+  if (cap && base_total + part > cap && L.splits > 1) {
+    // shrink splits to what fits
+    int64_t fit = (int64_t)((cap - base_total) / (M * N * sizeof(z64)));
+    if (fit < 2) fit = 1;
+    L.nkb_split = (int)((L.nkb + fit - 1) / fit);
+    L.splits = (int)((L.nkb + L.nkb_split - 1) / L.nkb_split);
+    part = L.splits > 1 ? (size_t)L.splits * M * N * sizeof(z64) : 0;
+  }
+  L.total = base_total + part;
+  return L;
+}
+
+}  // namespace
+
+size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K) {
+  if (M <= 0 || N <= 0 || K <= 0) return 256;
+  return plan_layout(M, N, K, 0).total;
+}
+
+agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
+                        int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                        void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  AGB_ARG_CHECK(M >= 0 && N >= 0 && K >= 0, "cgemm_tf32x3: negative size");
+  if (M == 0 || N == 0) return AGB_OK;
+  AGB_ARG_CHECK(A && B && C && scratch, "cgemm_tf32x3: null pointer");
+  AGB_ARG_CHECK(((uintptr_t)scratch & 255) == 0, "cgemm_tf32x3: scratch must be 256-byte aligned");
+  if (K == 0) {
+    // C = beta*C
+    return zgemm(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, stream);
+  }
+  Layout L = plan_layout(M, N, K, scratch_bytes);
+  if (scratch_bytes < L.total) {
+    agb_set_error_message("cgemm_tf32x3: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  AGB_ARG_CHECK(L.Np / BN <= 0x7fffffff && L.Mp / BM <= 65535, "cgemm_tf32x3: grid too large");
+  char* base = (char*)scratch;
+  int* err = (int*)base;
+  float* PA = (float*)(base + L.offA);
+  float* PB = (float*)(base + L.offB);
+  z64* part = L.splits > 1 ? (z64*)(base + L.offP) : nullptr;
+  {
+    dim3 g((unsigned)(L.Kp / 32 + (L.Kp % 32 ? 1 : 0)), (unsigned)(L.Mp / 32));
+    prep_kernel<<<g, 256, 0, stream>>>(A, M, K, sAm, sAk, conjA, L.Mp, L.Kp, PA);
+    AGB_LAUNCH_CHECK();
+    dim3 gb((unsigned)(L.Kp / 32 + (L.Kp % 32 ? 1 : 0)), (unsigned)(L.Np / 32));
+    prep_kernel<<<gb, 256, 0, stream>>>(B, N, K, sBn, sBk, conjB, L.Np, L.Kp, PB);
+    AGB_LAUNCH_CHECK();
+  }
+  CUtensorMap mA, mB;
+  if (!encode_planes(&mA, PA, 4 * L.Mp, L.Kp) || !encode_planes(&mB, PB, 4 * L.Np, L.Kp)) {
+    agb_set_error_message("cgemm_tf32x3: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
+    return AGB_ERR_CUDA;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_set = true;
+  }
+  GemmParams p;
+  p.M = M; p.N = N; p.nkb = L.nkb_split; p.nkb_total = (int)L.nkb;
+  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = part; p.err = err;
+  p.rowsA = L.Mp; p.rowsB = L.Np;
+  dim3 grid((unsigned)(L.Np / BN), (unsigned)(L.Mp / BM), (unsigned)L.splits);
+  tf32x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
+  AGB_LAUNCH_CHECK();
+  if (part) {
+    splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>(part, L.splits, M, N, alpha, beta, C, ldc);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+}  // namespace agb
+
+extern "C" {
+
+size_t agb_cgemm_tf32x3_scratch_bytes(int64_t M, int64_t N, int64_t K) { return agb::cgemm_tf32x3_scratch(M, N, K); }
+
+agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
+                            int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn, int conjB,
+                            double beta_re, double beta_im, void* C, int64_t ldc, void* scratch, size_t scratch_bytes,
+                            void* stream) {
+  return agb::cgemm_tf32x3(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
+                           (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
+                           scratch, scratch_bytes, (cudaStream_t)stream);
+}
+
+/* Reads and clears the error word a 3xTF32 GEMM keeps at the start of its scratch
+ * (non-zero: a bounded wait inside the kernel ran out). Synchronises the stream. */
+agb_status agb_scratch_status(void* scratch, void* stream) {
+  if (!scratch) return AGB_ERR_ARG;
+  int h = 0;
+  AGB_CUDA_TRY(cudaMemcpyAsync(&h, scratch, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  AGB_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (h != 0) {
+    AGB_CUDA_TRY(cudaMemsetAsync(scratch, 0, sizeof(int), (cudaStream_t)stream));
+    agb_set_error_message("tcgen05 GEMM: a bounded wait timed out", __FILE__, __LINE__);
+    return AGB_ERR_TIMEOUT;
+  }
+  return AGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+"""Small dense complex helpers routed through the library's FP64 GEMM."""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .device import device, ptr, stream_ptr
+
+
+def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, out=None, beta=0.0):
+    """C = alpha * op(A) @ op(B) (+ beta*C) for 2-D complex128 CUDA tensors via agb_zgemm."""
+    A = A.to(device=device(), dtype=torch.complex128)
+    B = B.to(device=device(), dtype=torch.complex128)
+    M, K = (A.shape[1], A.shape[0]) if transA else (A.shape[0], A.shape[1])
+    K2, N = (B.shape[1], B.shape[0]) if transB else (B.shape[0], B.shape[1])
+    assert K == K2, (A.shape, B.shape, transA, transB)
+    sAm, sAk = (A.stride(1), A.stride(0)) if transA else (A.stride(0), A.stride(1))
+    sBk, sBn = (B.stride(1), B.stride(0)) if transB else (B.stride(0), B.stride(1))
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.complex128, device=device())
+        beta = 0.0
+    alpha, beta = complex(alpha), complex(beta)
+    _lib.call("agb_zgemm", M, N, K, alpha.real, alpha.imag, ptr(A), sAm, sAk, int(conjA), ptr(B), sBk, sBn,
+              int(conjB), beta.real, beta.imag, ptr(out), out.stride(0), stream_ptr())
+    return out
+
+
+def jk_fock(ERI_AO, D, h, scale):
+    """F = h + scale * sum_ls D_ls (2 (mn|ls) - (ml|ns)) (apyib/hf_wfn.py:81, apyib/utils.py:249)."""
+    n = D.shape[0]
+    eri = ERI_AO.to(device=device(), dtype=torch.float64).contiguous()
+    D = D.to(device=device(), dtype=torch.complex128).contiguous()
+    h = h.to(device=device(), dtype=torch.complex128).contiguous()
+    F = torch.empty((n, n), dtype=torch.complex128, device=device())
+    _lib.call("agb_jk_fock", ptr(eri), n, ptr(D), ptr(h), float(scale), ptr(F), stream_ptr())
+    return F

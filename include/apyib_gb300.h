@@ -1,0 +1,192 @@
+/*
+ * apyib_gb300 — C ABI of the GB300 (sm_103a) correlated-wavefunction hot path.
+ *
+ * Every entry point takes device pointers, sizes and a cudaStream_t passed as
+ * void*, returns an agb_status (0 = AGB_OK) and never frees caller memory.
+ * Complex data are interleaved (re, im) doubles (numpy complex128 /
+ * torch.complex128 layout), row-major, unless stated otherwise.
+ * Orbital conventions follow the reference: spin orbitals interleave alpha
+ * (even index) and beta (odd index); ERIs are chemist (pq|rs) and
+ * <pq||rs> = (pr|qs) - (ps|qr).  No entry point allocates device memory
+ * except agb_cisd_plan_create (host memory for the plan object only);
+ * device workspace is sized by the library and owned by the caller.
+ *
+ * Reference cross-walk (apyib project paths):
+ *   agb_zgemm / agb_cgemm_tf32x3   opt_einsum contractions of apyib/ci_wfn.py:309-334
+ *   agb_compute_f_so               apyib/utils.py:283-313 (compute_F_SO)
+ *   agb_compute_eri_so             apyib/utils.py:317-365 (compute_ERI_SO)
+ *   agb_cisd_blocks_*              the <pq||rs> block slices formed in apyib/ci_wfn.py:284,309-334
+ *   agb_cisd_residual              apyib/ci_wfn.py:309-334 (CISD_SO) and :210-220 (CID_SO)
+ *   agb_cisd_update                apyib/ci_wfn.py:336-337
+ *   agb_vec_dots                   the DIIS Gram matrix, apyib/utils.py:121
+ *   agb_cisd_combine               apyib/utils.py:138 + ci_wfn.py:355,361-365
+ *   agb_mp2_so                     apyib/mp2_wfn.py:82-85 (solve_MP2_SO)
+ *   agb_ao2mo                      apyib/utils.py:274-277 (compute_ERI_MO)
+ *   agb_jk_fock                    apyib/hf_wfn.py:81 and apyib/utils.py:241,249
+ */
+#ifndef APYIB_GB300_H
+#define APYIB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int agb_status;
+#define AGB_OK 0
+#define AGB_ERR_ARG 1          /* bad argument (shape, null pointer, size) */
+#define AGB_ERR_CUDA 2         /* a CUDA runtime/driver call failed */
+#define AGB_ERR_UNSUPPORTED 3  /* feature not available (e.g. not sm_103a) */
+#define AGB_ERR_TIMEOUT 4      /* a bounded device-side wait ran out */
+#define AGB_ERR_WORKSPACE 5    /* workspace missing or too small */
+
+#define AGB_PREC_FP64 0        /* FP64 CUDA-core arithmetic */
+#define AGB_PREC_TF32X3 1      /* complex FP32 via 3xTF32 tcgen05 MMAs, FP32 accumulate */
+
+/* Library version (major*10000 + minor*100 + patch). */
+int agb_version(void);
+/* Number of kernels this library has launched in this process (diagnostics;
+ * no reference counterpart). */
+unsigned long long agb_launch_count(void);
+/* Last error message recorded by a failing call on this host thread. */
+const char* agb_last_error(void);
+
+/* ---------------------------------------------------------------- GEMMs -- */
+
+/* C[m,n] = alpha * sum_k opA(m,k) * opB(k,n) + beta * C[m,n]
+ * opA(m,k) = A[m*sAm + k*sAk] (conjugated if conjA), opB(k,n) = B[k*sBk + n*sBn]
+ * (conjugated if conjB); strides in complex elements; C row-major with ldc.
+ * Replaces the complex128 opt_einsum/zgemm contractions of apyib/ci_wfn.py:309-334. */
+agb_status agb_zgemm(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                     const void* A, int64_t sAm, int64_t sAk, int conjA,
+                     const void* B, int64_t sBk, int64_t sBn, int conjB,
+                     double beta_re, double beta_im, void* C, int64_t ldc, void* stream);
+
+/* Same contraction computed as complex FP32 with 3xTF32 split products on the
+ * tcgen05 tensor cores (FP32 accumulation in TMEM), FP64 in and out.
+ * scratch must hold agb_cgemm_tf32x3_scratch_bytes(M,N,K) bytes. */
+size_t agb_cgemm_tf32x3_scratch_bytes(int64_t M, int64_t N, int64_t K);
+agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                            const void* A, int64_t sAm, int64_t sAk, int conjA,
+                            const void* B, int64_t sBk, int64_t sBn, int conjB,
+                            double beta_re, double beta_im, void* C, int64_t ldc,
+                            void* scratch, size_t scratch_bytes, void* stream);
+
+/* Reads and clears the status word a 3xTF32 GEMM keeps in the first bytes of its
+ * scratch (zero it once before first use): AGB_ERR_TIMEOUT if a bounded
+ * device-side wait ran out.  Synchronises the stream. */
+agb_status agb_scratch_status(void* scratch, void* stream);
+
+/* -------------------------------------------------- spin-orbital expansion -- */
+
+/* F_SO[p,q] = F_MO[p/2,q/2] if p%2 == q%2 else 0; F_MO n x n, F_SO 2n x 2n.
+ * Replaces apyib/utils.py:283-313 (compute_F_SO). */
+agb_status agb_compute_f_so(const void* F_MO, int64_t n, void* F_SO, void* stream);
+/* Chemist ERI_SO[p,q,r,s] = ERI_MO[p/2,q/2,r/2,s/2] if p%2==q%2 and r%2==s%2
+ * else 0, for an n0 x n1 x n2 x n3 ERI_MO.  Replaces apyib/utils.py:317-365. */
+agb_status agb_compute_eri_so(const void* ERI_MO, int64_t n0, int64_t n1, int64_t n2, int64_t n3,
+                              void* ERI_SO, void* stream);
+
+/* ------------------------------------------------------------- CISD plan -- */
+
+typedef struct agb_cisd_plan agb_cisd_plan;
+
+#define AGB_PLAN_MIXED 1       /* also keep 3xTF32-prepared operands (AGB_PREC_TF32X3 residuals) */
+#define AGB_PLAN_NO_SINGLES 2  /* CID_SO: t1 == 0, no singles blocks */
+#define AGB_PLAN_MP2 4         /* MP2_SO only: <ab||ij> and <ij||ab> blocks, no residual */
+
+/* o, v: occupied / virtual spin orbitals (even, >= 2).  Host allocation only. */
+agb_status agb_cisd_plan_create(int o, int v, int flags, agb_cisd_plan** plan);
+agb_status agb_cisd_plan_destroy(agb_cisd_plan* plan);
+/* Device workspace the plan needs; the caller allocates it (any allocator). */
+agb_status agb_cisd_plan_workspace_bytes(const agb_cisd_plan* plan, size_t* bytes);
+agb_status agb_cisd_plan_set_workspace(agb_cisd_plan* plan, void* workspace, size_t bytes);
+/* Sizes of the packed amplitude vector [t1 (o*v) | t2 (o(o-1)/2 * v(v-1)/2)]. */
+agb_status agb_cisd_plan_sizes(const agb_cisd_plan* plan, int64_t* n1, int64_t* n2);
+
+/* Fock matrix (full spin-orbital F_SO, nso x nso) and SO orbital energies
+ * eps_so (nso doubles, occupied first) used for the denominators
+ * D_ia = e_i - e_a, D_ijab = e_i + e_j - e_a - e_b (apyib/ci_wfn.py:268-271). */
+agb_status agb_cisd_set_fock(agb_cisd_plan* plan, const void* F_SO, const double* eps_so, void* stream);
+/* (F_SO and eps_so are device pointers.) */
+
+/* Build every antisymmetrised block the residual reads, from
+ *  - a spatial-MO chemist tensor ERI_MO (nmo^4, nmo = (o+v)/2), applying the
+ *    spin integration of apyib/utils.py:317-365 on the fly;
+ *  - a full spin-orbital chemist tensor ERI_SO (nso^4);
+ *  - Hermitian factors Bf[L,p,q] (naux x nso x nso): (pq|rs) = sum_L Bf[L,p,q] Bf[L,r,s].
+ * 'scratch' (factors variant only) must hold agb_cisd_factor_scratch_bytes bytes. */
+agb_status agb_cisd_blocks_from_mo(agb_cisd_plan* plan, const void* ERI_MO, void* stream);
+agb_status agb_cisd_blocks_from_so(agb_cisd_plan* plan, const void* ERI_SO, void* stream);
+size_t agb_cisd_factor_scratch_bytes(const agb_cisd_plan* plan, int64_t naux);
+agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* plan, const void* Bf, int64_t naux,
+                                        void* scratch, size_t scratch_bytes, void* stream);
+
+#define AGB_RES_CONST 1        /* include the constant terms <ab||ij> and F_ai */
+#define AGB_RES_ETERM 2        /* include -E * t */
+
+/* Packed residual of apyib/ci_wfn.py:309-334: t = [t1 | t2p] and r = [r1 | r2p]
+ * are packed amplitude vectors (t2p[p(i<j), p(a<b)] = t2[i,j,a,b]).
+ * flags selects the constant and -E*t terms (both set for the reference residual;
+ * neither for the linear part L(t) used by iterative refinement). */
+agb_status agb_cisd_residual(agb_cisd_plan* plan, int precision, const void* t, double E_re, double E_im,
+                             int flags, void* r, void* stream);
+
+/* Status of the plan's device-side waits (AGB_ERR_TIMEOUT after a timed-out
+ * tcgen05 GEMM); synchronises the stream. */
+agb_status agb_cisd_status(agb_cisd_plan* plan, void* stream);
+
+/* t_out = t + r / D (apyib/ci_wfn.py:336-337) on packed vectors. */
+agb_status agb_cisd_update(agb_cisd_plan* plan, const void* t, const void* r, void* t_out, void* stream);
+
+/* out[j] = w1 * sum_{k<n1} conj(y_j[k]) x[k] + w2 * sum_{k>=n1} conj(y_j[k]) x[k], j < ny <= 16.
+ * (DIIS Gram row, apyib/utils.py:121, with w2 = 4 for packed doubles.) */
+agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x,
+                        const void* const* ys, int ny, void* out, void* partials, size_t partials_bytes,
+                        void* stream);
+size_t agb_vec_partials_bytes(int ny);
+
+/* t_new = sum_j c_j y_j (apyib/utils.py:138; ny <= 16; ny = 1, c = 1 copies),
+ * fused with the energy E = sum_ia t1*F_ov + sum_p t2p*<ij||ab>_p (ci_wfn.py:355) and the
+ * unconjugated squared norms s1 = sum (t1_old - t1_new)^2, s2 = 4 sum (t2p_old - t2p_new)^2
+ * (ci_wfn.py:361-365).  out3 receives (E, s1, s2) as three complex doubles.
+ * t_old may alias t_new (read before write per element). */
+agb_status agb_cisd_combine(agb_cisd_plan* plan, const void* const* ys, const double* coefs, int ny,
+                            const void* t_old, void* t_new, void* out3, void* partials,
+                            size_t partials_bytes, void* stream);
+
+/* Unpack a packed amplitude vector into t1[o,v] and the full antisymmetric t2[o,o,v,v]. */
+agb_status agb_cisd_unpack(agb_cisd_plan* plan, const void* t, void* t1, void* t2, void* stream);
+/* Pack t1[o,v], t2[o,o,v,v] into a packed amplitude vector. */
+agb_status agb_cisd_pack(agb_cisd_plan* plan, const void* t1, const void* t2, void* t, void* stream);
+/* Initial guesses t1 = F_ai/D_ia, t2p = <ab||ij>/D (apyib/ci_wfn.py:287-290). */
+agb_status agb_cisd_guess(agb_cisd_plan* plan, void* t, void* stream);
+
+/* ------------------------------------------------------------------- MP2 -- */
+
+/* MP2_SO from a built plan: t2p = <ab||ij>/D, E = sum_p <ij||ab>_p t2p
+ * (apyib/mp2_wfn.py:82-85); t receives the packed vector (t1 part zero). */
+agb_status agb_mp2_so(agb_cisd_plan* plan, void* t, void* E_out, void* partials, size_t partials_bytes,
+                      void* stream);
+
+/* ------------------------------------------------------ AO -> MO, J/K -- */
+
+/* ERI_MO[p,q,r,s] = sum C*[m,p] C[n,q] C*[l,r] C[s',s] (mn|ls') for real AO ERIs
+ * (nbf^4 doubles) and complex C (nbf x nmo), four quarter steps
+ * (apyib/utils.py:274-277).  scratch: agb_ao2mo_scratch_bytes. */
+size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo);
+agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t nmo, void* ERI_MO,
+                     void* scratch, size_t scratch_bytes, int precision, void* stream);
+
+/* F = h + scale * sum_ls D[l,s] (2 (mn|ls) - (ml|ns)) with real AO ERIs and
+ * complex D, h, F (nbf x nbf).  One pass over the ERIs for J and K.
+ * apyib/hf_wfn.py:81 (scale 0.5) and apyib/utils.py:241,249 (scale 1). */
+agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale,
+                       void* F, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* APYIB_GB300_H */

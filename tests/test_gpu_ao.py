@@ -1,0 +1,68 @@
+"""GPU SCF (J/K), AO->MO transform and the full SCF -> CISD_SO / MP2_SO
+pipeline against fixtures generated by the reference itself."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from apyib_gb300 import _lib  # noqa: E402
+from apyib_gb300.ci_wfn import ci_wfn  # noqa: E402
+from apyib_gb300.hamiltonian import Hamiltonian  # noqa: E402
+from apyib_gb300.hf_wfn import hf_wfn  # noqa: E402
+from apyib_gb300.mp2_wfn import mp2_wfn  # noqa: E402
+from apyib_gb300 import utils  # noqa: E402
+from tests.gpu_util import GOLD  # noqa: E402
+
+FILES = sorted(glob.glob(os.path.join(GOLD, "ao_*.npz")))
+
+
+def params(method, fc):
+    return dict(method=method, e_convergence=1e-13, d_convergence=1e-13, DIIS=True, freeze_core=fc,
+                max_iterations=100, F_el=[0, 0, 0], F_mag=[0, 0, 0])
+
+
+def make(g):
+    H = Hamiltonian.from_arrays(g["T"], g["V"], g["S"], g["ERI"], float(g["E_nuc"]), nelec=2 * int(g["ndocc"]),
+                                nfzc=int(g["nfzc"]))
+    return H
+
+
+@pytest.mark.parametrize("path", FILES, ids=os.path.basename)
+def test_scf_matches_reference(path):
+    g = dict(np.load(path))
+    fc = int(g["nfzc"]) > 0
+    wfn = hf_wfn(make(g))
+    E, C = wfn.solve_SCF(params("RHF", fc))
+    assert abs(E - g["E_scf"]) < 1e-10
+    np.testing.assert_allclose(wfn.eps, g["eps"], atol=1e-9)
+
+
+@pytest.mark.parametrize("path", FILES, ids=os.path.basename)
+def test_transforms_and_correlated_energies(path):
+    g = dict(np.load(path))
+    fc = int(g["nfzc"]) > 0
+    wfn = hf_wfn(make(g))
+    wfn.solve_SCF(params("RHF", fc))
+    # continue from the reference's orbitals so phases match the fixtures
+    wfn.C = g["C"]
+    wfn.eps = g["eps"]
+    wfn.E_SCF = g["E_scf"]
+    p = params("CISD_SO", fc)
+    C_list, I_list = utils.get_slices(p, wfn)
+    F_MO, E_fc = utils.compute_F_MO(p, wfn, C_list)
+    np.testing.assert_allclose(F_MO, g["F_MO"], atol=1e-11)
+    assert abs(E_fc - g["E_fc"]) < 1e-11
+    ERI_MO = utils.compute_ERI_MO(p, wfn, C_list)
+    np.testing.assert_allclose(ERI_MO, g["ERI_MO"], atol=1e-12)
+    E, t1, t2 = ci_wfn(p, wfn).solve_CISD_SO()
+    assert abs(E - g["E_cisd"]) < 1e-10
+    np.testing.assert_allclose(t2, g["t2_cisd"], atol=1e-9)
+    E, t2 = ci_wfn(params("CID_SO", fc), wfn).solve_CID_SO()
+    assert abs(E - g["E_cid"]) < 1e-10
+    E, t2 = mp2_wfn(params("MP2_SO", fc), wfn).solve_MP2_SO()
+    assert abs(E - g["E_mp2"]) < 1e-10
+    np.testing.assert_allclose(t2, g["t2_mp2"], atol=1e-9)

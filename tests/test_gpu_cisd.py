@@ -1,0 +1,108 @@
+"""GPU CISD_SO / CID_SO / MP2_SO parity against the reference-pinned oracle
+and the golden fixtures.  FP64 mode: energies to 1e-10 Eh, amplitudes to
+1e-9 max-abs.  Mixed mode: |dE| <= 1e-9 Eh against the FP64 result."""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from apyib_gb300 import _lib, synthetic  # noqa: E402
+from apyib_gb300.cisd import CISDPlan  # noqa: E402
+from apyib_gb300.ci_wfn import solve_so_system  # noqa: E402
+from oracle import port  # noqa: E402
+from tests.gpu_util import load_gold, so_golden_files  # noqa: E402
+
+P = dict(max_iterations=100, DIIS=True, e_convergence=1e-13, d_convergence=1e-13)
+
+
+def prob_of(g):
+    return synthetic.so_factors(int(g["o"]), int(g["v"]), seed=int(g["seed"]), real=bool(g["real"]))
+
+
+@pytest.mark.parametrize("path", so_golden_files(with_inputs=True), ids=os.path.basename)
+@pytest.mark.parametrize("source", ["factors", "so", "mo_like"])
+def test_single_residual_matches_reference(path, source):
+    g = load_gold(os.path.basename(path))
+    prob = prob_of(g)
+    o, v = prob.o, prob.v
+    plan = CISDPlan(o, v)
+    F = g["F_pert"]
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    plan.set_fock(torch.as_tensor(F), eps_so)
+    eri = np.einsum("Lpq,Lrs->pqrs", prob.B, prob.B)
+    if source == "factors":
+        plan.blocks_from_factors(torch.as_tensor(prob.B))
+    else:
+        plan.blocks_from_so(torch.as_tensor(eri))
+    t = plan.guess()
+    E0, _, _ = plan.combine([t], [1.0], t, t)
+    r = plan.residual(t, E0)
+    t1n = plan.update(t, r)
+    t1, t2 = plan.unpack(t1n)
+    np.testing.assert_allclose(t1.cpu().numpy(), g["t1_iter1"], atol=1e-13, rtol=0)
+    np.testing.assert_allclose(t2.cpu().numpy(), g["t2_iter1"], atol=1e-13, rtol=0)
+
+
+@pytest.mark.parametrize("path", so_golden_files(), ids=os.path.basename)
+def test_solves_match_reference(path):
+    g = load_gold(os.path.basename(path))
+    prob = prob_of(g)
+    F = prob.fock_so()
+    E, t1, t2 = solve_so_system(F, prob.eps_o, prob.eps_v, P, B=prob.B)
+    assert abs(E - g["E_cisd"]) < 1e-10
+    np.testing.assert_allclose(t1.cpu().numpy(), g["t1_cisd"], atol=1e-9, rtol=0)
+    if "t2_cisd" in g:
+        np.testing.assert_allclose(t2.cpu().numpy(), g["t2_cisd"], atol=1e-9, rtol=0)
+    E, _, t2 = solve_so_system(F, prob.eps_o, prob.eps_v, P, B=prob.B, singles=False)
+    assert abs(E - g["E_cid"]) < 1e-10
+    plan = CISDPlan(prob.o, prob.v, mp2_only=True)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    plan.set_fock(torch.as_tensor(F), eps_so)
+    plan.blocks_from_factors(torch.as_tensor(prob.B))
+    E, t = plan.mp2()
+    assert abs(E - g["E_mp2"]) < 1e-12
+    if "t2_mp2" in g:
+        _, t2 = plan.unpack(t)
+        np.testing.assert_allclose(t2.cpu().numpy(), g["t2_mp2"], atol=1e-12)
+
+
+@pytest.mark.parametrize("o,v,seed", [(8, 30, 31), (12, 44, 32)])
+def test_solve_matches_oracle_larger(o, v, seed):
+    prob = synthetic.so_factors(o, v, seed=seed)
+    blk = port.blocks_from_factors(prob.B, o)
+    F = prob.fock_so()
+    Er, t1r, t2r = port.solve_cisd_so(F, blk, prob.eps_o, prob.eps_v, P)
+    E, t1, t2 = solve_so_system(F, prob.eps_o, prob.eps_v, P, B=prob.B)
+    assert abs(E - Er) < 1e-10
+    assert np.abs(t2.cpu().numpy() - t2r).max() < 1e-9
+    assert np.abs(t1.cpu().numpy() - t1r).max() < 1e-9
+
+
+def test_nondiagonal_fock_solve_matches_oracle():
+    prob = synthetic.so_factors(6, 14, seed=41)
+    rng = np.random.default_rng(0)
+    F = prob.fock_so()
+    n = prob.nso
+    pert = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * 0.003
+    pert = pert + pert.conj().T
+    mask = (np.add.outer(np.arange(n) % 2, np.arange(n) % 2) % 2) == 0
+    F = F + pert * mask
+    blk = port.blocks_from_factors(prob.B, prob.o)
+    Er, t1r, t2r = port.solve_cisd_so(F, blk, prob.eps_o, prob.eps_v, P)
+    E, t1, t2 = solve_so_system(F, prob.eps_o, prob.eps_v, P, B=prob.B)
+    assert abs(E - Er) < 1e-10
+    assert np.abs(t2.cpu().numpy() - t2r).max() < 1e-9
+
+
+def test_mixed_precision_reaches_fp64_energy():
+    prob = synthetic.so_factors(20, 80, seed=7)
+    F = prob.fock_so()
+    p = dict(P, e_convergence=1e-12, d_convergence=1e-10)
+    E64, _, t2_64 = solve_so_system(F, prob.eps_o, prob.eps_v, p, B=prob.B)
+    hist = []
+    Em, _, t2_m = solve_so_system(F, prob.eps_o, prob.eps_v, p, B=prob.B, precision="mixed", history=hist)
+    assert abs(Em - E64) < 1e-9, (Em, E64, hist)
+    assert np.abs(t2_m.cpu().numpy() - t2_64.cpu().numpy()).max() < 1e-8

@@ -1,0 +1,97 @@
+"""GPU parity of the library kernels against NumPy (complex128)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from apyib_gb300 import _lib  # noqa: E402
+from apyib_gb300.device import ptr, stream_ptr, to_dev, workspace  # noqa: E402
+from apyib_gb300.linalg import jk_fock, zmm  # noqa: E402
+from oracle import port  # noqa: E402
+from tests.gpu_util import crandn  # noqa: E402
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb,ca,cb", [
+    (1, 1, 1, False, False, False, False),
+    (37, 53, 29, False, False, False, False),
+    (64, 64, 64, True, False, True, False),
+    (130, 70, 300, False, True, False, True),
+    (5, 7, 5000, True, True, True, True),      # split-K would apply with scratch
+])
+def test_zgemm_matches_numpy(M, N, K, ta, tb, ca, cb):
+    rng = np.random.default_rng(M * 7 + N)
+    A = crandn(rng, *((K, M) if ta else (M, K)))
+    B = crandn(rng, *((N, K) if tb else (K, N)))
+    opA = A.T if ta else A
+    opB = B.T if tb else B
+    if ca:
+        opA = opA.conj()
+    if cb:
+        opB = opB.conj()
+    ref = (2 - 1j) * opA @ opB
+    C = zmm(to_dev(A), to_dev(B), transA=ta, conjA=ca, transB=tb, conjB=cb, alpha=2 - 1j).cpu().numpy()
+    np.testing.assert_allclose(C, ref, rtol=0, atol=1e-12 * np.sqrt(K) * 4)
+
+
+def tf32_gemm(A, B, alpha=1.0, beta=0.0, C=None, transB=False):
+    Ad, Bd = to_dev(A), to_dev(B)
+    M, K = A.shape
+    N = B.shape[0] if transB else B.shape[1]
+    out = to_dev(C) if C is not None else torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    nb = _lib.load().agb_cgemm_tf32x3_scratch_bytes(M, N, K)
+    buf, sp, _ = workspace(nb)
+    torch.cuda.synchronize()
+    buf.zero_()
+    sBk, sBn = (1, K) if transB else (N, 1)
+    a, b = complex(alpha), complex(beta)
+    _lib.call("agb_cgemm_tf32x3", M, N, K, a.real, a.imag, ptr(Ad), K, 1, 0, ptr(Bd), sBk, sBn, 0, b.real, b.imag,
+              ptr(out), N, ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
+    _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 16), (1, 1, 1), (200, 300, 77), (60, 240, 6000), (513, 129, 1000)])
+def test_tf32x3_gemm_accuracy(M, N, K):
+    """3xTF32 complex GEMM: error ~1e-6 relative to sum|a||b| (FP32-level)."""
+    rng = np.random.default_rng(M + N + K)
+    A = crandn(rng, M, K)
+    B = crandn(rng, K, N)
+    ref = A @ B
+    got = tf32_gemm(A, B)
+    scale = np.abs(A) @ np.abs(B)
+    err = np.abs(got - ref) / scale
+    assert err.max() < 2e-6, err.max()
+
+
+def test_tf32x3_gemm_alpha_beta_and_transposed_b():
+    rng = np.random.default_rng(5)
+    A = crandn(rng, 150, 90)
+    Bt = crandn(rng, 170, 90)
+    C0 = crandn(rng, 150, 170)
+    ref = (0.5 + 2j) * A @ Bt.T + (1 - 1j) * C0
+    got = tf32_gemm(A, Bt, alpha=0.5 + 2j, beta=1 - 1j, C=C0, transB=True)
+    assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5
+
+
+def test_jk_fock_matches_oracle():
+    rng = np.random.default_rng(3)
+    n = 19
+    A = rng.standard_normal((40, n, n))
+    A = A + A.transpose(0, 2, 1)
+    eri = np.einsum("Lmn,Lls->mnls", A, A) / 40
+    D = crandn(rng, n, n)
+    h = crandn(rng, n, n)
+    F = jk_fock(to_dev(eri, torch.float64), to_dev(D), to_dev(h), 0.5).cpu().numpy()
+    np.testing.assert_allclose(F, port.jk_fock(h, eri, D, 0.5), atol=1e-11)
+
+
+def test_so_expansion_matches_oracle():
+    from apyib_gb300 import utils
+    rng = np.random.default_rng(4)
+    F = crandn(rng, 5, 5)
+    g = crandn(rng, 3, 4, 5, 2)
+    np.testing.assert_array_equal(utils.compute_F_SO(None, F), port.compute_F_SO(F))
+    np.testing.assert_array_equal(utils.compute_ERI_SO(None, g), port.compute_ERI_SO(g))
