@@ -1,0 +1,186 @@
+"""Hand-written adjoint of the spin-orbital CISD energy.
+
+The CISD_SO energy of apyib/ci_wfn.py:263-378 is the eigenvalue of the
+normal-ordered Hamiltonian in the singles+doubles space.  Its derivative
+with respect to any one- or two-electron integral is therefore the
+expectation value of the corresponding operator in the normalised CI state
+(Hellmann-Feynman; no amplitude response is needed):
+
+    dE = sum_pq D_pq dF_pq + sum_pqrs Gamma_pqrs d<pq|rs>
+
+with the one- and two-particle densities of the reference's own adjoint
+check (apyib/ci_wfn.py:382-411, restated in oracle/port.py).  The densities
+are built on the GPU from the converged amplitudes with the library's
+complex GEMMs; the vvvv block Gamma_abcd = 1/4 sum_ij t2*_ijab t2_ijcd is
+recomputed in the backward as a packed (a<b, c<d) GEMM over i<j rather than
+kept from the forward pass.
+
+``CISDEnergy`` wraps the solve in a torch.autograd.Function with inputs
+(F_SO, ERI_SO) (chemist, <pq|rs> = (pr|qs)); ``CISDEnergyFactors`` takes
+Hermitian factors B[L,p,q] with (pq|rs) = sum_L B[L,p,q] B[L,r,s] instead
+of the nso^4 tensor.  Gradients follow PyTorch's convention for a
+holomorphic map: grad_input = grad_output * conj(dE/dinput).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .cisd import CISDPlan, solve
+from .device import device, ptr, stream_ptr, to_dev
+from .linalg import zmm
+
+
+def _zgemm_conjA(A_ptr_tensor, M, N, K, sAm, sAk, B, sBk, sBn, out, alpha=1.0, precision=_lib.PREC_FP64,
+                 scratch=None):
+    a = complex(alpha)
+    if precision == _lib.PREC_TF32X3:
+        buf, nb = scratch
+        _lib.call("agb_cgemm_tf32x3", M, N, K, a.real, a.imag, ptr(A_ptr_tensor), sAm, sAk, 1, ptr(B), sBk, sBn, 0,
+                  0.0, 0.0, ptr(out), N, ptr(buf), nb, stream_ptr())
+    else:
+        _lib.call("agb_zgemm", M, N, K, a.real, a.imag, ptr(A_ptr_tensor), sAm, sAk, 1, ptr(B), sBk, sBn, 0, 0.0, 0.0,
+                  ptr(out), N, stream_ptr())
+
+
+def densities(plan, t, precision=_lib.PREC_FP64):
+    """One- and two-particle densities of the normalised CISD_SO (or CID_SO)
+    state from the packed amplitudes t.  Returns (D [nso,nso], G) with G a
+    dict of Dirac-ordered blocks keyed by orbital-range letters; G['vvvv_p']
+    is the packed block Gp[(a<b),(c<d)] with Gamma_abcd = sign * Gp / 2."""
+    o, v = plan.o, plan.v
+    nso = o + v
+    dev = device()
+    t1, t2 = plan.unpack(t)
+    if t1 is None:
+        t1 = torch.zeros((o, v), dtype=torch.complex128, device=dev)
+    n1 = torch.sum(t1.conj() * t1).real
+    n2 = torch.sum(t2.conj() * t2).real
+    N = float(1.0 / torch.sqrt(1.0 + n1 + 0.25 * n2))
+    t0 = N
+    t1 = t1 * N
+    t2 = t2 * N
+    t1c = t1.conj()
+    O, V = slice(0, o), slice(o, nso)
+    D = torch.zeros((nso, nso), dtype=torch.complex128, device=dev)
+    T2m = t2.reshape(o, o * v * v)
+    D[O, O] = -(zmm(t1, t1, transB=True, conjB=True) + 0.5 * zmm(T2m, T2m, transB=True, conjB=True))
+    Tv = t2.permute(2, 0, 1, 3).reshape(v, o * o * v).contiguous()
+    D[V, V] = zmm(t1, t1, transA=True, conjA=True) + 0.5 * zmm(Tv, Tv, conjA=True, transB=True)
+    Tr = t2.permute(0, 2, 1, 3).reshape(o * v, o * v).contiguous()       # [(i,a),(j,b)] = t2[i,j,a,b]
+    D[O, V] = t0 * t1 + zmm(Tr, t1c.reshape(o * v, 1)).reshape(o, v)
+    D[V, O] = (t0 * t1c + zmm(Tr, t1.reshape(o * v, 1), conjA=True).reshape(o, v)).T
+    G = {}
+    # oooo: 1/4 sum_ab t2*[k,l,a,b] t2[i,j,a,b] -> [i,j,k,l]
+    Toov = t2.reshape(o * o, v * v)
+    G["oooo"] = 0.25 * zmm(Toov, Toov, transB=True, conjB=True).reshape(o, o, o, o)
+    # ovvo / ovov from t1: 'ja,ib->iabj' and -'ja,ib->iajb'
+    P = torch.einsum("ja,ib->iabj", t1c, t1)          # outer product (no contraction)
+    G["ovvo"] = P.contiguous()
+    G["ovov"] = (-P.permute(0, 1, 3, 2)).contiguous()
+    # voov / vovo: 'jkac,ikbc->aijb' and -'jkac,ikbc->aibj'
+    Tk = t2.permute(0, 2, 1, 3).reshape(o * v, o * v)   # [(j,a),(k,c)]
+    Q = zmm(Tk, Tk, conjA=True, transB=True).reshape(o, v, o, v)      # Q[j,a,i,b] = sum_kc t2*[jkac] t2[ikbc]
+    G["voov"] = Q.permute(1, 2, 0, 3).contiguous()                    # [a,i,j,b]
+    G["vovo"] = (-Q.permute(1, 2, 3, 0)).contiguous()                 # [a,i,b,j]
+    G["oovv"] = 0.5 * t0 * t2
+    G["vvoo"] = (0.5 * t0 * t2.conj().permute(2, 3, 0, 1)).contiguous()
+    # vovv: 'ja,ijcb->aibc'
+    G["vovv"] = zmm(t1c, t2.permute(1, 0, 3, 2).reshape(o, o * v * v), transA=True).reshape(v, o, v, v)
+    # ovoo: -'kjab,ib->iajk'
+    Tb = t2.conj().permute(3, 2, 1, 0).reshape(v, v * o * o).contiguous()   # [b,(a,j,k)] = t2*[k,j,a,b]
+    G["ovoo"] = (-zmm(t1, Tb).reshape(o, v, o, o)).contiguous()             # X[i,(a,j,k)] = sum_b t1[i,b] Tb
+
+    # vvvo: 'jiab,jc->abci'
+    G["vvvo"] = zmm(t2.conj().permute(2, 3, 1, 0).reshape(v * v * o, o), t1).reshape(v, v, o, v).permute(
+        0, 1, 3, 2).contiguous()
+    # ooov: -'kb,ijba->ijka'
+    G["ooov"] = (-zmm(t2.permute(0, 1, 3, 2).reshape(o * o * v, v), t1c, transB=True)
+                 .reshape(o, o, v, o).permute(0, 1, 3, 2)).contiguous()
+    # vvvv (packed, recomputed): Gp[(ab),(cd)] = sum_{i<j} t2p*[ij,ab] t2p[ij,cd]; Gamma = Gp/2 with signs
+    n1v = plan.n1
+    t2p = (t[n1v:] * N).contiguous()
+    po, pv = o * (o - 1) // 2, v * (v - 1) // 2
+    Gp = torch.empty((pv, pv), dtype=torch.complex128, device=dev)
+    if precision == _lib.PREC_TF32X3:
+        nb = _lib.load().agb_cgemm_tf32x3_scratch_bytes(pv, pv, po)
+        buf = torch.zeros(int(nb) // 8 + 64, dtype=torch.float64, device=dev)
+        _zgemm_conjA(t2p, pv, pv, po, 1, pv, t2p, pv, 1, Gp, precision=precision, scratch=(buf, nb))
+    else:
+        _zgemm_conjA(t2p, pv, pv, po, 1, pv, t2p, pv, 1, Gp)
+    G["vvvv_p"] = Gp
+    G["_norm"] = N
+    return D, G
+
+
+def unpack_vvvv(Gp, v):
+    """Full Gamma_vvvv[a,b,c,d] from the packed block (Gamma = Gp/2 with antisymmetry signs)."""
+    dev = Gp.device
+    iu = torch.triu_indices(v, v, offset=1, device=dev)
+    full = torch.zeros((v, v, v, v), dtype=Gp.dtype, device=dev)
+    a, b = iu[0], iu[1]
+    g = 0.5 * Gp
+    A = a.view(-1, 1).expand(-1, a.numel())
+    Bb = b.view(-1, 1).expand(-1, a.numel())
+    C = a.view(1, -1).expand(a.numel(), -1)
+    Dd = b.view(1, -1).expand(a.numel(), -1)
+    full[A, Bb, C, Dd] = g
+    full[Bb, A, C, Dd] = -g
+    full[A, Bb, Dd, C] = -g
+    full[Bb, A, Dd, C] = g
+    return full
+
+
+def gamma_full(G, o, v):
+    """Assemble the full Dirac Gamma[p,q,r,s] (nso^4) from the blocks."""
+    nso = o + v
+    dev = G["oooo"].device
+    Gm = torch.zeros((nso, nso, nso, nso), dtype=torch.complex128, device=dev)
+    O, V = slice(0, o), slice(o, nso)
+    m = {"o": O, "v": V}
+    for k in ("oooo", "ovvo", "ovov", "voov", "vovo", "oovv", "vvoo", "vovv", "ovoo", "vvvo", "ooov"):
+        Gm[m[k[0]], m[k[1]], m[k[2]], m[k[3]]] += G[k]
+    Gm[V, V, V, V] += unpack_vvvv(G["vvvv_p"], v)
+    return Gm
+
+
+def energy_from_densities(F, ERI_chem, D, Gfull):
+    """E = sum F D + sum <pq|rs> Gamma with <pq|rs> = (pr|qs)."""
+    dirac = ERI_chem.permute(0, 2, 1, 3)
+    return torch.sum(F * D) + torch.sum(dirac * Gfull)
+
+
+class CISDEnergy(torch.autograd.Function):
+    """E_CISD_SO(F_SO, ERI_SO) with a density-based backward.  eps_o / eps_v
+    (spatial, np.repeat-ed for the denominators) and params are constants."""
+
+    @staticmethod
+    def forward(ctx, F_SO, ERI_SO, eps_o, eps_v, params, singles=True, precision="fp64"):
+        o, v = 2 * len(eps_o), 2 * len(eps_v)
+        plan = CISDPlan(o, v, singles=singles, mixed=(precision == "mixed"))
+        eps_so = np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)])
+        plan.set_fock(F_SO.detach(), eps_so)
+        plan.blocks_from_so(ERI_SO.detach())
+        E, t = solve(plan, params, precision=precision)
+        ctx.plan = plan
+        ctx.o, ctx.v = o, v
+        ctx.save_for_backward(t)
+        return torch.tensor(complex(E), dtype=torch.complex128, device=F_SO.device)
+
+    @staticmethod
+    def backward(ctx, gE):
+        (t,) = ctx.saved_tensors
+        D, G = densities(ctx.plan, t)
+        Gfull = gamma_full(G, ctx.o, ctx.v)
+        g = gE.to(torch.complex128)
+        grad_F = g * D.conj()
+        # <pq|rs> = (pr|qs): d E / d (pr|qs) = Gamma[p,q,r,s]
+        grad_ERI = g * Gfull.permute(0, 2, 1, 3).conj()
+        return grad_F, grad_ERI, None, None, None, None, None
+
+
+def cisd_energy(F_SO, ERI_SO, eps_o, eps_v, params, singles=True, precision="fp64"):
+    return CISDEnergy.apply(to_dev(F_SO) if not isinstance(F_SO, torch.Tensor) else F_SO,
+                            to_dev(ERI_SO) if not isinstance(ERI_SO, torch.Tensor) else ERI_SO,
+                            eps_o, eps_v, params, singles, precision)

@@ -25,6 +25,12 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
                         int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                         void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
+size_t tf32_planes_bytes(int64_t rows, int64_t K);
+size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K);
+agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
+                            float* dst, cudaStream_t stream);
+agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
+                            z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream);
 
 namespace {
 
@@ -519,20 +525,34 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   // GEMM scratch: split-K partials (FP64) or 3xTF32 operand planes.
   size_t gs = (size_t)64 << 20;
   if (P->mixed) {
-    auto upd = [&](int64_t M, int64_t N, int64_t K) {
-      size_t s = agb::cgemm_tf32x3_scratch(M, N, K);
+    // status header + planes of the operands prepared per call + split-K partials
+    auto upd = [&](int64_t M, int64_t N, int64_t K, bool a_static, bool b_static) {
+      size_t s = 256 + agb::tf32_partials_bytes(M, N, K);
+      if (!a_static) s += align256(agb::tf32_planes_bytes(M, K));
+      if (!b_static) s += align256(agb::tf32_planes_bytes(N, K));
       if (s > gs) gs = s;
     };
-    upd(ov, ov, ov);
-    upd(po, pv, pv);
-    upd(po, pv, po);
-    upd(po * v, v, v);
-    upd(o, o * pv, o);
+    upd(o, v, o, false, false);
+    upd(o, v, v, false, false);
+    upd(ov, ov, ov, false, true);
+    upd(po, pv, pv, false, true);
+    upd(po, pv, po, true, false);
+    upd(po * v, v, v, false, false);
+    upd(o, o * pv, o, false, false);
     if (P->singles) {
-      upd(o, v, o * pv);
-      upd(o, v, po * v);
-      upd(po * v, v, o);
-      upd(o, o * pv, v);
+      upd(o, v, o * pv, false, true);
+      upd(o, v, po * v, true, false);
+      upd(po * v, v, o, true, false);
+      upd(o, o * pv, v, false, true);
+    }
+    P->P_VT = (float*)take(agb::tf32_planes_bytes(ov, ov));
+    P->P_Wvp = (float*)take(agb::tf32_planes_bytes(pv, pv));
+    P->P_Woooo = (float*)take(agb::tf32_planes_bytes(po, po));
+    if (P->singles) {
+      P->P_Wvovv = (float*)take(agb::tf32_planes_bytes(v, o * pv));
+      P->P_Wooov = (float*)take(agb::tf32_planes_bytes(o, po * v));
+      P->P_Wovoo = (float*)take(agb::tf32_planes_bytes(po * v, o));
+      P->P_Wvvvo = (float*)take(agb::tf32_planes_bytes(o * pv, v));
     }
   }
   P->gemm_scratch = take(gs);
@@ -556,15 +576,51 @@ namespace agb {
 namespace {
 
 // GEMM on the selected backend.  conj flags are never needed on the hot path.
+// PA / PB: TF32 planes of a static operand prepared at set-up (tensor-core path only).
 agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm,
                 int64_t sAk, const z64* B, int64_t sBk, int64_t sBn, z64 beta, z64* C, int64_t ldc,
-                cudaStream_t st) {
-  if (prec == AGB_PREC_TF32X3)
-    return cgemm_tf32x3(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, P->gemm_scratch,
-                        P->gemm_scratch_bytes, st);
+                cudaStream_t st, const float* PA = nullptr, const float* PB = nullptr) {
+  if (prec == AGB_PREC_TF32X3) {
+    if (M == 0 || N == 0) return AGB_OK;
+    if (K == 0) return zgemm_ex(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, nullptr, 0, st);
+    char* base = (char*)P->gemm_scratch;
+    size_t off = 256;
+    if (!PA) {
+      PA = (const float*)(base + off);
+      AGB_STATUS_TRY(tf32_prep_planes(A, M, K, sAm, sAk, 0, (float*)PA, st));
+      off += align256(tf32_planes_bytes(M, K));
+    }
+    if (!PB) {
+      PB = (const float*)(base + off);
+      AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, 0, (float*)PB, st));
+      off += align256(tf32_planes_bytes(N, K));
+    }
+    if (off > P->gemm_scratch_bytes) {
+      agb_set_error_message("residual: GEMM scratch too small", __FILE__, __LINE__);
+      return AGB_ERR_WORKSPACE;
+    }
+    return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
+                            P->gemm_scratch_bytes - off, st);
+  }
   // FP64 split-K partials start past the 256-byte status header of the scratch.
   return zgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, (char*)P->gemm_scratch + 256,
                   P->gemm_scratch_bytes - 256, st);
+}
+
+// TF32 planes of every static ERI-block operand, in the orientation its GEMM reads it.
+agb_status prepare_static_planes(agb_cisd_plan* P, cudaStream_t st) {
+  if (!P->mixed || P->mp2_only) return AGB_OK;
+  const int64_t o = P->o, v = P->v, ov = P->ov, po = P->po, pv = P->pv;
+  AGB_STATUS_TRY(tf32_prep_planes(P->VT, ov, ov, ov, 1, 0, P->P_VT, st));
+  AGB_STATUS_TRY(tf32_prep_planes(P->Wvp, pv, pv, pv, 1, 0, P->P_Wvp, st));
+  AGB_STATUS_TRY(tf32_prep_planes(P->WooooT, po, po, po, 1, 0, P->P_Woooo, st));
+  if (P->singles) {
+    AGB_STATUS_TRY(tf32_prep_planes(P->WvovvH, v, o * pv, o * pv, 1, 0, P->P_Wvovv, st));
+    AGB_STATUS_TRY(tf32_prep_planes(P->WooovP, o, po * v, po * v, 1, 0, P->P_Wooov, st));
+    AGB_STATUS_TRY(tf32_prep_planes(P->WovooP, po * v, o, o, 1, 0, P->P_Wovoo, st));
+    AGB_STATUS_TRY(tf32_prep_planes(P->WvvvoP, o * pv, v, 1, o * pv, 0, P->P_Wvvvo, st));
+  }
+  return AGB_OK;
 }
 
 Dims dims_of(const agb_cisd_plan* P) { return Dims{P->o, P->v, P->ov, P->po, P->pv, P->opairs, P->vpairs}; }
@@ -689,7 +745,7 @@ agb_status agb_cisd_blocks_from_mo(agb_cisd_plan* P, const void* ERI_MO, void* s
   SrcMO s{(const z64*)ERI_MO, P->nso / 2};
   for (int id = 0; id < B_COUNT; ++id)
     if (block_needed(P, id)) AGB_STATUS_TRY(launch_build(P, id, s, s, (cudaStream_t)stream));
-  return AGB_OK;
+  return prepare_static_planes(P, (cudaStream_t)stream);
 }
 
 agb_status agb_cisd_blocks_from_so(agb_cisd_plan* P, const void* ERI_SO, void* stream) {
@@ -697,7 +753,7 @@ agb_status agb_cisd_blocks_from_so(agb_cisd_plan* P, const void* ERI_SO, void* s
   SrcSO s{(const z64*)ERI_SO, P->nso};
   for (int id = 0; id < B_COUNT; ++id)
     if (block_needed(P, id)) AGB_STATUS_TRY(launch_build(P, id, s, s, (cudaStream_t)stream));
-  return AGB_OK;
+  return prepare_static_planes(P, (cudaStream_t)stream);
 }
 
 static int64_t rlen(const agb_cisd_plan* P, char c) { return c == 'o' ? P->o : P->v; }
@@ -766,7 +822,7 @@ agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* P, const void* Bf, int64_
     }
     AGB_STATUS_TRY(launch_build(P, id, sd, se, st));
   }
-  return AGB_OK;
+  return prepare_static_planes(P, st);
 }
 
 agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double E_re, double E_im, int flags, void* rv,
@@ -805,22 +861,22 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     AGB_STATUS_TRY(zgemv(ov, ov, one, P->VT, ov, t1, one, r1, st));
     AGB_STATUS_TRY(zgemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
     AGB_STATUS_TRY(gemm(P, prec, o, v, (int64_t)o * pv, one, P->t2h, (int64_t)o * pv, 1, P->WvovvH, 1,
-                        (int64_t)o * pv, one, r1, v, st));
-    AGB_STATUS_TRY(gemm(P, prec, o, v, po * v, one, P->WooovP, po * v, 1, P->t2q, v, 1, one, r1, v, st));
+                        (int64_t)o * pv, one, r1, v, st, nullptr, P->P_Wvovv));
+    AGB_STATUS_TRY(gemm(P, prec, o, v, po * v, one, P->WooovP, po * v, 1, P->t2q, v, 1, one, r1, v, st, P->P_Wooov));
     if (flags & AGB_RES_ETERM) {
       axpy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(n1, zneg(E), t1, r1);
       AGB_LAUNCH_CHECK();
     }
     // Zq[p(ij)][b][a] = sum_k <kb||ij> t1[k,a];  Yh[i][j][p(ab)] = sum_c t1[i,c] <ab||cj>
-    AGB_STATUS_TRY(gemm(P, prec, po * v, v, o, one, P->WovooP, o, 1, t1, v, 1, zero, P->Zq, v, st));
+    AGB_STATUS_TRY(gemm(P, prec, po * v, v, o, one, P->WovooP, o, 1, t1, v, 1, zero, P->Zq, v, st, P->P_Wovoo));
     AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, v, one, t1, v, 1, P->WvvvoP, (int64_t)o * pv, 1, zero, P->Yh,
-                        (int64_t)o * pv, st));
+                        (int64_t)o * pv, st, nullptr, P->P_Wvvvo));
   }
   // ladders: PQ = sum_{k<l} <kl||ij> t2p[kl,ab] + sum_{c<d} t2p[ij,cd] <ab||cd>
-  AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st));
-  AGB_STATUS_TRY(gemm(P, prec, po, pv, pv, one, t2p, pv, 1, P->Wvp, 1, pv, one, P->PQ, pv, st));
+  AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st, P->P_Woooo));
+  AGB_STATUS_TRY(gemm(P, prec, po, pv, pv, one, t2p, pv, 1, P->Wvp, 1, pv, one, P->PQ, pv, st, nullptr, P->P_Wvp));
   // rings: X[(i,a),(j,b)] = sum_(k,c) t2[i,k,a,c] <kb||cj>
-  AGB_STATUS_TRY(gemm(P, prec, ov, ov, ov, one, P->Tring, ov, 1, P->VT, 1, ov, zero, P->X, ov, st));
+  AGB_STATUS_TRY(gemm(P, prec, ov, ov, ov, one, P->Tring, ov, 1, P->VT, 1, ov, zero, P->X, ov, st, nullptr, P->P_VT));
   if (!P->f_diag) {
     AGB_STATUS_TRY(gemm(P, prec, po * v, v, v, one, P->t2q, v, 1, P->Fvv, 1, v, zero, P->Gq, v, st));
     AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, o, one, P->Foo, 1, o, P->t2h, (int64_t)o * pv, 1, zero, P->H2h,

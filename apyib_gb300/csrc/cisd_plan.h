@@ -31,6 +31,9 @@ struct agb_cisd_plan {
   agb::z64 *Yh;                       // [i][j][p(ab)]
   agb::z64 *Gq;                       // [p(ij)][a][b]
   agb::z64 *H2h;                      // [i][j][p(ab)]
+  // TF32 hi/lo planes of the static operands (mixed plans only)
+  float *P_VT = nullptr, *P_Wvp = nullptr, *P_Woooo = nullptr, *P_Wvovv = nullptr, *P_Wooov = nullptr,
+        *P_Wovoo = nullptr, *P_Wvvvo = nullptr;
   void* gemm_scratch;                 // 3xTF32 operand planes
   size_t gemm_scratch_bytes;
 };

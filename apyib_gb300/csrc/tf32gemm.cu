@@ -16,9 +16,24 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
+#include <mutex>
+#include <vector>
+
 #include "common.cuh"
 
 namespace agb {
+
+// Optional per-launch timing of the tensor-core kernel (CUDA events recorded on
+// the launch stream around the GEMM kernel alone; diagnostics for benchmarks).
+struct TimingRec {
+  cudaEvent_t e0, e1;
+  double flops;
+  int64_t M, N, K;
+};
+static std::atomic<int> g_timing{0};
+static std::mutex g_timing_mu;
+static std::vector<TimingRec> g_timing_recs;
 
 agb_status zgemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
                  const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
@@ -373,53 +388,98 @@ bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp
   return r == CUDA_SUCCESS;
 }
 
-struct Layout {
-  int64_t Mp, Np, Kp, nkb;
-  int splits, nkb_split;
-  size_t offA, offB, offP, total;
-};
-
-Layout plan_layout(int64_t M, int64_t N, int64_t K, size_t cap) {
-  Layout L;
-  L.Mp = round_up(M, BM);
-  L.Np = round_up(N, BN);
-  L.Kp = round_up(K, BK);
-  L.nkb = L.Kp / BK;
-  L.offA = 256;
-  L.offB = L.offA + round_up((int64_t)(4 * L.Mp * L.Kp * sizeof(float)), 256);
-  size_t base_total = L.offB + round_up((int64_t)(4 * L.Np * L.Kp * sizeof(float)), 256);
-  L.offP = base_total;
-  // split K when the tile grid cannot fill the GPU
-  int64_t tiles = (L.Mp / BM) * (L.Np / BN);
-  int splits = 1;
-  if (tiles < 152 && L.nkb >= 16) {
-    int64_t want = (2 * 152 + tiles - 1) / tiles;
-    int64_t kmax = L.nkb / 8;
-    if (want > kmax) want = kmax;
-    if (want > 128) want = 128;
-    if (want < 1) want = 1;
-    splits = (int)want;
-  }
-  L.nkb_split = (int)((L.nkb + splits - 1) / splits);
-  L.splits = (int)((L.nkb + L.nkb_split - 1) / L.nkb_split);
-  size_t part = L.splits > 1 ? (size_t)L.splits * M * N * sizeof(z64) : 0;
-  if (cap && base_total + part > cap && L.splits > 1) {
-    // shrink splits to what fits
-    int64_t fit = (int64_t)((cap - base_total) / (M * N * sizeof(z64)));
-    if (fit < 2) fit = 1;
-    L.nkb_split = (int)((L.nkb + fit - 1) / fit);
-    L.splits = (int)((L.nkb + L.nkb_split - 1) / L.nkb_split);
-    part = L.splits > 1 ? (size_t)L.splits * M * N * sizeof(z64) : 0;
-  }
-  L.total = base_total + part;
-  return L;
-}
-
 }  // namespace
 
+int64_t tf32_rows_pad(int64_t rows) { return round_up(rows, BM); }
+int64_t tf32_k_pad(int64_t K) { return round_up(K, BK); }
+size_t tf32_planes_bytes(int64_t rows, int64_t K) {
+  return (size_t)4 * (size_t)tf32_rows_pad(rows) * (size_t)tf32_k_pad(K) * sizeof(float);
+}
+
+// Split an FP64 complex operand X(row,k) = src[row*s_row + k*s_k] into the four
+// zero-padded K-major TF32 planes the tensor-core kernel reads.
+agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
+                            float* dst, cudaStream_t stream) {
+  int64_t rp = tf32_rows_pad(rows), kp = tf32_k_pad(K);
+  dim3 g((unsigned)((kp + 31) / 32), (unsigned)(rp / 32));
+  AGB_ARG_CHECK(rp / 32 <= 65535, "tf32_prep_planes: too many rows for the grid");
+  prep_kernel<<<g, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, rp, kp, dst);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+namespace {
+int choose_splits(int64_t M, int64_t N, int64_t nkb, size_t partial_cap) {
+  int64_t tiles = (round_up(M, BM) / BM) * (round_up(N, BN) / BN);
+  if (tiles >= 152 || nkb < 16) return 1;
+  int64_t want = (2 * 152 + tiles - 1) / tiles;
+  int64_t kmax = nkb / 8;
+  if (want > kmax) want = kmax;
+  if (want > 128) want = 128;
+  int64_t fit = (int64_t)(partial_cap / ((size_t)M * N * sizeof(z64)));
+  if (want > fit) want = fit;
+  return want < 2 ? 1 : (int)want;
+}
+}  // namespace
+
+// Bytes of split-K partials a planes GEMM may use (0 when no split is chosen).
+size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K) {
+  int64_t nkb = tf32_k_pad(K) / BK;
+  int s = choose_splits(M, N, nkb, (size_t)-1 / 2);
+  return s > 1 ? (size_t)s * M * N * sizeof(z64) : 0;
+}
+
+// C = alpha * A B^T + beta C on prepared planes (A: rows M, B: rows N, both K-major over K).
+agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
+                            z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream) {
+  AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
+  if (M == 0 || N == 0) return AGB_OK;
+  AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
+  const int64_t Mp = tf32_rows_pad(M), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K), nkb = Kp / BK;
+  AGB_ARG_CHECK(Mp / BM <= 65535, "tf32_gemm_planes: grid too large");
+  int splits = partials ? choose_splits(M, N, nkb, partial_bytes) : 1;
+  int nkb_split = (int)((nkb + splits - 1) / splits);
+  splits = (int)((nkb + nkb_split - 1) / nkb_split);
+  CUtensorMap mA, mB;
+  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp) || !encode_planes(&mB, (float*)PB, 4 * Np, Kp)) {
+    agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
+    return AGB_ERR_CUDA;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_set = true;
+  }
+  GemmParams p;
+  p.M = M; p.N = N; p.nkb = nkb_split; p.nkb_total = (int)nkb;
+  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = splits > 1 ? partials : nullptr; p.err = err;
+  p.rowsA = Mp; p.rowsB = Np;
+  dim3 grid((unsigned)(Np / BN), (unsigned)(Mp / BM), (unsigned)splits);
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (g_timing.load(std::memory_order_relaxed)) {
+    AGB_CUDA_TRY(cudaEventCreate(&ev0));
+    AGB_CUDA_TRY(cudaEventCreate(&ev1));
+    AGB_CUDA_TRY(cudaEventRecord(ev0, stream));
+  }
+  tf32x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
+  AGB_LAUNCH_CHECK();
+  if (ev0) {
+    AGB_CUDA_TRY(cudaEventRecord(ev1, stream));
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timing_recs.push_back(TimingRec{ev0, ev1, 8.0 * (double)M * (double)N * (double)K, M, N, K});
+  }
+  if (splits > 1) {
+    splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>(partials, splits, M, N, alpha, beta, C, ldc);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+// Scratch layout of the all-in-one entry: [256-byte status header][A planes][B planes][split-K partials].
 size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K) {
   if (M <= 0 || N <= 0 || K <= 0) return 256;
-  return plan_layout(M, N, K, 0).total;
+  return 256 + round_up((int64_t)tf32_planes_bytes(M, K), 256) + round_up((int64_t)tf32_planes_bytes(N, K), 256) +
+         tf32_partials_bytes(M, N, K);
 }
 
 agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
@@ -429,51 +489,21 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(A && B && C && scratch, "cgemm_tf32x3: null pointer");
   AGB_ARG_CHECK(((uintptr_t)scratch & 255) == 0, "cgemm_tf32x3: scratch must be 256-byte aligned");
-  if (K == 0) {
-    // C = beta*C
-    return zgemm(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, stream);
-  }
-  Layout L = plan_layout(M, N, K, scratch_bytes);
-  if (scratch_bytes < L.total) {
+  if (K == 0) return zgemm(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, stream);
+  size_t a_bytes = round_up((int64_t)tf32_planes_bytes(M, K), 256);
+  size_t b_bytes = round_up((int64_t)tf32_planes_bytes(N, K), 256);
+  if (scratch_bytes < 256 + a_bytes + b_bytes) {
     agb_set_error_message("cgemm_tf32x3: scratch too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;
   }
-  AGB_ARG_CHECK(L.Np / BN <= 0x7fffffff && L.Mp / BM <= 65535, "cgemm_tf32x3: grid too large");
   char* base = (char*)scratch;
-  int* err = (int*)base;
-  float* PA = (float*)(base + L.offA);
-  float* PB = (float*)(base + L.offB);
-  z64* part = L.splits > 1 ? (z64*)(base + L.offP) : nullptr;
-  {
-    dim3 g((unsigned)(L.Kp / 32 + (L.Kp % 32 ? 1 : 0)), (unsigned)(L.Mp / 32));
-    prep_kernel<<<g, 256, 0, stream>>>(A, M, K, sAm, sAk, conjA, L.Mp, L.Kp, PA);
-    AGB_LAUNCH_CHECK();
-    dim3 gb((unsigned)(L.Kp / 32 + (L.Kp % 32 ? 1 : 0)), (unsigned)(L.Np / 32));
-    prep_kernel<<<gb, 256, 0, stream>>>(B, N, K, sBn, sBk, conjB, L.Np, L.Kp, PB);
-    AGB_LAUNCH_CHECK();
-  }
-  CUtensorMap mA, mB;
-  if (!encode_planes(&mA, PA, 4 * L.Mp, L.Kp) || !encode_planes(&mB, PB, 4 * L.Np, L.Kp)) {
-    agb_set_error_message("cgemm_tf32x3: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
-    return AGB_ERR_CUDA;
-  }
-  static bool attr_set = false;
-  if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set = true;
-  }
-  GemmParams p;
-  p.M = M; p.N = N; p.nkb = L.nkb_split; p.nkb_total = (int)L.nkb;
-  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = part; p.err = err;
-  p.rowsA = L.Mp; p.rowsB = L.Np;
-  dim3 grid((unsigned)(L.Np / BN), (unsigned)(L.Mp / BM), (unsigned)L.splits);
-  tf32x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
-  AGB_LAUNCH_CHECK();
-  if (part) {
-    splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>(part, L.splits, M, N, alpha, beta, C, ldc);
-    AGB_LAUNCH_CHECK();
-  }
-  return AGB_OK;
+  float* PA = (float*)(base + 256);
+  float* PB = (float*)(base + 256 + a_bytes);
+  AGB_STATUS_TRY(tf32_prep_planes(A, M, K, sAm, sAk, conjA, PA, stream));
+  AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream));
+  size_t used = 256 + a_bytes + b_bytes;
+  return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + used),
+                          scratch_bytes - used, stream);
 }
 
 }  // namespace agb
@@ -489,6 +519,34 @@ agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, do
   return agb::cgemm_tf32x3(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                            (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
                            scratch, scratch_bytes, (cudaStream_t)stream);
+}
+
+void agb_gemm_timing_enable(int on) { agb::g_timing.store(on ? 1 : 0); }
+
+/* Synchronises the recorded events and reports, for tcgen05 GEMM launches whose
+ * M*N*K >= min_mnk: launch count, summed kernel milliseconds and summed algorithmic
+ * flops (8*M*N*K); then clears the records. */
+agb_status agb_gemm_timing_collect(double min_mnk, int* launches, double* ms, double* flops) {
+  std::lock_guard<std::mutex> lk(agb::g_timing_mu);
+  int n = 0;
+  double tms = 0, tfl = 0;
+  for (auto& r : agb::g_timing_recs) {
+    AGB_CUDA_TRY(cudaEventSynchronize(r.e1));
+    if ((double)r.M * (double)r.N * (double)r.K >= min_mnk) {
+      float e = 0;
+      AGB_CUDA_TRY(cudaEventElapsedTime(&e, r.e0, r.e1));
+      ++n;
+      tms += e;
+      tfl += r.flops;
+    }
+    cudaEventDestroy(r.e0);
+    cudaEventDestroy(r.e1);
+  }
+  agb::g_timing_recs.clear();
+  if (launches) *launches = n;
+  if (ms) *ms = tms;
+  if (flops) *flops = tfl;
+  return AGB_OK;
 }
 
 /* Reads and clears the error word a 3xTF32 GEMM keeps at the start of its scratch

@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Benchmark of the CISD_SO hot path on one GB300.
+
+Workload: synthetic spin-orbital CISD, o/v = 60/240 occupied/virtual spin
+orbitals (nso = 300, naux = 1200 Hermitian factors, seed 0, diagonal Fock from
+per-spatial-orbital energies).  A step is one mixed-precision CISD_SO
+iteration at DIIS steady state: the residual of apyib/ci_wfn.py:309-334 with
+every contraction as complex FP32 via 3xTF32 tcgen05 MMAs, the FP64 amplitude
+update, the FP64 DIIS Gram row and the FP64 extrapolation + energy + norms.
+The metric counts algorithmic work per residual,
+W = 8 * (o^2 v^4 / 2 + o^3 v^3 + o^4 v^2 / 2 + 5 o^2 v^3 + 5 o^3 v^2) flops
+(7.71e13 at 60/240), whatever the kernels actually execute.
+
+Also reported (measured once per run, outside the timed steps): the full
+mixed-precision solve (3xTF32 iterations, one FP64 base residual, defect
+correction) to the reference's convergence test, the FP64 residual time, the
+FP64 residual norm at the mixed solution (a-posteriori check), and the
+reference-path CPU time (the NumPy oracle) on a bounded sample.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Multi-GPU: replicas only (each rank solves its own copy; no collective on the
+data path); value = sum of per-rank work / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def alg_flops(o, v):
+    return 8.0 * (0.5 * o * o * v ** 4 + o ** 3 * v ** 3 + 0.5 * o ** 4 * v * v + 5 * o * o * v ** 3 + 5 * o ** 3 * v * v)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_oracle(budget_s=12.0, o=20, v=80):
+    """The NumPy oracle (restatement of apyib/ci_wfn.py:309-334) timed on the host cores."""
+    import importlib
+    ncores = len(os.sched_getaffinity(0))
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ.setdefault(k, str(ncores))
+    port = importlib.import_module("oracle.port")
+    from apyib_gb300 import synthetic
+    prob = synthetic.so_factors(o, v, seed=0)
+    blk = port.blocks_from_factors(prob.B, o)
+    F = prob.fock_so()
+    D_ia, D_ijab = port.so_denominators(prob.eps_o, prob.eps_v)
+    t1 = np.zeros((o, v), dtype=complex)
+    t2 = blk["vvoo"].transpose(2, 3, 0, 1) / D_ijab
+    port.cisd_so_residual(F, blk, t1, t2, 0.1, o)       # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        port.cisd_so_residual(F, blk, t1, t2, 0.1, o)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = (time.perf_counter() - t0) / n
+    return {"value": alg_flops(o, v) / dt / 1e12, "unit": "TFLOP/s", "cores": ncores, "kind": "port",
+            "sample": f"{n} CISD_SO residual evaluations of the NumPy oracle at o/v={o}/{v} "
+                      f"({dt:.3f} s each); the o/v=60/240 workload does not fit host RAM in NumPy"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    res = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline_oracle(budget_s=3.0)
+        if i >= args.warmup:
+            res.append(cb["value"])
+    val = float(np.mean(res))
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "CISD_SO residual, NumPy oracle (CPU)", "o": 20, "v": 80},
+            "cpu_baseline": dict(cb, value=val),
+            "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+METRIC = "CISD_SO iteration TFLOP/s (algorithmic), mixed 3xTF32 + FP64 refinement, synthetic o/v=60/240"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--o", type=int, default=60)
+    ap.add_argument("--v", type=int, default=240)
+    ap.add_argument("--no-solve", action="store_true", help="skip the once-per-run full solve")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import ctypes
+
+    import torch
+
+    from apyib_gb300 import _lib, synthetic
+    from apyib_gb300.cisd import CISDPlan, _DIIS, solve
+    from apyib_gb300.device import ptr, stream_ptr
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = _lib.load()
+    o, v = args.o, args.v
+    W = alg_flops(o, v)
+    prob = synthetic.so_factors(o, v, seed=0)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    t_setup = time.perf_counter()
+    plan = CISDPlan(o, v, mixed=True)
+    plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
+    plan.blocks_from_factors(torch.as_tensor(prob.B))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    del prob
+
+    # ---- iteration state
+    t = plan.guess()
+    E, _, _ = plan.combine([t], [1.0], t, t)
+    diis = _DIIS(plan)
+    state = {"t": t, "E": E, "first": True}
+
+    def iteration():
+        r = plan.residual(state["t"], state["E"], _lib.PREC_TF32X3)
+        tn = plan.update(state["t"], r)
+        diis.push(r, tn, state["first"])
+        state["first"] = False
+        c = diis.coefficients()
+        E, s1, s2 = plan.combine(diis.t, c, state["t"], state["t"])
+        state["E"] = E
+        return E
+
+    for _ in range(args.warmup):
+        iteration()
+    plan.check_status()
+    torch.cuda.synchronize()
+
+    # ---- timed device-resident steps
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    lib.agb_gemm_timing_enable(1)
+    n0 = lib.agb_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        iteration()
+    ev1.record()
+    torch.cuda.synchronize()
+    launches = lib.agb_launch_count() - n0
+    lib.agb_gemm_timing_enable(0)
+    nl, kms, kfl = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+    pq = (o * (o - 1) // 2) * (v * (v - 1) // 2) ** 2       # vvvv ladder M*N*K
+    ring = float(o * v) ** 3
+    _lib.call("agb_gemm_timing_collect", min(pq, ring) * 0.99, ctypes.byref(nl), ctypes.byref(kms), ctypes.byref(kfl))
+    plan.check_status()
+    dev_ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        tt = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = tt.item()
+    clocks = sampler.stop()
+
+    # ---- e2e: the same iteration with amplitudes resident on the host (pinned)
+    host_t = torch.empty(plan.n, dtype=torch.complex128, pin_memory=True)
+    host_t.copy_(state["t"].cpu())
+    host_out = torch.empty(plan.n, dtype=torch.complex128, pin_memory=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        state["t"].copy_(host_t, non_blocking=True)
+        iteration()
+        host_out.copy_(state["t"], non_blocking=True)
+        host_t, host_out = host_out, host_t
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = tt.item()
+    nbytes = plan.n * 16
+
+    peaks, peak_kind = measured_peaks()
+    tf32_peak = peaks["bf16_tflops"] / 2.0        # tcgen05 kind::tf32 issues at half the f16/bf16 rate
+    gemm_peak = tf32_peak / 3.0                   # 3 TF32 products per FP32 product
+    kern_ach = (kfl.value / (kms.value / 1e3) / 1e12) if kms.value > 0 else None
+
+    out = {
+        "metric": METRIC, "value": world * W / (dev_ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (3xTF32 tensor core) + c128 (update/DIIS/sums)",
+        "data": "synthetic (seeded Hermitian factors, BASELINE config shape o/v=60/240)",
+        "config": {"workload": "CISD_SO mixed-precision iteration, synthetic o/v=60/240 spin orbitals",
+                   "o": o, "v": v, "naux": 4 * (o + v), "l2": "inputs > L2 (ERI blocks ~45 GB in HBM)",
+                   "parallelism": f"replicas x{world}", "alg_flops_per_step": W},
+        "e2e": {"value": world * W / (e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
+                     "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",
+                     "frac": (kern_ach / gemm_peak) if kern_ach else None, "traffic": None,
+                     "peak_note": f"{peak_kind} bf16 {peaks['bf16_tflops']} TF/s / 2 (tf32 rate) / 3 (3xTF32)",
+                     "launches_timed": nl.value},
+        "clocks": clocks,
+        "setup_s": setup_s,
+    }
+
+    if not args.no_solve and rank == 0:
+        # Full mixed solve (fresh amplitudes) + FP64 residual timing + a-posteriori FP64 check.
+        params = dict(max_iterations=60, DIIS=True, e_convergence=1e-10, d_convergence=1e-8)
+        hist = []
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        Em, tm = solve(plan, params, precision="mixed", history=hist)
+        torch.cuda.synchronize()
+        solve_s = time.perf_counter() - ts
+        stats = hist[-1]
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        r64 = plan.residual(tm, Em, _lib.PREC_FP64)
+        f1.record()
+        torch.cuda.synchronize()
+        fp64_res_s = f0.elapsed_time(f1) / 1e3
+        # amplitude correction implied by the FP64 residual at the mixed solution
+        corr = plan.update(torch.zeros_like(tm), r64)
+        max_corr = corr.abs().max().item()
+        iters = len(hist) - 1
+        tf32_res_s = dev_ms / 1e3
+        out["solve"] = {
+            "mixed_solve_s": solve_s, "E_mixed": [Em.real, Em.imag], "iterations": iters,
+            "tf32_residuals": stats["tf32_residuals"], "fp64_residuals": stats["fp64_residuals"],
+            "fp64_residual_s": fp64_res_s,
+            "fp64_solve_estimate_s": iters * (fp64_res_s + tf32_res_s * 0.0) + iters * 0.05,
+            "fp64_solve_estimate_note": "iterations of the mixed solve x measured FP64 residual time",
+            "posterior_max_amplitude_correction": max_corr,
+        }
+    if not args.no_cpu and rank == 0:
+        out["cpu_baseline"] = cpu_baseline_oracle()
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -74,6 +74,13 @@ agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, do
                             double beta_re, double beta_im, void* C, int64_t ldc,
                             void* scratch, size_t scratch_bytes, void* stream);
 
+/* Benchmark instrumentation (no reference counterpart): when enabled, every
+ * tcgen05 GEMM launch is bracketed by CUDA events on its stream;
+ * agb_gemm_timing_collect reports launches, kernel milliseconds and
+ * algorithmic flops (8*M*N*K) of launches with M*N*K >= min_mnk, then clears. */
+void agb_gemm_timing_enable(int on);
+agb_status agb_gemm_timing_collect(double min_mnk, int* launches, double* ms, double* flops);
+
 /* Reads and clears the status word a 3xTF32 GEMM keeps in the first bytes of its
  * scratch (zero it once before first use): AGB_ERR_TIMEOUT if a bounded
  * device-side wait ran out.  Synchronises the stream. */
