@@ -397,10 +397,10 @@ __device__ __forceinline__ void block_reduce_store(z64 (&acc)[NV], z64* out) {
   }
 }
 
-// out[k] = sum over blocks of partial[b*nv + k], fixed order (deterministic)
-__global__ void finish_partials_kernel(const z64* __restrict__ partial, int nblocks, int nv, z64* out) {
+// out[k] = sum over blocks of partial[b*nv + k] for k < count <= nv, fixed order (deterministic)
+__global__ void finish_partials_kernel(const z64* __restrict__ partial, int nblocks, int nv, int count, z64* out) {
   int k = threadIdx.x;
-  if (k >= nv) return;
+  if (k >= count || k >= nv) return;
   z64 s = zmk(0, 0);
   for (int b = 0; b < nblocks; ++b) s = zadd(s, partial[(int64_t)b * nv + k]);
   out[k] = s;
@@ -941,7 +941,7 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
   AGB_LAUNCH_CHECK();
   int nv = ny <= 4 ? 4 : (ny <= 8 ? 8 : 16);
   // finish only the first ny of the nv slots (stride nv)
-  finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, (z64*)out);
+  finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -965,7 +965,7 @@ agb_status agb_cisd_combine(agb_cisd_plan* P, const void* const* ys, const doubl
   A.t_old = (const z64*)t_old; A.t_new = (z64*)t_new; A.ew = P->EW;
   combine_kernel<<<kRedBlocks, 256, 0, st>>>(A, (z64*)partials);
   AGB_LAUNCH_CHECK();
-  finish_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kRedBlocks, 3, (z64*)out3);
+  finish_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kRedBlocks, 3, 3, (z64*)out3);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
