@@ -22,6 +22,7 @@ AGB_ERR_WORKSPACE = 5
 
 PREC_FP64 = 0
 PREC_TF32X3 = 1
+PREC_DF64 = 2
 
 PLAN_MIXED = 1
 PLAN_NO_SINGLES = 2
@@ -44,6 +45,8 @@ SIGNATURES = {
     "agb_last_error": (_c.c_char_p, []),
     "agb_zgemm": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp, _i64,
                          _vp]),
+    "agb_zgemm_df64": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
+                              _i64, _vp]),
     "agb_cgemm_tf32x3_scratch_bytes": (_sz, [_i64, _i64, _i64]),
     "agb_cgemm_tf32x3": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
                                 _i64, _vp, _sz, _vp]),
@@ -61,7 +64,7 @@ SIGNATURES = {
     "agb_cisd_blocks_from_mo": (_int, [_vp, _vp, _vp]),
     "agb_cisd_blocks_from_so": (_int, [_vp, _vp, _vp]),
     "agb_cisd_factor_scratch_bytes": (_sz, [_vp, _i64]),
-    "agb_cisd_blocks_from_factors": (_int, [_vp, _vp, _i64, _vp, _sz, _vp]),
+    "agb_cisd_blocks_from_factors": (_int, [_vp, _vp, _i64, _vp, _sz, _int, _vp]),
     "agb_cisd_residual": (_int, [_vp, _int, _vp, _d, _d, _int, _vp, _vp]),
     "agb_cisd_status": (_int, [_vp, _vp]),
     "agb_cisd_update": (_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -72,6 +75,7 @@ SIGNATURES = {
     "agb_cisd_pack": (_int, [_vp, _vp, _vp, _vp, _vp]),
     "agb_cisd_guess": (_int, [_vp, _vp, _vp]),
     "agb_mp2_so": (_int, [_vp, _vp, _vp, _vp, _sz, _vp]),
+    "agb_mp2_spatial": (_int, [_vp, _i64, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "agb_ao2mo_scratch_bytes": (_sz, [_i64, _i64]),
     "agb_ao2mo": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _sz, _int, _vp]),
     "agb_jk_fock": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp]),

@@ -9,7 +9,12 @@ expectation value of the corresponding operator in the normalised CI state
     dE = sum_pq D_pq dF_pq + sum_pqrs Gamma_pqrs d<pq|rs>
 
 with the one- and two-particle densities of the reference's own adjoint
-check (apyib/ci_wfn.py:382-411, restated in oracle/port.py).  The densities
+check (apyib/ci_wfn.py:382-411, restated in oracle/port.py).  This holds
+for integral changes that keep F_ov = F_vo = 0 (canonical orbitals): the
+reference's doubles equations omit the F_ov t1 coupling, so with a non-zero
+occupied-virtual Fock block its projective energy is not stationary and the
+density gradient of that block is not the derivative of the solver's energy.
+Two-electron perturbations are unrestricted.  The densities
 are built on the GPU from the converged amplitudes with the library's
 complex GEMMs; the vvvv block Gamma_abcd = 1/4 sum_ij t2*_ijab t2_ijcd is
 recomputed in the backward as a packed (a<b, c<d) GEMM over i<j rather than
@@ -52,6 +57,10 @@ def densities(plan, t, precision=_lib.PREC_FP64):
     o, v = plan.o, plan.v
     nso = o + v
     dev = device()
+
+    def mm(*a, **k):
+        return zmm(*a, precision=precision, **k)
+
     t1, t2 = plan.unpack(t)
     if t1 is None:
         t1 = torch.zeros((o, v), dtype=torch.complex128, device=dev)
@@ -65,38 +74,38 @@ def densities(plan, t, precision=_lib.PREC_FP64):
     O, V = slice(0, o), slice(o, nso)
     D = torch.zeros((nso, nso), dtype=torch.complex128, device=dev)
     T2m = t2.reshape(o, o * v * v)
-    D[O, O] = -(zmm(t1, t1, transB=True, conjB=True) + 0.5 * zmm(T2m, T2m, transB=True, conjB=True))
+    D[O, O] = -(mm(t1, t1, transB=True, conjB=True) + 0.5 * mm(T2m, T2m, transB=True, conjB=True))
     Tv = t2.permute(2, 0, 1, 3).reshape(v, o * o * v).contiguous()
-    D[V, V] = zmm(t1, t1, transA=True, conjA=True) + 0.5 * zmm(Tv, Tv, conjA=True, transB=True)
+    D[V, V] = mm(t1, t1, transA=True, conjA=True) + 0.5 * mm(Tv, Tv, conjA=True, transB=True)
     Tr = t2.permute(0, 2, 1, 3).reshape(o * v, o * v).contiguous()       # [(i,a),(j,b)] = t2[i,j,a,b]
-    D[O, V] = t0 * t1 + zmm(Tr, t1c.reshape(o * v, 1)).reshape(o, v)
-    D[V, O] = (t0 * t1c + zmm(Tr, t1.reshape(o * v, 1), conjA=True).reshape(o, v)).T
+    D[O, V] = t0 * t1 + mm(Tr, t1c.reshape(o * v, 1)).reshape(o, v)
+    D[V, O] = (t0 * t1c + mm(Tr, t1.reshape(o * v, 1), conjA=True).reshape(o, v)).T
     G = {}
     # oooo: 1/4 sum_ab t2*[k,l,a,b] t2[i,j,a,b] -> [i,j,k,l]
     Toov = t2.reshape(o * o, v * v)
-    G["oooo"] = 0.25 * zmm(Toov, Toov, transB=True, conjB=True).reshape(o, o, o, o)
+    G["oooo"] = 0.25 * mm(Toov, Toov, transB=True, conjB=True).reshape(o, o, o, o)
     # ovvo / ovov from t1: 'ja,ib->iabj' and -'ja,ib->iajb'
     P = torch.einsum("ja,ib->iabj", t1c, t1)          # outer product (no contraction)
     G["ovvo"] = P.contiguous()
     G["ovov"] = (-P.permute(0, 1, 3, 2)).contiguous()
     # voov / vovo: 'jkac,ikbc->aijb' and -'jkac,ikbc->aibj'
     Tk = t2.permute(0, 2, 1, 3).reshape(o * v, o * v)   # [(j,a),(k,c)]
-    Q = zmm(Tk, Tk, conjA=True, transB=True).reshape(o, v, o, v)      # Q[j,a,i,b] = sum_kc t2*[jkac] t2[ikbc]
+    Q = mm(Tk, Tk, conjA=True, transB=True).reshape(o, v, o, v)      # Q[j,a,i,b] = sum_kc t2*[jkac] t2[ikbc]
     G["voov"] = Q.permute(1, 2, 0, 3).contiguous()                    # [a,i,j,b]
     G["vovo"] = (-Q.permute(1, 2, 3, 0)).contiguous()                 # [a,i,b,j]
     G["oovv"] = 0.5 * t0 * t2
     G["vvoo"] = (0.5 * t0 * t2.conj().permute(2, 3, 0, 1)).contiguous()
     # vovv: 'ja,ijcb->aibc'
-    G["vovv"] = zmm(t1c, t2.permute(1, 0, 3, 2).reshape(o, o * v * v), transA=True).reshape(v, o, v, v)
+    G["vovv"] = mm(t1c, t2.permute(1, 0, 3, 2).reshape(o, o * v * v), transA=True).reshape(v, o, v, v)
     # ovoo: -'kjab,ib->iajk'
     Tb = t2.conj().permute(3, 2, 1, 0).reshape(v, v * o * o).contiguous()   # [b,(a,j,k)] = t2*[k,j,a,b]
-    G["ovoo"] = (-zmm(t1, Tb).reshape(o, v, o, o)).contiguous()             # X[i,(a,j,k)] = sum_b t1[i,b] Tb
+    G["ovoo"] = (-mm(t1, Tb).reshape(o, v, o, o)).contiguous()             # X[i,(a,j,k)] = sum_b t1[i,b] Tb
 
     # vvvo: 'jiab,jc->abci'
-    G["vvvo"] = zmm(t2.conj().permute(2, 3, 1, 0).reshape(v * v * o, o), t1).reshape(v, v, o, v).permute(
+    G["vvvo"] = mm(t2.conj().permute(2, 3, 1, 0).reshape(v * v * o, o), t1).reshape(v, v, o, v).permute(
         0, 1, 3, 2).contiguous()
     # ooov: -'kb,ijba->ijka'
-    G["ooov"] = (-zmm(t2.permute(0, 1, 3, 2).reshape(o * o * v, v), t1c, transB=True)
+    G["ooov"] = (-mm(t2.permute(0, 1, 3, 2).reshape(o * o * v, v), t1c, transB=True)
                  .reshape(o, o, v, o).permute(0, 1, 3, 2)).contiguous()
     # vvvv (packed, recomputed): Gp[(ab),(cd)] = sum_{i<j} t2p*[ij,ab] t2p[ij,cd]; Gamma = Gp/2 with signs
     n1v = plan.n1

@@ -9,11 +9,14 @@ t = [t1 (o*v) | t2p (o(o-1)/2 * v(v-1)/2)] held in HBM.
 Precision modes:
   * ``fp64``  - every contraction in FP64 (the parity mode);
   * ``mixed`` - residuals as complex FP32 with 3xTF32 tensor-core products
-    until the energy change reaches ``switch_tol``, then one FP64 residual at
-    a base point t_b and further iterations whose residual is
+    until the energy change reaches ``switch_tol``, then one high-precision
+    residual at a base point t_b and further iterations whose residual is
     r(t) = r64(t_b) + L32(t - t_b) - E_b (t - t_b) - (E - E_b) t,
     i.e. only the small amplitude change goes through the FP32 tensor cores
-    (defect correction).  DIIS, the update and all sums stay FP64.
+    (defect correction).  DIIS, the update and all sums stay FP64.  The base
+    residual's GEMMs run in double-float on the FP32 pipe (``base_precision
+    ='df64'``, ~2^-44 relative, several times faster than GB300's FP64 pipe)
+    or in FP64 (``'fp64'``); its elementwise work is FP64 either way.
 """
 from __future__ import annotations
 
@@ -69,26 +72,28 @@ class CISDPlan:
 
     # ------------------------------------------------------------ set-up
     def set_fock(self, F_SO, eps_so):
-        F = F_SO.to(device=device(), dtype=torch.complex128).contiguous()
+        F = F_SO.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
         e = torch.as_tensor(eps_so, dtype=torch.float64).to(device()).contiguous()
         self._F, self._eps = F, e
         _lib.call("agb_cisd_set_fock", self._h, ptr(F), ptr(e), stream_ptr())
 
     def blocks_from_mo(self, ERI_MO):
-        g = ERI_MO.to(device=device(), dtype=torch.complex128).contiguous()
+        g = ERI_MO.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
         _lib.call("agb_cisd_blocks_from_mo", self._h, ptr(g), stream_ptr())
 
     def blocks_from_so(self, ERI_SO):
-        g = ERI_SO.to(device=device(), dtype=torch.complex128).contiguous()
+        g = ERI_SO.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
         _lib.call("agb_cisd_blocks_from_so", self._h, ptr(g), stream_ptr())
 
-    def blocks_from_factors(self, B):
-        Bd = B.to(device=device(), dtype=torch.complex128).contiguous()
+    def blocks_from_factors(self, B, precision=_lib.PREC_FP64):
+        """Blocks from Hermitian factors; precision PREC_FP64 or PREC_DF64 (double-float
+        products, ~1e-13 relative, several times faster on GB300)."""
+        Bd = B.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
         naux = Bd.shape[0]
         nb = _lib.load().agb_cisd_factor_scratch_bytes(self._h, naux)
         buf, sptr, _ = workspace(nb)
         _lib.call("agb_cisd_blocks_from_factors", self._h, ptr(Bd), ctypes.c_int64(naux), _vp(sptr),
-                  ctypes.c_size_t(nb), stream_ptr())
+                  ctypes.c_size_t(nb), int(precision), stream_ptr())
         torch.cuda.current_stream().synchronize()
         del buf
 
@@ -150,8 +155,8 @@ class CISDPlan:
 
     def pack(self, t1, t2):
         t = self.vec()
-        t2 = t2.to(device=device(), dtype=torch.complex128).contiguous()
-        t1 = None if t1 is None else t1.to(device=device(), dtype=torch.complex128).contiguous()
+        t2 = t2.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
+        t1 = None if t1 is None else t1.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
         _lib.call("agb_cisd_pack", self._h, ptr(t1), ptr(t2), ptr(t), stream_ptr())
         return t
 
@@ -215,7 +220,8 @@ class _DIIS:
         return _bordered_diis(self.B)
 
 
-def solve(plan, params, precision="fp64", print_level=0, history=None, switch_tol=1e-8, max_mixed=None):
+def solve(plan, params, precision="fp64", print_level=0, history=None, switch_tol=1e-8, max_mixed=None,
+          base_precision="df64"):
     """Jacobi + DIIS CISD_SO (plan.singles) or CID_SO iteration.
 
     Returns (E, t) with t the packed amplitude vector on the device.  The
@@ -279,7 +285,7 @@ def solve(plan, params, precision="fp64", print_level=0, history=None, switch_to
             if (it > 1 and abs(dE) < switch_tol) or stalled or capped or conv:
                 # switch to defect correction around an FP64 base residual
                 t_b = t.clone()
-                r_b = plan.residual(t_b, E, _lib.PREC_FP64)
+                r_b = plan.residual(t_b, E, _lib.PREC_DF64 if base_precision == "df64" else _lib.PREC_FP64)
                 stats["fp64_residuals"] += 1
                 base = (t_b, E, r_b)
                 phase = "refine"

@@ -19,6 +19,9 @@ namespace agb {
 agb_status zgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                     void* scratch, size_t scratch_bytes, cudaStream_t stream);
+agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                     void* scratch, size_t scratch_bytes, cudaStream_t stream);
 agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
                  cudaStream_t stream);
 agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
@@ -602,6 +605,9 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
     return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
                             P->gemm_scratch_bytes - off, st);
   }
+  if (prec == AGB_PREC_DF64)
+    return dfgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, (char*)P->gemm_scratch + 256,
+                     P->gemm_scratch_bytes - 256, st);
   // FP64 split-K partials start past the 256-byte status header of the scratch.
   return zgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, (char*)P->gemm_scratch + 256,
                   P->gemm_scratch_bytes - 256, st);
@@ -775,8 +781,10 @@ size_t agb_cisd_factor_scratch_bytes(const agb_cisd_plan* P, int64_t naux) {
 }
 
 agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* P, const void* Bf, int64_t naux, void* scratch,
-                                        size_t scratch_bytes, void* stream) {
+                                        size_t scratch_bytes, int precision, void* stream) {
   AGB_ARG_CHECK(P && P->ws && Bf && naux > 0, "blocks_from_factors: bad argument");
+  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_DF64,
+                "blocks_from_factors: precision must be AGB_PREC_FP64 or AGB_PREC_DF64");
   if (!scratch || scratch_bytes < agb_cisd_factor_scratch_bytes(P, naux)) {
     agb_set_error_message("blocks_from_factors: scratch too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;
@@ -802,6 +810,9 @@ agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* P, const void* Bf, int64_
     const z64* A = sub[c0 == 'v'][c1 == 'v'];
     const z64* B = sub[c2 == 'v'][c3 == 'v'];
     int64_t M = rlen(P, c0) * rlen(P, c1), N = rlen(P, c2) * rlen(P, c3);
+    if (precision == AGB_PREC_DF64)
+      return dfgemm_ex(M, N, naux, zmk(1, 0), A, naux, 1, 0, B, 1, naux, 0, zmk(0, 0), out, N,
+                       (char*)P->gemm_scratch + 256, P->gemm_scratch_bytes - 256, st);
     return zgemm_ex(M, N, naux, zmk(1, 0), A, naux, 1, 0, B, 1, naux, 0, zmk(0, 0), out, N,
                     (char*)P->gemm_scratch + 256, P->gemm_scratch_bytes - 256, st);
   };
@@ -829,8 +840,9 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
                              void* stream) {
   AGB_ARG_CHECK(P && P->ws && tv && rv, "residual: bad argument");
   AGB_ARG_CHECK(!P->mp2_only, "residual: plan created with AGB_PLAN_MP2");
-  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || prec == AGB_PREC_TF32X3, "residual: unknown precision");
-  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || P->mixed, "residual: plan created without AGB_PLAN_MIXED");
+  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || prec == AGB_PREC_TF32X3 || prec == AGB_PREC_DF64,
+                "residual: unknown precision");
+  AGB_ARG_CHECK(prec != AGB_PREC_TF32X3 || P->mixed, "residual: plan created without AGB_PLAN_MIXED");
   cudaStream_t st = (cudaStream_t)stream;
   const int o = P->o, v = P->v;
   const int64_t ov = P->ov, po = P->po, pv = P->pv, n1 = P->n1;

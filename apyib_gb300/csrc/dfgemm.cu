@@ -1,0 +1,189 @@
+// Complex GEMM in double-float ("df64") arithmetic on the FP32 CUDA cores.
+//
+// GB300's FP64 pipe issues about two DFMA per clock per SM, while the FP32 pipe
+// issues 128 FMA per clock per SM.  Each FP64 operand is split on load into a
+// float pair x = x_hi + x_lo (48 significant bits); products use the exact
+// FMA split p = x_hi*y_hi, e = fma(x_hi, y_hi, -p) plus the two cross terms,
+// and the running sum is a float pair updated with Knuth's two-sum, so the
+// result carries ~2^-44 relative error after 10^4-term sums: far below what
+// the iterative-refinement residual needs, at roughly five times the FP64
+// GEMM's rate.  Same contract and strides as the FP64 zgemm.
+#include "common.cuh"
+
+namespace agb {
+
+namespace {
+constexpr int BM = 64, BN = 64, BK = 16;
+
+struct DfArgs {
+  int64_t M, N, K;
+  z64 alpha, beta;
+  const z64* A; int64_t sAm, sAk; int conjA;
+  const z64* B; int64_t sBk, sBn; int conjB;
+  z64* C; int64_t ldc;
+  int64_t kchunk;
+  z64* partial;
+};
+
+// (re_hi, re_lo, im_hi, im_lo)
+__device__ __forceinline__ float4 split_z(z64 v) {
+  float rh = __double2float_rn(v.x);
+  float rl = __double2float_rn(v.x - (double)rh);
+  float ih = __double2float_rn(v.y);
+  float il = __double2float_rn(v.y - (double)ih);
+  return make_float4(rh, rl, ih, il);
+}
+
+// (s, c) += (xh + xl) * (yh + yl).  The _rn intrinsics keep the compiler from
+// contracting the rounded product into the two-sum (which would void it).
+__device__ __forceinline__ void df_mac(float& s, float& c, float xh, float xl, float yh, float yl) {
+  float p = __fmul_rn(xh, yh);
+  float e = fmaf(xh, yh, -p);
+  e = fmaf(xh, yl, e);
+  e = fmaf(xl, yh, e);
+  float t = __fadd_rn(s, p);
+  float z = __fsub_rn(t, s);
+  float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  c = __fadd_rn(c, __fadd_rn(err, e));
+  s = t;
+}
+
+__global__ void __launch_bounds__(256) dfgemm_kernel(DfArgs p) {
+  __shared__ float4 As[BK][BM + 1];
+  __shared__ float4 Bs[BK][BN + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, tid = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  float sr[4][4], cr[4][4], si[4][4], ci[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sr[i][j] = cr[i][j] = si[i][j] = ci[i][j] = 0.f;
+  const bool a_kfast = (p.sAk == 1), b_nfast = (p.sBn == 1);
+  const int64_t kbeg = (int64_t)blockIdx.z * p.kchunk;
+  const int64_t kend = (kbeg + p.kchunk < p.K) ? kbeg + p.kchunk : p.K;
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+    for (int r = 0; r < (BM * BK) / 256; ++r) {
+      int idx = tid + 256 * r, m, k;
+      if (a_kfast) { k = idx % BK; m = idx / BK; } else { m = idx % BM; k = idx / BM; }
+      int64_t gm = m0 + m, gk = k0 + k;
+      z64 v = zmk(0, 0);
+      if (gm < p.M && gk < kend) {
+        v = p.A[gm * p.sAm + gk * p.sAk];
+        if (p.conjA) v.y = -v.y;
+      }
+      As[k][m] = split_z(v);
+    }
+#pragma unroll
+    for (int r = 0; r < (BN * BK) / 256; ++r) {
+      int idx = tid + 256 * r, n, k;
+      if (b_nfast) { n = idx % BN; k = idx / BN; } else { k = idx % BK; n = idx / BK; }
+      int64_t gn = n0 + n, gk = k0 + k;
+      z64 v = zmk(0, 0);
+      if (gn < p.N && gk < kend) {
+        v = p.B[gk * p.sBk + gn * p.sBn];
+        if (p.conjB) v.y = -v.y;
+      }
+      Bs[k][n] = split_z(v);
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < BK; ++kk) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          // re += ar*br - ai*bi ; im += ar*bi + ai*br
+          df_mac(sr[i][j], cr[i][j], a[i].x, a[i].y, b[j].x, b[j].y);
+          df_mac(sr[i][j], cr[i][j], a[i].z, a[i].w, -b[j].z, -b[j].w);
+          df_mac(si[i][j], ci[i][j], a[i].x, a[i].y, b[j].z, b[j].w);
+          df_mac(si[i][j], ci[i][j], a[i].z, a[i].w, b[j].x, b[j].y);
+        }
+    }
+    __syncthreads();
+  }
+  const bool use_beta = (p.beta.x != 0.0 || p.beta.y != 0.0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int64_t gm = m0 + ty + 16 * i;
+    if (gm >= p.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t gn = n0 + tx + 16 * j;
+      if (gn >= p.N) continue;
+      z64 acc = zmk((double)sr[i][j] + (double)cr[i][j], (double)si[i][j] + (double)ci[i][j]);
+      if (p.partial) {
+        p.partial[((int64_t)blockIdx.z * p.M + gm) * p.N + gn] = acc;
+      } else {
+        z64* c = p.C + gm * p.ldc + gn;
+        z64 out = zmul(p.alpha, acc);
+        if (use_beta) out = zadd(out, zmul(p.beta, *c));
+        *c = out;
+      }
+    }
+  }
+}
+
+__global__ void df_splitk_sum_kernel(const z64* __restrict__ partial, int splits, int64_t M, int64_t N, z64 alpha,
+                                     z64 beta, z64* C, int64_t ldc) {
+  int64_t total = M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    z64 s = zmk(0, 0);
+    for (int z = 0; z < splits; ++z) s = zadd(s, partial[(int64_t)z * total + e]);
+    int64_t m = e / N, n = e % N;
+    z64* c = C + m * ldc + n;
+    z64 out = zmul(alpha, s);
+    if (beta.x != 0.0 || beta.y != 0.0) out = zadd(out, zmul(beta, *c));
+    *c = out;
+  }
+}
+}  // namespace
+
+agb_status zgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                    const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                    void* scratch, size_t scratch_bytes, cudaStream_t stream);
+int zgemm_splits(int64_t M, int64_t N, int64_t K, size_t scratch_bytes);
+
+agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                     void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  AGB_ARG_CHECK(M >= 0 && N >= 0 && K >= 0, "dfgemm: negative size");
+  if (M == 0 || N == 0) return AGB_OK;
+  if (K == 0 || (alpha.x == 0.0 && alpha.y == 0.0))
+    return zgemm_ex(M, N, K, alpha, A, sAm, sAk, conjA, B, sBk, sBn, conjB, beta, C, ldc, nullptr, 0, stream);
+  AGB_ARG_CHECK(A && B && C, "dfgemm: null pointer");
+  AGB_ARG_CHECK((M + BM - 1) / BM <= 65535, "dfgemm: M too large for grid");
+  int splits = scratch ? zgemm_splits(M, N, K, scratch_bytes) : 1;
+  int64_t kchunk = K;
+  if (splits > 1) {
+    kchunk = (K + splits - 1) / splits;
+    kchunk = (kchunk + BK - 1) / BK * BK;
+    splits = (int)((K + kchunk - 1) / kchunk);
+  }
+  DfArgs p{M, N, K, alpha, beta, A, sAm, sAk, conjA, B, sBk, sBn, conjB, C, ldc, kchunk,
+           splits > 1 ? (z64*)scratch : nullptr};
+  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)splits);
+  dfgemm_kernel<<<grid, 256, 0, stream>>>(p);
+  AGB_LAUNCH_CHECK();
+  if (splits > 1) {
+    df_splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>((const z64*)scratch, splits, M, N, alpha, beta,
+                                                                    C, ldc);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+}  // namespace agb
+
+extern "C" agb_status agb_zgemm_df64(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
+                                     int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,
+                                     int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* stream) {
+  return agb::dfgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
+                        (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, nullptr, 0,
+                        (cudaStream_t)stream);
+}

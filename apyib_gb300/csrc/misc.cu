@@ -372,3 +372,59 @@ agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const v
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Closed-shell (spatial-orbital) MP2, apyib/mp2_wfn.py:42-59:
+//   t2[i,j,a,b] = <ab|ij> / D_ijab,  E = sum (2 <ij|ab> - <ij|ba>) t2,  <pq|rs> = (pr|qs).
+namespace agb {
+namespace {
+__global__ void __launch_bounds__(256) mp2_spatial_kernel(const z64* __restrict__ g, int64_t n, int no, int nv,
+                                                          const double* __restrict__ eps, z64* __restrict__ t2,
+                                                          z64* __restrict__ partial) {
+  z64 acc = zmk(0, 0);
+  const int64_t total = (int64_t)no * no * nv * nv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int b = (int)(e % nv);
+    int64_t r = e / nv;
+    int a = (int)(r % nv);
+    r /= nv;
+    int j = (int)(r % no), i = (int)(r / no);
+    int64_t A = no + a, B = no + b;
+    z64 ab_ij = g[((A * n + i) * n + B) * n + j];   // (ai|bj)
+    z64 ij_ab = g[(((int64_t)i * n + A) * n + j) * n + B];   // (ia|jb)
+    z64 ij_ba = g[(((int64_t)i * n + B) * n + j) * n + A];   // (ib|ja)
+    double inv = 1.0 / (eps[i] + eps[j] - eps[A] - eps[B]);
+    z64 t = zmk(ab_ij.x * inv, ab_ij.y * inv);
+    t2[e] = t;
+    acc = zadd(acc, zmul(zsub(zscale(ij_ab, 2.0), ij_ba), t));
+  }
+  __shared__ z64 sh[32];
+  acc = warp_sum(acc);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = acc;
+  __syncthreads();
+  if (w == 0) {
+    acc = lane < (int)(blockDim.x >> 5) ? sh[lane] : zmk(0, 0);
+    acc = warp_sum(acc);
+    if (lane == 0) partial[blockIdx.x] = acc;
+  }
+}
+}  // namespace
+}  // namespace agb
+
+extern "C" agb_status agb_mp2_spatial(const void* ERI_MO, int64_t nmo, int64_t no, const double* eps, void* t2,
+                                      void* E_out, void* partials, size_t partials_bytes, void* stream) {
+  using namespace agb;
+  AGB_ARG_CHECK(ERI_MO && eps && t2 && E_out && nmo > 0 && no > 0 && no < nmo, "mp2_spatial: bad argument");
+  if (!partials || partials_bytes < sizeof(z64) * kMp2Blocks) {
+    agb_set_error_message("mp2_spatial: partials buffer too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  mp2_spatial_kernel<<<kMp2Blocks, 256, 0, st>>>((const z64*)ERI_MO, nmo, (int)no, (int)(nmo - no), eps, (z64*)t2,
+                                                 (z64*)partials);
+  AGB_LAUNCH_CHECK();
+  sum_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}

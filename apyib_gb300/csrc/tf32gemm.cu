@@ -41,14 +41,16 @@ agb_status zgemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 16;   // BK in fp32 elements (64 bytes)
-constexpr int STAGES = 3;
-constexpr int PLANE_TILE_BYTES = 128 * BK * 4;               // 8 KB
-constexpr int STAGE_BYTES = 8 * PLANE_TILE_BYTES;            // 4 A planes + 4 B planes = 64 KB
+constexpr int BM = 128, BN = 256, BK = 16;   // BK in fp32 elements (64 bytes)
+constexpr int STAGES = 2;
+constexpr int A_TILE_BYTES = BM * BK * 4;                    // 8 KB per A plane tile
+constexpr int B_TILE_BYTES = BN * BK * 4;                    // 16 KB per B plane tile
+constexpr int STAGE_BYTES = 4 * (A_TILE_BYTES + B_TILE_BYTES);   // 96 KB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int THREADS = 192;
-constexpr unsigned TMEM_COLS = 256;
+constexpr unsigned TMEM_COLS = 2 * BN;                       // Re and Im accumulators
 constexpr long long kWaitCycles = 8000000000LL;  // ~4 s at 2 GHz
+constexpr int kGroupM = 12;                      // tile rows per raster group
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -168,7 +170,16 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile_n = blockIdx.x, tile_m = blockIdx.y, split = blockIdx.z;
+  // Grouped raster: CTAs launched together cover a band of kGroupM tile rows
+  // across a few tile columns, so the A and B panels they stream stay in L2.
+  const int ntn = gridDim.x, ntm = gridDim.y;
+  const int lin = blockIdx.y * ntn + blockIdx.x;
+  const int gsz = kGroupM * ntn;
+  const int first_m = (lin / gsz) * kGroupM;
+  const int gm = min(ntm - first_m, kGroupM);
+  const int tile_m = first_m + (lin % gsz) % gm;
+  const int tile_n = (lin % gsz) / gm;
+  const int split = blockIdx.z;
   const int kb0 = split * p.nkb;
   int nk = p.nkb_total - kb0;
   if (nk > p.nkb) nk = p.nkb;
@@ -205,8 +216,8 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
         mbar_expect_tx(&full_bar[s], STAGE_BYTES);
         int kx = (kb0 + kb) * BK;
         for (int pl = 0; pl < 4; ++pl) {
-          tma_load_2d(st + pl * PLANE_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
-          tma_load_2d(st + (4 + pl) * PLANE_TILE_BYTES, &mapB, &full_bar[s], kx,
+          tma_load_2d(st + pl * A_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
+          tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kx,
                       (int)(pl * p.rowsB + tile_n * BN));
         }
         issued = kb + 1;
@@ -239,8 +250,8 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
           uint64_t a[4], b[4];
 #pragma unroll
           for (int pl = 0; pl < 4; ++pl) {
-            a[pl] = make_desc(st + pl * PLANE_TILE_BYTES + ks * 32);
-            b[pl] = make_desc(st + (4 + pl) * PLANE_TILE_BYTES + ks * 32);
+            a[pl] = make_desc(st + pl * A_TILE_BYTES + ks * 32);
+            b[pl] = make_desc(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
           }
           uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
           // Re: Ar Br - Ai Bi
@@ -317,32 +328,36 @@ __device__ __forceinline__ float tf32_rna(float x) {
 __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t K, int64_t s_row, int64_t s_k,
                             int conj, int64_t rows_pad, int64_t Kp, float* __restrict__ planes) {
   __shared__ z64 tile[32][33];
-  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
-  for (int i = ty; i < 32; i += 8) {
-    int64_t r, k;
-    if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
-    z64 v = zmk(0, 0);
-    if (r < nrows && k < K) v = src[r * s_row + k * s_k];
-    if (conj) v.y = -v.y;
-    if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
-  }
-  __syncthreads();
+  const int64_t tiles_k = (Kp + 31) / 32, tiles = (rows_pad / 32) * tiles_k;
   const int64_t plane = rows_pad * Kp;
-  for (int i = ty; i < 32; i += 8) {
-    int64_t r = r0 + i, k = k0 + tx;
-    if (r >= rows_pad || k >= Kp) continue;
-    z64 v = tile[i][tx];
-    float rh = tf32_rna(__double2float_rn(v.x));
-    float rl = tf32_rna(__double2float_rn(v.x - (double)rh));
-    float ih = tf32_rna(__double2float_rn(v.y));
-    float il = tf32_rna(__double2float_rn(v.y - (double)ih));
-    int64_t off = r * Kp + k;
-    planes[off] = rh;
-    planes[plane + off] = rl;
-    planes[2 * plane + off] = ih;
-    planes[3 * plane + off] = il;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_k) * 32, k0 = (t % tiles_k) * 32;
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r, k;
+      if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
+      z64 v = zmk(0, 0);
+      if (r < nrows && k < K) v = src[r * s_row + k * s_k];
+      if (conj) v.y = -v.y;
+      if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r = r0 + i, k = k0 + tx;
+      if (r >= rows_pad || k >= Kp) continue;
+      z64 v = tile[i][tx];
+      float rh = tf32_rna(__double2float_rn(v.x));
+      float rl = tf32_rna(__double2float_rn(v.x - (double)rh));
+      float ih = tf32_rna(__double2float_rn(v.y));
+      float il = tf32_rna(__double2float_rn(v.y - (double)ih));
+      int64_t off = r * Kp + k;
+      planes[off] = rh;
+      planes[plane + off] = rl;
+      planes[2 * plane + off] = ih;
+      planes[3 * plane + off] = il;
+    }
+    __syncthreads();
   }
 }
 
@@ -375,12 +390,12 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp) {
+bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp, int box_rows) {
   auto enc = get_encode();
   if (!enc) return false;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
   cuuint64_t strides[1] = {(cuuint64_t)(Kp * sizeof(float))};
-  cuuint32_t box[2] = {(cuuint32_t)BK, 128u};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1u, 1u};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -390,7 +405,8 @@ bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp
 
 }  // namespace
 
-int64_t tf32_rows_pad(int64_t rows) { return round_up(rows, BM); }
+// Plane rows are padded to the larger tile edge so one layout serves as A or B.
+int64_t tf32_rows_pad(int64_t rows) { return round_up(rows, BN > BM ? BN : BM); }
 int64_t tf32_k_pad(int64_t K) { return round_up(K, BK); }
 size_t tf32_planes_bytes(int64_t rows, int64_t K) {
   return (size_t)4 * (size_t)tf32_rows_pad(rows) * (size_t)tf32_k_pad(K) * sizeof(float);
@@ -401,9 +417,9 @@ size_t tf32_planes_bytes(int64_t rows, int64_t K) {
 agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
                             float* dst, cudaStream_t stream) {
   int64_t rp = tf32_rows_pad(rows), kp = tf32_k_pad(K);
-  dim3 g((unsigned)((kp + 31) / 32), (unsigned)(rp / 32));
-  AGB_ARG_CHECK(rp / 32 <= 65535, "tf32_prep_planes: too many rows for the grid");
-  prep_kernel<<<g, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, rp, kp, dst);
+  int64_t tiles = (rp / 32) * ((kp + 31) / 32);
+  int grid = (int)(tiles < 152 * 32 ? tiles : 152 * 32);
+  prep_kernel<<<grid, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, rp, kp, dst);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -441,7 +457,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
   CUtensorMap mA, mB;
-  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp) || !encode_planes(&mB, (float*)PB, 4 * Np, Kp)) {
+  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM) || !encode_planes(&mB, (float*)PB, 4 * Np, Kp, BN)) {
     agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
@@ -454,7 +470,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   p.M = M; p.N = N; p.nkb = nkb_split; p.nkb_total = (int)nkb;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = splits > 1 ? partials : nullptr; p.err = err;
   p.rowsA = Mp; p.rowsB = Np;
-  dim3 grid((unsigned)(Np / BN), (unsigned)(Mp / BM), (unsigned)splits);
+  dim3 grid((unsigned)(round_up(N, BN) / BN), (unsigned)(round_up(M, BM) / BM), (unsigned)splits);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (g_timing.load(std::memory_order_relaxed)) {
     AGB_CUDA_TRY(cudaEventCreate(&ev0));

@@ -28,16 +28,25 @@ def stream_ptr():
 
 
 def ptr(t):
+    """Raw device pointer of a tensor whose storage holds exactly its values
+    (torch's lazy conjugate / negative views do not, and are refused)."""
     if t is None:
         return ctypes.c_void_p(0)
+    if t.is_conj() or t.is_neg():
+        raise ValueError("lazy conj/neg view passed to the C ABI; call resolve_conj()/resolve_neg() first")
     return ctypes.c_void_p(t.data_ptr())
+
+
+def materialize(t):
+    """Contiguous tensor with any lazy conjugation or negation applied."""
+    return t.resolve_conj().resolve_neg().contiguous()
 
 
 def to_dev(x, dtype=torch.complex128):
     """NumPy array or tensor -> contiguous CUDA tensor of ``dtype``."""
     dev = device()
     if isinstance(x, torch.Tensor):
-        return x.to(device=dev, dtype=dtype).contiguous()
+        return materialize(x.to(device=dev, dtype=dtype))
     return torch.as_tensor(np.ascontiguousarray(x)).to(device=dev, dtype=dtype).contiguous()
 
 

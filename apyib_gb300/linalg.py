@@ -1,16 +1,20 @@
 """Small dense complex helpers routed through the library's FP64 GEMM."""
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from . import _lib
-from .device import device, ptr, stream_ptr
+from .device import device, ptr, stream_ptr, workspace
 
 
-def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, out=None, beta=0.0):
-    """C = alpha * op(A) @ op(B) (+ beta*C) for 2-D complex128 CUDA tensors via agb_zgemm."""
-    A = A.to(device=device(), dtype=torch.complex128)
-    B = B.to(device=device(), dtype=torch.complex128)
+def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, out=None, beta=0.0,
+        precision=_lib.PREC_FP64):
+    """C = alpha * op(A) @ op(B) (+ beta*C) for 2-D complex128 CUDA tensors via agb_zgemm
+    (FP64) or agb_cgemm_tf32x3 (complex FP32 as 3xTF32 on the tensor cores)."""
+    A = A.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg()
+    B = B.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg()
     M, K = (A.shape[1], A.shape[0]) if transA else (A.shape[0], A.shape[1])
     K2, N = (B.shape[1], B.shape[0]) if transB else (B.shape[0], B.shape[1])
     assert K == K2, (A.shape, B.shape, transA, transB)
@@ -20,6 +24,16 @@ def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, o
         out = torch.empty((M, N), dtype=torch.complex128, device=device())
         beta = 0.0
     alpha, beta = complex(alpha), complex(beta)
+    if precision == _lib.PREC_TF32X3 and M > 0 and N > 0 and K > 0:
+        nb = _lib.load().agb_cgemm_tf32x3_scratch_bytes(M, N, K)
+        buf, sp, _ = workspace(nb)
+        buf[:256].zero_()
+        _lib.call("agb_cgemm_tf32x3", M, N, K, alpha.real, alpha.imag, ptr(A), sAm, sAk, int(conjA), ptr(B), sBk,
+                  sBn, int(conjB), beta.real, beta.imag, ptr(out), out.stride(0), ctypes.c_void_p(sp),
+                  ctypes.c_size_t(nb), stream_ptr())
+        _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
+        del buf
+        return out
     _lib.call("agb_zgemm", M, N, K, alpha.real, alpha.imag, ptr(A), sAm, sAk, int(conjA), ptr(B), sBk, sBn,
               int(conjB), beta.real, beta.imag, ptr(out), out.stride(0), stream_ptr())
     return out
@@ -29,8 +43,8 @@ def jk_fock(ERI_AO, D, h, scale):
     """F = h + scale * sum_ls D_ls (2 (mn|ls) - (ml|ns)) (apyib/hf_wfn.py:81, apyib/utils.py:249)."""
     n = D.shape[0]
     eri = ERI_AO.to(device=device(), dtype=torch.float64).contiguous()
-    D = D.to(device=device(), dtype=torch.complex128).contiguous()
-    h = h.to(device=device(), dtype=torch.complex128).contiguous()
+    D = D.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
+    h = h.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
     F = torch.empty((n, n), dtype=torch.complex128, device=device())
     _lib.call("agb_jk_fock", ptr(eri), n, ptr(D), ptr(h), float(scale), ptr(F), stream_ptr())
     return F

@@ -23,6 +23,25 @@ class mp2_wfn(object):
         self.D_ijab = (self.eps_o.reshape(-1, 1, 1, 1) + self.eps_o.reshape(-1, 1, 1) - self.eps_v.reshape(-1, 1)
                        - self.eps_v)
 
+    def solve_MP2(self, return_torch=False):
+        """apyib/mp2_wfn.py:42-59: closed-shell MP2 over complex spatial orbitals on the GPU."""
+        import ctypes
+
+        import torch
+
+        from .device import ptr, stream_ptr
+        ERI_MO = compute_ERI_MO(self.parameters, self.wfn, self.C_list, return_torch=True)
+        no, nv = len(self.eps_o), len(self.eps_v)
+        nmo = no + nv
+        eps = to_dev(np.concatenate([self.eps_o, self.eps_v]), torch.float64)
+        t2 = torch.empty((no, no, nv, nv), dtype=torch.complex128, device=ERI_MO.device)
+        E = torch.empty(1, dtype=torch.complex128, device=ERI_MO.device)
+        part = torch.empty(1024, dtype=torch.complex128, device=ERI_MO.device)
+        _lib.call("agb_mp2_spatial", ptr(ERI_MO), nmo, no, ptr(eps), ptr(t2), ptr(E), ptr(part),
+                  ctypes.c_size_t(part.numel() * 16), stream_ptr())
+        Ev = np.complex128(E.cpu().numpy()[0])
+        return (Ev, t2) if return_torch else (Ev, t2.cpu().numpy())
+
     def solve_MP2_SO(self, return_torch=False):
         """apyib/mp2_wfn.py:64-87: t2 = <ij||ab>/D, E = 1/4 sum <ij||ab> t2, on the GPU."""
         ERI_MO = compute_ERI_MO(self.parameters, self.wfn, self.C_list, return_torch=True)

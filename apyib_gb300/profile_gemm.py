@@ -1,0 +1,34 @@
+"""Run one 3xTF32 tensor-core complex GEMM of a given shape twice (for ncu).
+
+    python -m apyib_gb300.profile_gemm M N K
+
+A: [M,K] complex128 row-major, B: [N,K] (used transposed), random normal.
+"""
+import ctypes
+import sys
+
+import torch
+
+from . import _lib
+from .device import ptr, stream_ptr, workspace
+
+
+def main(argv):
+    M, N, K = (int(a) for a in argv[:3])
+    torch.cuda.set_device(0)
+    A = torch.randn(M, K, dtype=torch.complex128, device="cuda")
+    B = torch.randn(N, K, dtype=torch.complex128, device="cuda")
+    C = torch.zeros(M, N, dtype=torch.complex128, device="cuda")
+    nb = _lib.load().agb_cgemm_tf32x3_scratch_bytes(M, N, K)
+    buf, sp, _ = workspace(nb)
+    buf.zero_()
+    for _ in range(2):
+        _lib.call("agb_cgemm_tf32x3", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
+                  ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
+    _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
+    torch.cuda.synchronize()
+    print("ok", M, N, K)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -144,6 +144,22 @@ def run_reference(args, rank, world):
     return 0
 
 
+def max_over_ranks(x, dist=None):
+    """Max of a per-rank scalar over all ranks (identity without a process group)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(x)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_throughput(world, work_per_rank, max_seconds):
+    """Whole-job throughput of independent replicas: total work / slowest rank."""
+    return world * work_per_rank / max_seconds
+
+
 METRIC = "CISD_SO iteration TFLOP/s (algorithmic), mixed 3xTF32 + FP64 refinement, synthetic o/v=60/240"
 
 
@@ -186,7 +202,9 @@ def main():
     t_setup = time.perf_counter()
     plan = CISDPlan(o, v, mixed=True)
     plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
-    plan.blocks_from_factors(torch.as_tensor(prob.B))
+    # integral blocks from the factors with double-float GEMMs (~1e-13 relative; the FP64
+    # pipe would take ~5x longer); every solve below uses these same blocks
+    plan.blocks_from_factors(torch.as_tensor(prob.B), precision=_lib.PREC_DF64)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
     del prob
@@ -233,11 +251,7 @@ def main():
     ring = float(o * v) ** 3
     _lib.call("agb_gemm_timing_collect", min(pq, ring) * 0.99, ctypes.byref(nl), ctypes.byref(kms), ctypes.byref(kfl))
     plan.check_status()
-    dev_ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        tt = torch.tensor([dev_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms = tt.item()
+    dev_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist)
     clocks = sampler.stop()
 
     # ---- e2e: the same iteration with amplitudes resident on the host (pinned)
@@ -256,11 +270,7 @@ def main():
         host_t, host_out = host_out, host_t
     e1.record()
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        tt = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = tt.item()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist)
     nbytes = plan.n * 16
 
     peaks, peak_kind = measured_peaks()
@@ -269,14 +279,14 @@ def main():
     kern_ach = (kfl.value / (kms.value / 1e3) / 1e12) if kms.value > 0 else None
 
     out = {
-        "metric": METRIC, "value": world * W / (dev_ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": world,
+        "metric": METRIC, "value": aggregate_throughput(world, W, dev_ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (3xTF32 tensor core) + c128 (update/DIIS/sums)",
         "data": "synthetic (seeded Hermitian factors, BASELINE config shape o/v=60/240)",
         "config": {"workload": "CISD_SO mixed-precision iteration, synthetic o/v=60/240 spin orbitals",
                    "o": o, "v": v, "naux": 4 * (o + v), "l2": "inputs > L2 (ERI blocks ~45 GB in HBM)",
                    "parallelism": f"replicas x{world}", "alg_flops_per_step": W},
-        "e2e": {"value": world * W / (e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
+        "e2e": {"value": aggregate_throughput(world, W, e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
@@ -288,6 +298,8 @@ def main():
         "setup_s": setup_s,
     }
 
+    del diis, state, host_t, host_out
+    torch.cuda.empty_cache()
     if not args.no_solve and rank == 0:
         # Full mixed solve (fresh amplitudes) + FP64 residual timing + a-posteriori FP64 check.
         params = dict(max_iterations=60, DIIS=True, e_convergence=1e-10, d_convergence=1e-8)
@@ -313,10 +325,47 @@ def main():
             "mixed_solve_s": solve_s, "E_mixed": [Em.real, Em.imag], "iterations": iters,
             "tf32_residuals": stats["tf32_residuals"], "fp64_residuals": stats["fp64_residuals"],
             "fp64_residual_s": fp64_res_s,
-            "fp64_solve_estimate_s": iters * (fp64_res_s + tf32_res_s * 0.0) + iters * 0.05,
+            "fp64_solve_estimate_s": iters * fp64_res_s,
             "fp64_solve_estimate_note": "iterations of the mixed solve x measured FP64 residual time",
             "posterior_max_amplitude_correction": max_corr,
         }
+        del r64, corr
+        # Adjoint: one backward (CISD densities, vvvv block recomputed, 3xTF32 GEMMs) at the solution,
+        # against the 2*(3N+3) = 24 full solves a finite-difference AAT/APT set needs for H2O (N = 3).
+        from apyib_gb300.adjoint import densities
+        torch.cuda.empty_cache()
+        torch.cuda.synchronize()
+        a0 = time.perf_counter()
+        Dm, Gm = densities(plan, tm, precision=_lib.PREC_TF32X3)
+        torch.cuda.synchronize()
+        bwd_s = time.perf_counter() - a0
+        out["adjoint"] = {"backward_s": bwd_s, "fd_solves": 24, "fd_estimate_s": 24 * solve_s,
+                          "note": "one density backward vs 24 mixed solves (central differences, 3N+3 = 12 "
+                                  "parameters for H2O), both at o/v=60/240"}
+        del Dm, Gm, tm, plan
+        torch.cuda.empty_cache()
+        # Measured FP64-vs-mixed solve comparison where the FP64 solve fits the run: o/v = 40/160.
+        o3, v3 = 40, 160
+        prob3 = synthetic.so_factors(o3, v3, seed=0)
+        eps3 = np.concatenate([np.repeat(prob3.eps_o, 2), np.repeat(prob3.eps_v, 2)])
+        plan3 = CISDPlan(o3, v3, mixed=True)
+        plan3.set_fock(torch.as_tensor(prob3.fock_so()), eps3)
+        plan3.blocks_from_factors(torch.as_tensor(prob3.B), precision=_lib.PREC_DF64)
+        res3 = {}
+        for prec in ("fp64", "mixed"):
+            h3 = []
+            torch.cuda.synchronize()
+            s0 = time.perf_counter()
+            E3, _ = solve(plan3, params, precision=prec, history=h3)
+            torch.cuda.synchronize()
+            res3[prec] = (time.perf_counter() - s0, E3, len(h3) - 1)
+        out["solve_40_160"] = {
+            "fp64_solve_s": res3["fp64"][0], "mixed_solve_s": res3["mixed"][0],
+            "speedup": res3["fp64"][0] / res3["mixed"][0],
+            "abs_dE_mixed_vs_fp64": abs(res3["mixed"][1] - res3["fp64"][1]),
+            "E_fp64": [res3["fp64"][1].real, res3["fp64"][1].imag],
+            "iterations": {"fp64": res3["fp64"][2], "mixed": res3["mixed"][2]}}
+        del plan3
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline_oracle()
     if rank == 0:

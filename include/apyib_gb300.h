@@ -44,6 +44,7 @@ typedef int agb_status;
 
 #define AGB_PREC_FP64 0        /* FP64 CUDA-core arithmetic */
 #define AGB_PREC_TF32X3 1      /* complex FP32 via 3xTF32 tcgen05 MMAs, FP32 accumulate */
+#define AGB_PREC_DF64 2        /* double-float (2 x FP32, ~48-bit) GEMMs on the FP32 pipe, FP64 elsewhere */
 
 /* Library version (major*10000 + minor*100 + patch). */
 int agb_version(void);
@@ -63,6 +64,14 @@ agb_status agb_zgemm(int64_t M, int64_t N, int64_t K, double alpha_re, double al
                      const void* A, int64_t sAm, int64_t sAk, int conjA,
                      const void* B, int64_t sBk, int64_t sBn, int conjB,
                      double beta_re, double beta_im, void* C, int64_t ldc, void* stream);
+
+/* Same contraction in double-float arithmetic (each FP64 value split into two
+ * floats, exact FMA product splitting, two-sum accumulation; ~2^-44 relative)
+ * on the FP32 CUDA cores, which GB300 issues far faster than FP64. */
+agb_status agb_zgemm_df64(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                          const void* A, int64_t sAm, int64_t sAk, int conjA,
+                          const void* B, int64_t sBk, int64_t sBn, int conjB,
+                          double beta_re, double beta_im, void* C, int64_t ldc, void* stream);
 
 /* Same contraction computed as complex FP32 with 3xTF32 split products on the
  * tcgen05 tensor cores (FP32 accumulation in TMEM), FP64 in and out.
@@ -128,8 +137,9 @@ agb_status agb_cisd_set_fock(agb_cisd_plan* plan, const void* F_SO, const double
 agb_status agb_cisd_blocks_from_mo(agb_cisd_plan* plan, const void* ERI_MO, void* stream);
 agb_status agb_cisd_blocks_from_so(agb_cisd_plan* plan, const void* ERI_SO, void* stream);
 size_t agb_cisd_factor_scratch_bytes(const agb_cisd_plan* plan, int64_t naux);
+/* precision: AGB_PREC_FP64, or AGB_PREC_DF64 for the factor products in double-float. */
 agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* plan, const void* Bf, int64_t naux,
-                                        void* scratch, size_t scratch_bytes, void* stream);
+                                        void* scratch, size_t scratch_bytes, int precision, void* stream);
 
 #define AGB_RES_CONST 1        /* include the constant terms <ab||ij> and F_ai */
 #define AGB_RES_ETERM 2        /* include -E * t */
@@ -155,6 +165,7 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
                         void* stream);
 size_t agb_vec_partials_bytes(int ny);
 
+
 /* t_new = sum_j c_j y_j (apyib/utils.py:138; ny <= 16; ny = 1, c = 1 copies),
  * fused with the energy E = sum_ia t1*F_ov + sum_p t2p*<ij||ab>_p (ci_wfn.py:355) and the
  * unconjugated squared norms s1 = sum (t1_old - t1_new)^2, s2 = 4 sum (t2p_old - t2p_new)^2
@@ -177,6 +188,13 @@ agb_status agb_cisd_guess(agb_cisd_plan* plan, void* t, void* stream);
  * (apyib/mp2_wfn.py:82-85); t receives the packed vector (t1 part zero). */
 agb_status agb_mp2_so(agb_cisd_plan* plan, void* t, void* E_out, void* partials, size_t partials_bytes,
                       void* stream);
+
+/* Closed-shell MP2 over complex spatial orbitals (apyib/mp2_wfn.py:42-59):
+ * t2[i,j,a,b] = <ab|ij>/D_ijab, E = sum (2<ij|ab> - <ij|ba>) t2, from the active
+ * chemist ERI_MO (nmo^4, first no orbitals occupied) and eps (nmo doubles, device).
+ * t2 receives no*no*nv*nv complex values; E_out one complex (device). */
+agb_status agb_mp2_spatial(const void* ERI_MO, int64_t nmo, int64_t no, const double* eps, void* t2,
+                           void* E_out, void* partials, size_t partials_bytes, void* stream);
 
 /* ------------------------------------------------------ AO -> MO, J/K -- */
 

@@ -270,6 +270,19 @@ def solve_mp2_so(blk, eps_o, eps_v):
     return E, t2
 
 
+def solve_mp2_spatial(ERI_MO, eps_o, eps_v):
+    """apyib/mp2_wfn.py:42-59: t2 = <ab|ij>/D, E = sum (2<ij|ab> - <ij|ba>) t2 over
+    spatial orbitals; ERI_MO is the active chemist tensor, occupied orbitals first."""
+    no = len(eps_o)
+    O = slice(0, no)
+    V = slice(no, ERI_MO.shape[0])
+    dirac = ERI_MO.transpose(0, 2, 1, 3)
+    D = eps_o.reshape(-1, 1, 1, 1) + eps_o.reshape(-1, 1, 1) - eps_v.reshape(-1, 1) - eps_v
+    t2 = dirac[V, V, O, O].transpose(2, 3, 0, 1) / D
+    E = np.einsum("ijab,ijab->", 2 * dirac[O, O, V, V] - dirac[O, O, V, V].transpose(0, 1, 3, 2), t2)
+    return E, t2
+
+
 # ----------------------------------------------------------------------------
 # AO -> MO, Fock and SCF
 # ----------------------------------------------------------------------------

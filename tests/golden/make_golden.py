@@ -125,6 +125,8 @@ def ao_case(nbf, ndocc, seed, field, nfzc=0):
         else:
             E, t2 = ref.mp2_wfn.mp2_wfn(p, wfn).solve_MP2_SO()
             out.update(E_mp2=E, t2_mp2=t2)
+            E, t2 = ref.mp2_wfn.mp2_wfn(params("MP2", fc=nfzc > 0), wfn).solve_MP2()
+            out.update(E_mp2_spatial=E, t2_mp2_spatial=t2)
     return out
 
 

@@ -66,3 +66,6 @@ def test_transforms_and_correlated_energies(path):
     E, t2 = mp2_wfn(params("MP2_SO", fc), wfn).solve_MP2_SO()
     assert abs(E - g["E_mp2"]) < 1e-10
     np.testing.assert_allclose(t2, g["t2_mp2"], atol=1e-9)
+    E, t2 = mp2_wfn(params("MP2", fc), wfn).solve_MP2()
+    assert abs(E - g["E_mp2_spatial"]) < 1e-10
+    np.testing.assert_allclose(t2, g["t2_mp2_spatial"], atol=1e-9)

@@ -97,12 +97,32 @@ def test_nondiagonal_fock_solve_matches_oracle():
     assert np.abs(t2.cpu().numpy() - t2r).max() < 1e-9
 
 
-def test_mixed_precision_reaches_fp64_energy():
+@pytest.mark.parametrize("base", ["df64", "fp64"])
+def test_mixed_precision_reaches_fp64_energy(base):
+    from apyib_gb300.cisd import solve
     prob = synthetic.so_factors(20, 80, seed=7)
     F = prob.fock_so()
     p = dict(P, e_convergence=1e-12, d_convergence=1e-10)
     E64, _, t2_64 = solve_so_system(F, prob.eps_o, prob.eps_v, p, B=prob.B)
+    plan = CISDPlan(prob.o, prob.v, mixed=True)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    plan.set_fock(torch.as_tensor(F), eps_so)
+    plan.blocks_from_factors(torch.as_tensor(prob.B))
     hist = []
-    Em, _, t2_m = solve_so_system(F, prob.eps_o, prob.eps_v, p, B=prob.B, precision="mixed", history=hist)
+    Em, t = solve(plan, p, precision="mixed", history=hist, base_precision=base)
+    _, t2_m = plan.unpack(t)
     assert abs(Em - E64) < 1e-9, (Em, E64, hist)
     assert np.abs(t2_m.cpu().numpy() - t2_64.cpu().numpy()).max() < 1e-8
+
+
+def test_df64_residual_matches_fp64_residual():
+    prob = synthetic.so_factors(12, 44, seed=9)
+    plan = CISDPlan(prob.o, prob.v)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
+    plan.blocks_from_factors(torch.as_tensor(prob.B))
+    t = plan.guess()
+    r64 = plan.residual(t, 0.1 - 0.01j, _lib.PREC_FP64)
+    rdf = plan.residual(t, 0.1 - 0.01j, _lib.PREC_DF64)
+    err = (rdf - r64).abs().max().item() / r64.abs().max().item()
+    assert err < 1e-11, err

@@ -95,3 +95,19 @@ def test_so_expansion_matches_oracle():
     g = crandn(rng, 3, 4, 5, 2)
     np.testing.assert_array_equal(utils.compute_F_SO(None, F), port.compute_F_SO(F))
     np.testing.assert_array_equal(utils.compute_ERI_SO(None, g), port.compute_ERI_SO(g))
+
+
+@pytest.mark.parametrize("M,N,K", [(37, 53, 29), (130, 70, 3000), (5, 7, 20000)])
+def test_df64_gemm_accuracy(M, N, K):
+    """Double-float GEMM: error ~1e-13 relative to sum|a||b| (vs ~1e-16 FP64, ~1e-6 3xTF32)."""
+    rng = np.random.default_rng(M * 3 + K)
+    A = crandn(rng, M, K)
+    B = crandn(rng, K, N)
+    Ad, Bd = to_dev(A), to_dev(B)
+    C = torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    _lib.call("agb_zgemm_df64", M, N, K, 1.0, 0.0, ptr(Ad), K, 1, 0, ptr(Bd), N, 1, 0, 0.0, 0.0, ptr(C), N,
+              stream_ptr())
+    got = C.cpu().numpy()
+    ref = A @ B
+    err = np.abs(got - ref) / (np.abs(A) @ np.abs(B))
+    assert err.max() < 1e-12, err.max()

@@ -122,3 +122,12 @@ def test_adjoint_densities_reproduce_energy():
     # Normal-ordered: subtract the occupied reference part of F.
     E_adj = np.einsum("pq,pq->", F, D) + np.einsum("pqrs,pqrs->", dirac, G)
     assert abs(E_adj - E) < 1e-10
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "ao_*.npz"))), ids=os.path.basename)
+def test_spatial_mp2_matches_reference(path):
+    g = dict(np.load(path))
+    nfzc, ndocc = int(g["nfzc"]), int(g["ndocc"])
+    E, t2 = port.solve_mp2_spatial(g["ERI_MO"], g["eps"][nfzc:ndocc], g["eps"][ndocc:])
+    assert abs(E - g["E_mp2_spatial"]) < 1e-12
+    np.testing.assert_allclose(t2, g["t2_mp2_spatial"], atol=1e-13)
