@@ -70,6 +70,7 @@ SIGNATURES = {
     "agb_cisd_update": (_int, [_vp, _vp, _vp, _vp, _vp]),
     "agb_vec_dots": (_int, [_i64, _i64, _d, _d, _vp, _c.POINTER(_vp), _int, _vp, _vp, _sz, _vp]),
     "agb_vec_partials_bytes": (_sz, [_int]),
+    "agb_vec_dots_noalloc": (_int, [_i64, _i64, _d, _d, _vp, _c.POINTER(_vp), _int, _vp, _vp]),
     "agb_cisd_combine": (_int, [_vp, _c.POINTER(_vp), _c.POINTER(_d), _int, _vp, _vp, _vp, _vp, _sz, _vp]),
     "agb_cisd_unpack": (_int, [_vp, _vp, _vp, _vp, _vp]),
     "agb_cisd_pack": (_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -958,6 +958,67 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
   return AGB_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// agb_vec_dots_noalloc: the DIIS Gram-row reduction for callers that cannot
+// allocate device memory.  Its block partial sums live in the file-scope array
+// below (kRedBlocks x 16 complex doubles = 155,648 bytes), which every device
+// that loads this library keeps until the process exits.
+namespace {
+constexpr int kNoAllocMaxVec = 16;
+__device__ __align__(256) z64 g_dots_noalloc_scratch[kRedBlocks * kNoAllocMaxVec];
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 256;
+void* g_noalloc_scratch_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+extern "C" {
+
+agb_status agb_vec_dots_noalloc(int64_t n1, int64_t n2, double w1, double w2, const void* x, const void* const* ys,
+                                int ny, void* out, void* stream) {
+  AGB_ARG_CHECK(x && ys && out && n1 >= 0 && n2 >= 0, "vec_dots_noalloc: bad argument");
+  if (ny < 1 || ny > kNoAllocMaxVec) {
+    agb_set_error_message("vec_dots_noalloc: ny must be between 1 and 16 (the fixed scratch holds 16 partial sums "
+                          "per block)", __FILE__, __LINE__);
+    return AGB_ERR_ARG;
+  }
+  int dev = 0;
+  AGB_CUDA_TRY(cudaGetDevice(&dev));
+  AGB_ARG_CHECK(dev >= 0 && dev < kNoAllocMaxDevices, "vec_dots_noalloc: device ordinal out of range");
+  void* scratch = nullptr;
+  {
+    // One-time set-up per device (with that device current): the host-side name of
+    // the array is not a device address, so look the address up and keep it.
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_scratch_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_dots_noalloc_scratch);
+      if (e != cudaSuccess || p == nullptr) {
+        agb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+        return AGB_ERR_CUDA;
+      }
+      g_noalloc_scratch_ptr[dev] = p;
+    }
+    scratch = g_noalloc_scratch_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  DotArgs A;
+  A.n1 = n1; A.n2 = n2; A.w1 = w1; A.w2 = w2; A.x = (const z64*)x; A.ny = ny;
+  for (int j = 0; j < kMaxVec; ++j) A.ys[j] = j < ny ? (const z64*)ys[j] : nullptr;
+  // Every partial slot read below is written earlier in this same call, so the
+  // array's previous contents never leak into the result.
+  z64* part = (z64*)scratch;
+  if (ny <= 4) dots_kernel<4><<<kRedBlocks, 256, 0, st>>>(A, part);
+  else if (ny <= 8) dots_kernel<8><<<kRedBlocks, 256, 0, st>>>(A, part);
+  else dots_kernel<16><<<kRedBlocks, 256, 0, st>>>(A, part);
+  AGB_LAUNCH_CHECK();
+  int nv = ny <= 4 ? 4 : (ny <= 8 ? 8 : 16);
+  finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, ny, (z64*)out);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
 agb_status agb_cisd_combine(agb_cisd_plan* P, const void* const* ys, const double* coefs, int ny, const void* t_old,
                             void* t_new, void* out3, void* partials, size_t partials_bytes, void* stream) {
   AGB_ARG_CHECK(P && P->ws && ys && coefs && t_old && t_new && out3, "combine: bad argument");

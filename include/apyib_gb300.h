@@ -165,6 +165,23 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
                         void* stream);
 size_t agb_vec_partials_bytes(int ny);
 
+/* agb_vec_dots without the caller-provided partials buffer.  No counterpart in
+ * the reference (which has no device code at all); it exists for callers that
+ * cannot allocate device memory themselves, e.g. a plugin whose host
+ * application owns every device allocation through its own pool and hands out
+ * only the vectors, or a latency-bound loop in which an allocation call (and
+ * the synchronisation it may imply) is not allowed.
+ * The block partial sums live in a fixed array inside the library (155,648
+ * bytes on every device that loads it, kept until the process exits), so this
+ * entry point allocates nothing and accepts at most ny = 16 vectors; larger ny
+ * is rejected with AGB_ERR_ARG.  The first call on a device looks up the
+ * array's device address (with that device current), so make that first call
+ * before any stream capture.  All calls on a device share the one array and
+ * each call leaves its partial sums there; calls that overlap on the GPU (for
+ * example on two streams at once) race on it, so the caller must keep them
+ * from overlapping. */
+agb_status agb_vec_dots_noalloc(int64_t n1, int64_t n2, double w1, double w2, const void* x,
+                                const void* const* ys, int ny, void* out, void* stream);
 
 /* t_new = sum_j c_j y_j (apyib/utils.py:138; ny <= 16; ny = 1, c = 1 copies),
  * fused with the energy E = sum_ia t1*F_ov + sum_p t2p*<ij||ab>_p (ci_wfn.py:355) and the
