@@ -9,22 +9,25 @@ expectation value of the corresponding operator in the normalised CI state
     dE = sum_pq D_pq dF_pq + sum_pqrs Gamma_pqrs d<pq|rs>
 
 with the one- and two-particle densities of the reference's own adjoint
-check (apyib/ci_wfn.py:382-411, restated in oracle/port.py).  This holds
-for integral changes that keep F_ov = F_vo = 0 (canonical orbitals): the
-reference's doubles equations omit the F_ov t1 coupling, so with a non-zero
-occupied-virtual Fock block its projective energy is not stationary and the
-density gradient of that block is not the derivative of the solver's energy.
-Two-electron perturbations are unrestricted.  The densities
+check (apyib/ci_wfn.py:382-411, restated in oracle/port.py), with one
+change: the reference's doubles equations (ci_wfn.py:319-334) have no F_vo t1
+coupling, so the eigenproblem the solver converges is not Hermitian once F_vo
+is non-zero; its left eigenvector at a point with F_vo = 0 is still the
+conjugate of the right one, and the derivative with respect to F_vo then
+lacks the sum_jb t2*_ijab t1_jb term of the exact CISD density.  ``densities``
+drops it by default (``vo_coupling=False``), which makes dE/dF exact for every
+Fock block; the two agree whenever F_vo = 0.  The densities
 are built on the GPU from the converged amplitudes with the library's
 complex GEMMs; the vvvv block Gamma_abcd = 1/4 sum_ij t2*_ijab t2_ijcd is
 recomputed in the backward as a packed (a<b, c<d) GEMM over i<j rather than
 kept from the forward pass.
 
 ``CISDEnergy`` wraps the solve in a torch.autograd.Function with inputs
-(F_SO, ERI_SO) (chemist, <pq|rs> = (pr|qs)); ``CISDEnergyFactors`` takes
-Hermitian factors B[L,p,q] with (pq|rs) = sum_L B[L,p,q] B[L,r,s] instead
-of the nso^4 tensor.  Gradients follow PyTorch's convention for a
-holomorphic map: grad_input = grad_output * conj(dE/dinput).
+(F_SO, ERI_SO) (chemist, <pq|rs> = (pr|qs)); ``CISDEnergyCore`` takes the AO
+core Hamiltonian h = T + V at fixed orbitals and returns dE/dh = C* D C^T,
+the route to magnetic-field derivatives (dh/dB = -mu_mag) without orbital
+relaxation.  Gradients follow PyTorch's convention for a holomorphic map:
+grad_input = grad_output * conj(dE/dinput).
 """
 from __future__ import annotations
 
@@ -49,11 +52,17 @@ def _zgemm_conjA(A_ptr_tensor, M, N, K, sAm, sAk, B, sBk, sBn, out, alpha=1.0, p
                   ptr(out), N, stream_ptr())
 
 
-def densities(plan, t, precision=_lib.PREC_FP64):
+def densities(plan, t, precision=_lib.PREC_FP64, vo_coupling=False):
     """One- and two-particle densities of the normalised CISD_SO (or CID_SO)
     state from the packed amplitudes t.  Returns (D [nso,nso], G) with G a
     dict of Dirac-ordered blocks keyed by orbital-range letters; G['vvvv_p']
-    is the packed block Gp[(a<b),(c<d)] with Gamma_abcd = sign * Gp / 2."""
+    is the packed block Gp[(a<b),(c<d)] with Gamma_abcd = sign * Gp / 2.
+
+    vo_coupling=True gives the exact CISD density of apyib/ci_wfn.py:393
+    (D_ai = t0 t1*_ia + sum_jb t2*_ijab t1_jb); the default drops the second
+    term, which couples F_vo to the doubles - a coupling the reference's
+    residual (ci_wfn.py:319-334) does not contain - so that D is the derivative
+    of the energy the solver actually converges (identical when F_vo = 0)."""
     o, v = plan.o, plan.v
     nso = o + v
     dev = device()
@@ -79,7 +88,10 @@ def densities(plan, t, precision=_lib.PREC_FP64):
     D[V, V] = mm(t1, t1, transA=True, conjA=True) + 0.5 * mm(Tv, Tv, conjA=True, transB=True)
     Tr = t2.permute(0, 2, 1, 3).reshape(o * v, o * v).contiguous()       # [(i,a),(j,b)] = t2[i,j,a,b]
     D[O, V] = t0 * t1 + mm(Tr, t1c.reshape(o * v, 1)).reshape(o, v)
-    D[V, O] = (t0 * t1c + mm(Tr, t1.reshape(o * v, 1), conjA=True).reshape(o, v)).T
+    if vo_coupling:
+        D[V, O] = (t0 * t1c + mm(Tr, t1.reshape(o * v, 1), conjA=True).reshape(o, v)).T
+    else:
+        D[V, O] = (t0 * t1c).T
     G = {}
     # oooo: 1/4 sum_ab t2*[k,l,a,b] t2[i,j,a,b] -> [i,j,k,l]
     Toov = t2.reshape(o * o, v * v)
@@ -193,3 +205,61 @@ def cisd_energy(F_SO, ERI_SO, eps_o, eps_v, params, singles=True, precision="fp6
     return CISDEnergy.apply(to_dev(F_SO) if not isinstance(F_SO, torch.Tensor) else F_SO,
                             to_dev(ERI_SO) if not isinstance(ERI_SO, torch.Tensor) else ERI_SO,
                             eps_o, eps_v, params, singles, precision)
+
+
+# ---------------------------------------------------------------------------
+# AO-level adjoint for the core Hamiltonian (field derivatives at fixed orbitals)
+
+def _fock_mo(h_AO, ERI_AO, C, C_list, freeze_core):
+    """F_MO = C_t^H (h + G[D_fc] + G[D_occ]) C_t with G[D] = 2J - K (apyib/utils.py:231-252)."""
+    from .linalg import jk_fock
+    f, o, _, t = C_list
+    h = h_AO
+    if freeze_core:
+        Cf = C[:, f].contiguous()
+        h = jk_fock(ERI_AO, zmm(Cf, Cf, transB=True, conjB=True), h, 1.0)
+    Co = C[:, o].contiguous()
+    F_AO = jk_fock(ERI_AO, zmm(Co, Co, transB=True, conjB=True), h, 1.0)
+    Ct = C[:, t].contiguous()
+    return zmm(zmm(Ct, F_AO, transA=True, conjA=True), Ct)
+
+
+class CISDEnergyCore(torch.autograd.Function):
+    """E_CISD_SO as a function of the AO core Hamiltonian h = T + V (complex),
+    at fixed orbitals C (the wavefunction object's) and fixed AO ERIs.
+    dE/dh = conj(C_t) D_sp C_t^T with D_sp the spin-summed active-space density,
+    so dE/dB = Re sum conj(grad_h) dh/dB for a field term dh/dB = -mu_mag."""
+
+    @staticmethod
+    def forward(ctx, h_AO, wfn, params, precision="fp64"):
+        from .utils import compute_ERI_MO, compute_F_SO, get_slices
+        C_list, _ = get_slices(params, wfn)
+        C = to_dev(np.asarray(wfn.C))
+        ERI = to_dev(wfn.H.ERI, torch.float64)
+        F_MO = _fock_mo(h_AO.detach(), ERI, C, C_list, params["freeze_core"])
+        ERI_MO = compute_ERI_MO(params, wfn, C_list, return_torch=True)
+        eps = np.asarray(wfn.eps)
+        eps_o, eps_v = eps[C_list[1]], eps[C_list[2]]
+        o, v = 2 * len(eps_o), 2 * len(eps_v)
+        plan = CISDPlan(o, v, mixed=(precision == "mixed"))
+        eps_so = np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)])
+        plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True), eps_so)
+        plan.blocks_from_mo(ERI_MO)
+        E, t = solve(plan, params, precision=precision)
+        ctx.plan = plan
+        ctx.Ct = C[:, C_list[3]].contiguous()
+        ctx.save_for_backward(t)
+        return torch.tensor(complex(E), dtype=torch.complex128, device=h_AO.device)
+
+    @staticmethod
+    def backward(ctx, gE):
+        (t,) = ctx.saved_tensors
+        D, _ = densities(ctx.plan, t)
+        D_sp = D[0::2, 0::2] + D[1::2, 1::2]            # F_SO[p,q] = F_MO[p/2,q/2] for equal spins
+        Ct = ctx.Ct
+        dEdh = zmm(zmm(Ct.conj().resolve_conj(), D_sp), Ct, transB=True)   # conj(C) D_sp C^T
+        return gE.to(torch.complex128) * dEdh.conj(), None, None, None
+
+
+def cisd_energy_core(h_AO, wfn, params, precision="fp64"):
+    return CISDEnergyCore.apply(h_AO, wfn, params, precision)

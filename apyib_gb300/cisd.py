@@ -21,6 +21,7 @@ Precision modes:
 from __future__ import annotations
 
 import ctypes
+import os
 import time
 
 import numpy as np
@@ -220,13 +221,24 @@ class _DIIS:
         return _bordered_diis(self.B)
 
 
+def _save_checkpoint(path, plan, t, E, it):
+    tmp = path + ".tmp.npz"
+    np.savez(tmp, t=t.cpu().numpy(), E=np.complex128(E), iteration=it, o=plan.o, v=plan.v, n1=plan.n1)
+    os.replace(tmp, path)
+
+
 def solve(plan, params, precision="fp64", print_level=0, history=None, switch_tol=1e-8, max_mixed=None,
-          base_precision="df64"):
+          base_precision="df64", checkpoint=None, checkpoint_every=5, resume=False):
     """Jacobi + DIIS CISD_SO (plan.singles) or CID_SO iteration.
 
     Returns (E, t) with t the packed amplitude vector on the device.  The
     convergence test, DIIS depth and the 'Not converged.' message follow
-    apyib/ci_wfn.py:361-378 and apyib/utils.py:104-140."""
+    apyib/ci_wfn.py:361-378 and apyib/utils.py:104-140.
+
+    checkpoint: path of an .npz file receiving the packed amplitudes, energy and
+    iteration every ``checkpoint_every`` iterations (written atomically); with
+    resume=True an existing checkpoint of the same shape is the starting point
+    (the DIIS history restarts; the reference keeps no checkpoints)."""
     e_conv, d_conv = params["e_convergence"], params["d_convergence"]
     maxit = params["max_iterations"]
     use_diis = params["DIIS"]
@@ -234,14 +246,22 @@ def solve(plan, params, precision="fp64", print_level=0, history=None, switch_to
     mixed = precision == "mixed"
     if mixed and not plan.mixed:
         raise ValueError("plan was created without mixed-precision support")
-    t = plan.guess()
+    start_it = 1
+    if resume and checkpoint and os.path.exists(checkpoint):
+        ck = np.load(checkpoint)
+        if int(ck["o"]) != plan.o or int(ck["v"]) != plan.v or int(ck["n1"]) != plan.n1:
+            raise ValueError(f"checkpoint {checkpoint} belongs to a different problem")
+        t = torch.as_tensor(ck["t"]).to(device())
+        start_it = int(ck["iteration"]) + 1
+    else:
+        t = plan.guess()
     E, _, _ = plan.combine([t], [1.0], t, t)
     diis = _DIIS(plan)
     phase = "tf32" if mixed else "fp64"
     base = None            # (t_b, E_b, r_b) for the defect-correction phase
     first = True
     stats = dict(fp64_residuals=0, tf32_residuals=0)
-    it = 1
+    it = start_it
     dE_prev = None
     while it <= maxit:
         E_old = E
@@ -295,6 +315,8 @@ def solve(plan, params, precision="fp64", print_level=0, history=None, switch_to
                 it += 1
                 continue
             dE_prev = dE
+        if checkpoint and (conv or it % checkpoint_every == 0):
+            _save_checkpoint(checkpoint, plan, t, E, it)
         if conv:
             break
         if it == maxit:

@@ -30,6 +30,7 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
 size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
 size_t tf32_planes_bytes(int64_t rows, int64_t K);
 size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K);
+size_t dfgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
 agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
                             float* dst, cudaStream_t stream);
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
@@ -529,11 +530,14 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   size_t gs = (size_t)64 << 20;
   if (P->mixed) {
     // status header + planes of the operands prepared per call + split-K partials
+    // (mixed plans also run the double-float base residual: room for its split operands)
     auto upd = [&](int64_t M, int64_t N, int64_t K, bool a_static, bool b_static) {
       size_t s = 256 + agb::tf32_partials_bytes(M, N, K);
       if (!a_static) s += align256(agb::tf32_planes_bytes(M, K));
       if (!b_static) s += align256(agb::tf32_planes_bytes(N, K));
       if (s > gs) gs = s;
+      size_t d = 256 + agb::dfgemm_scratch_bytes(M, N, K);
+      if (d > gs) gs = d;
     };
     upd(o, v, o, false, false);
     upd(o, v, v, false, false);

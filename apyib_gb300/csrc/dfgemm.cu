@@ -129,6 +129,106 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(DfArgs p) {
   }
 }
 
+// One-time split of an FP64 operand X(row,k) = src[row*s_row + k*s_k] into float4
+// (re_hi, re_lo, im_hi, im_lo) rows of length Kp (zero padded), through a shared
+// 32x32 tile so both the read and the write are coalesced.
+__global__ void df_split_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
+                                int conj, int64_t Kp, float4* __restrict__ dst) {
+  __shared__ z64 tile[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
+  const int64_t tiles_k = (Kp + 31) / 32, tiles = ((rows + 31) / 32) * tiles_k;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_k) * 32, k0 = (t % tiles_k) * 32;
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r, k;
+      if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
+      z64 v = zmk(0, 0);
+      if (r < rows && k < K) v = src[r * s_row + k * s_k];
+      if (conj) v.y = -v.y;
+      if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r = r0 + i, k = k0 + tx;
+      if (r < rows && k < Kp) dst[r * Kp + k] = split_z(tile[i][tx]);
+    }
+    __syncthreads();
+  }
+}
+
+// dfgemm_kernel on pre-split operands: A4 [M][Kp], B4 [N][Kp] (float4, K-contiguous).
+__global__ void __launch_bounds__(256) dfgemm_presplit_kernel(int64_t M, int64_t N, int64_t Kp, int64_t kchunk,
+                                                              z64 alpha, z64 beta, const float4* __restrict__ A4,
+                                                              const float4* __restrict__ B4, z64* C, int64_t ldc,
+                                                              z64* partial) {
+  __shared__ float4 As[BK][BM + 1];
+  __shared__ float4 Bs[BK][BN + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, tid = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  float sr[4][4], cr[4][4], si[4][4], ci[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sr[i][j] = cr[i][j] = si[i][j] = ci[i][j] = 0.f;
+  const int64_t kbeg = (int64_t)blockIdx.z * kchunk;
+  const int64_t kend = (kbeg + kchunk < Kp) ? kbeg + kchunk : Kp;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+    for (int r = 0; r < (BM * BK) / 256; ++r) {
+      int idx = tid + 256 * r, k = idx % BK, m = idx / BK;
+      int64_t gm = m0 + m, gk = k0 + k;
+      As[k][m] = (gm < M && gk < kend) ? A4[gm * Kp + gk] : zero4;
+    }
+#pragma unroll
+    for (int r = 0; r < (BN * BK) / 256; ++r) {
+      int idx = tid + 256 * r, k = idx % BK, n = idx / BK;
+      int64_t gn = n0 + n, gk = k0 + k;
+      Bs[k][n] = (gn < N && gk < kend) ? B4[gn * Kp + gk] : zero4;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < BK; ++kk) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          df_mac(sr[i][j], cr[i][j], a[i].x, a[i].y, b[j].x, b[j].y);
+          df_mac(sr[i][j], cr[i][j], a[i].z, a[i].w, -b[j].z, -b[j].w);
+          df_mac(si[i][j], ci[i][j], a[i].x, a[i].y, b[j].z, b[j].w);
+          df_mac(si[i][j], ci[i][j], a[i].z, a[i].w, b[j].x, b[j].y);
+        }
+    }
+    __syncthreads();
+  }
+  const bool use_beta = (beta.x != 0.0 || beta.y != 0.0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int64_t gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t gn = n0 + tx + 16 * j;
+      if (gn >= N) continue;
+      z64 acc = zmk((double)sr[i][j] + (double)cr[i][j], (double)si[i][j] + (double)ci[i][j]);
+      if (partial) {
+        partial[((int64_t)blockIdx.z * M + gm) * N + gn] = acc;
+      } else {
+        z64* c = C + gm * ldc + gn;
+        z64 out = zmul(alpha, acc);
+        if (use_beta) out = zadd(out, zmul(beta, *c));
+        *c = out;
+      }
+    }
+  }
+}
+
 __global__ void df_splitk_sum_kernel(const z64* __restrict__ partial, int splits, int64_t M, int64_t N, z64 alpha,
                                      z64 beta, z64* C, int64_t ldc) {
   int64_t total = M * N;
@@ -149,6 +249,16 @@ agb_status zgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
                     void* scratch, size_t scratch_bytes, cudaStream_t stream);
 int zgemm_splits(int64_t M, int64_t N, int64_t K, size_t scratch_bytes);
 
+// Scratch that lets dfgemm_ex take the pre-split path for this shape (split operands
+// plus split-K partials when the tile grid is small).
+size_t dfgemm_scratch_bytes(int64_t M, int64_t N, int64_t K) {
+  const int64_t Kp = (K + BK - 1) / BK * BK;
+  size_t s = ((size_t)(M + N) * (size_t)Kp * sizeof(float4) + 255) & ~(size_t)255;
+  int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+  if (tiles < 152 && Kp >= 8 * BK) s += (size_t)256 * M * N * sizeof(z64);
+  return s;
+}
+
 agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
                      const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                      void* scratch, size_t scratch_bytes, cudaStream_t stream) {
@@ -158,6 +268,41 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
     return zgemm_ex(M, N, K, alpha, A, sAm, sAk, conjA, B, sBk, sBn, conjB, beta, C, ldc, nullptr, 0, stream);
   AGB_ARG_CHECK(A && B && C, "dfgemm: null pointer");
   AGB_ARG_CHECK((M + BM - 1) / BM <= 65535, "dfgemm: M too large for grid");
+  // Pre-split path when the scratch holds both split operands (16 B per element).
+  const int64_t Kp = (K + BK - 1) / BK * BK;
+  const size_t split_bytes = ((size_t)(M + N) * (size_t)Kp * sizeof(float4) + 255) & ~(size_t)255;
+  if (scratch && scratch_bytes >= split_bytes) {
+    float4* A4 = (float4*)scratch;
+    float4* B4 = A4 + (size_t)M * Kp;
+    void* rest = (char*)scratch + split_bytes;
+    size_t rest_bytes = scratch_bytes - split_bytes;
+    auto launch_split = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, float4* dst) {
+      int64_t tiles = ((rows + 31) / 32) * ((Kp + 31) / 32);
+      int grid = (int)(tiles < 152 * 32 ? tiles : 152 * 32);
+      df_split_kernel<<<grid, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, Kp, dst);
+    };
+    launch_split(A, M, sAm, sAk, conjA, A4);
+    AGB_LAUNCH_CHECK();
+    launch_split(B, N, sBn, sBk, conjB, B4);
+    AGB_LAUNCH_CHECK();
+    int sp = zgemm_splits(M, N, Kp, rest_bytes);
+    int64_t kc = Kp;
+    if (sp > 1) {
+      kc = (Kp + sp - 1) / sp;
+      kc = (kc + BK - 1) / BK * BK;
+      sp = (int)((Kp + kc - 1) / kc);
+    }
+    dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)sp);
+    dfgemm_presplit_kernel<<<grid, 256, 0, stream>>>(M, N, Kp, kc, alpha, beta, A4, B4, C, ldc,
+                                                     sp > 1 ? (z64*)rest : nullptr);
+    AGB_LAUNCH_CHECK();
+    if (sp > 1) {
+      df_splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>((const z64*)rest, sp, M, N, alpha, beta, C,
+                                                                      ldc);
+      AGB_LAUNCH_CHECK();
+    }
+    return AGB_OK;
+  }
   int splits = scratch ? zgemm_splits(M, N, K, scratch_bytes) : 1;
   int64_t kchunk = K;
   if (splits > 1) {

@@ -28,7 +28,7 @@ def test_densities_match_oracle_and_energy(o, v, seed):
     prob = synthetic.so_factors(o, v, seed=seed)
     F = prob.fock_so()
     E, t, plan = solve_so_system(F, prob.eps_o, prob.eps_v, P, B=prob.B, return_plan=True)
-    D, G = densities(plan, t)
+    D, G = densities(plan, t, vo_coupling=True)     # the reference's exact CISD densities
     t1, t2 = plan.unpack(t)
     Dr, Gr = port.cisd_so_densities(t1.cpu().numpy(), t2.cpu().numpy(), o, o + v)
     np.testing.assert_allclose(D.cpu().numpy(), Dr, atol=1e-12)
@@ -47,12 +47,10 @@ def test_backward_matches_central_differences(h):
     n = o + v
     F = prob.fock_so()
     mask = (np.add.outer(np.arange(n) % 2, np.arange(n) % 2) % 2) == 0
-    # occupied-occupied and virtual-virtual blocks only: the reference's doubles
-    # equations (apyib/ci_wfn.py:319-334) omit the F_ov t1 coupling, so its energy is
-    # stationary (Hellmann-Feynman) only for F_ov = 0, as with canonical orbitals.
-    occ = np.arange(n) < o
-    mask = mask & (np.equal.outer(occ, occ))
-    dF = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * mask
+    # every spin-allowed Fock element, including the ov / vo blocks (the backward uses
+    # the solver-consistent D_vo; see apyib_gb300.adjoint)
+    # (scaled so the O(h^2) truncation of the central difference stays below 1e-6 relative at h = 1e-4)
+    dF = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * mask * 0.05
     dF = dF + dF.conj().T
     X = rng.standard_normal(prob.B.shape) + 1j * rng.standard_normal(prob.B.shape)
     dB = (X + np.conj(X.transpose(0, 2, 1))) / 2 * 1e-2
@@ -71,3 +69,32 @@ def test_backward_matches_central_differences(h):
         return Es.real
     fd = (E_at(h) - E_at(-h)) / (2 * h)
     assert abs(fd - pred) <= 1e-6 * max(abs(pred), 1e-8) + 1e-9, (fd, pred)
+
+
+def test_core_hamiltonian_backward_matches_central_differences():
+    """dE/dh at fixed orbitals against central differences of full GPU pipelines
+    (F_MO from h, ERI_MO, SO blocks, CISD_SO solve) along a magnetic-field-like
+    Hermitian direction dh = i * L / 2 (L real antisymmetric)."""
+    import os
+    import types
+    from apyib_gb300.adjoint import cisd_energy_core
+    from apyib_gb300.hamiltonian import Hamiltonian
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "ao_8_3_0_f.npz")))
+    H = Hamiltonian.from_arrays(g["T"], g["V"], g["S"], g["ERI"], float(g["E_nuc"]), nelec=2 * int(g["ndocc"]))
+    wfn = types.SimpleNamespace(H=H, C=g["C"], eps=g["eps"], ndocc=int(g["ndocc"]), nbf=int(g["nbf"]))
+    params = dict(method="CISD_SO", e_convergence=1e-13, d_convergence=1e-12, DIIS=True, freeze_core=False,
+                  max_iterations=100)
+    h0 = g["T"] + g["V"]
+    rng = np.random.default_rng(3)
+    Lz = rng.standard_normal(h0.shape)
+    dh = 1j * (Lz - Lz.T) / 2 * 0.5
+    ht = torch.tensor(h0, device="cuda", requires_grad=True)
+    E = cisd_energy_core(ht, wfn, params)
+    E.real.backward()
+    pred = np.real(np.sum(np.conj(ht.grad.cpu().numpy()) * dh))
+    h = 1e-4
+
+    def E_at(s):
+        return cisd_energy_core(torch.tensor(h0 + s * dh, device="cuda"), wfn, params).real.item()
+    fd = (E_at(h) - E_at(-h)) / (2 * h)
+    assert abs(fd - pred) <= 1e-6 * abs(pred) + 1e-10, (fd, pred)

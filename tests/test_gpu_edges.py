@@ -78,3 +78,20 @@ def test_full_size_properties_40_160():
     assert abs(E.imag) < 1e-12
     rdf = plan.residual(t, E, _lib.PREC_DF64)
     assert (rdf - r64).abs().max().item() < 1e-11 * max(1.0, r64.abs().max().item()) + 1e-13
+
+
+def test_checkpoint_resume_reaches_same_energy(tmp_path):
+    prob = synthetic.so_factors(6, 14, seed=8)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+
+    def plan_():
+        p = CISDPlan(prob.o, prob.v)
+        p.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
+        p.blocks_from_factors(torch.as_tensor(prob.B))
+        return p
+    E_full, _ = solve(plan_(), P)
+    ck = str(tmp_path / "ck.npz")
+    E_part, _ = solve(plan_(), dict(P, max_iterations=4), checkpoint=ck, checkpoint_every=2)
+    E_res, _ = solve(plan_(), P, checkpoint=ck, resume=True)
+    assert abs(E_res - E_full) < 1e-11
+    assert abs(E_part - E_full) > 1e-9          # the truncated run had not converged
