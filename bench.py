@@ -291,7 +291,11 @@ def main():
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
                      "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",
-                     "frac": (kern_ach / gemm_peak) if kern_ach else None, "traffic": None,
+                     "frac": (kern_ach / gemm_peak) if kern_ach else None,
+                     # DRAM bytes per launch of the same two launches (vvvv ladder, rings) at this size,
+                     # read + written, from one ncu capture of this command (profiles/tf32x3_gemm_traffic_60_240.md)
+                     "traffic": 0.5 * ((46.15 + 0.79) + (53.15 + 3.30)) * 1e9,
+                     "traffic_unit": "bytes per launch (mean of the vvvv and ring launches)",
                      "peak_note": f"{peak_kind} bf16 {peaks['bf16_tflops']} TF/s / 2 (tf32 rate) / 3 (3xTF32)",
                      "launches_timed": nl.value},
         "clocks": clocks,

@@ -122,6 +122,14 @@ def ao_case(nbf, ndocc, seed, field, nfzc=0):
             out.update(E_cisd=E, t1_cisd=t1, t2_cisd=t2)
             E, t2 = ref.ci_wfn.ci_wfn(params("CID_SO", fc=nfzc > 0), wfn).solve_CID_SO()
             out.update(E_cid=E)
+            # closed-shell spatial solvers (apyib/ci_wfn.py:51-167, 420-574)
+            import contextlib
+            import io
+            with contextlib.redirect_stdout(io.StringIO()):
+                E, t1, t2 = ref.ci_wfn.ci_wfn(params("CISD", fc=nfzc > 0), wfn).solve_CISD()
+                out.update(E_cisd_spatial=E, t1_cisd_spatial=t1, t2_cisd_spatial=t2)
+                E, t2 = ref.ci_wfn.ci_wfn(params("CID", fc=nfzc > 0), wfn).solve_CID()
+                out.update(E_cid_spatial=E, t2_cid_spatial=t2)
         else:
             E, t2 = ref.mp2_wfn.mp2_wfn(p, wfn).solve_MP2_SO()
             out.update(E_mp2=E, t2_mp2=t2)

@@ -69,3 +69,27 @@ def test_transforms_and_correlated_energies(path):
     E, t2 = mp2_wfn(params("MP2", fc), wfn).solve_MP2()
     assert abs(E - g["E_mp2_spatial"]) < 1e-10
     np.testing.assert_allclose(t2, g["t2_mp2_spatial"], atol=1e-9)
+    E, t1, t2 = ci_wfn(params("CISD", fc), wfn).solve_CISD()
+    assert abs(E - g["E_cisd_spatial"]) < 1e-10
+    np.testing.assert_allclose(t1, g["t1_cisd_spatial"], atol=1e-9)
+    np.testing.assert_allclose(t2, g["t2_cisd_spatial"], atol=1e-9)
+    E, t2 = ci_wfn(params("CID", fc), wfn).solve_CID()
+    assert abs(E - g["E_cid_spatial"]) < 1e-10
+    np.testing.assert_allclose(t2, g["t2_cid_spatial"], atol=1e-9)
+
+
+@pytest.mark.parametrize("path", FILES, ids=os.path.basename)
+def test_mixed_precision_through_ci_wfn(path):
+    """parameters['precision'] = 'mixed' through the drop-in class: tensor-core
+    iterations plus defect correction reach the reference energy to 1e-9 Eh."""
+    g = dict(np.load(path))
+    fc = int(g["nfzc"]) > 0
+    wfn = hf_wfn(make(g))
+    wfn.solve_SCF(params("RHF", fc))
+    wfn.C, wfn.eps, wfn.E_SCF = g["C"], g["eps"], g["E_scf"]
+    p = dict(params("CISD_SO", fc), precision="mixed", e_convergence=1e-12, d_convergence=1e-10)
+    E, t1, t2 = ci_wfn(p, wfn).solve_CISD_SO()
+    assert abs(E - g["E_cisd"]) < 1e-9
+    np.testing.assert_allclose(t2, g["t2_cisd"], atol=1e-8)
+    E, t2 = ci_wfn(dict(p, method="CID_SO"), wfn).solve_CID_SO()
+    assert abs(E - g["E_cid"]) < 1e-9

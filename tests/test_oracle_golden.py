@@ -131,3 +131,15 @@ def test_spatial_mp2_matches_reference(path):
     E, t2 = port.solve_mp2_spatial(g["ERI_MO"], g["eps"][nfzc:ndocc], g["eps"][ndocc:])
     assert abs(E - g["E_mp2_spatial"]) < 1e-12
     np.testing.assert_allclose(t2, g["t2_mp2_spatial"], atol=1e-13)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "ao_*.npz"))), ids=os.path.basename)
+def test_spatial_cisd_is_the_alpha_beta_block_of_the_so_solution(path):
+    """The reference's closed-shell spatial CISD / CID (apyib/ci_wfn.py:51-167,
+    420-574) give the same energies as its spin-orbital solvers, with
+    t1 = t1_SO[alpha, alpha] and t2 = t2_SO[alpha, beta, alpha, beta]."""
+    g = dict(np.load(path))
+    assert abs(g["E_cisd_spatial"] - g["E_cisd"]) < 1e-12
+    assert abs(g["E_cid_spatial"] - g["E_cid"]) < 1e-12
+    np.testing.assert_allclose(g["t2_cisd"][0::2, 1::2, 0::2, 1::2], g["t2_cisd_spatial"], atol=1e-13)
+    np.testing.assert_allclose(g["t1_cisd"][0::2, 0::2], g["t1_cisd_spatial"], atol=1e-13)
