@@ -47,6 +47,9 @@ SIGNATURES = {
                          _vp]),
     "agb_zgemm_df64": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
                               _i64, _vp]),
+    "agb_zgemm_df64_scratch_bytes": (_sz, [_i64, _i64, _i64]),
+    "agb_zgemm_df64_ex": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d,
+                                 _vp, _i64, _vp, _sz, _vp]),
     "agb_cgemm_tf32x3_scratch_bytes": (_sz, [_i64, _i64, _i64]),
     "agb_cgemm_tf32x3": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
                                 _i64, _vp, _sz, _vp]),

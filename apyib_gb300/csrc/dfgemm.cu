@@ -12,6 +12,7 @@
 // (Re = ArBr - AiBi, Im = (Ar+Ai)(Br+Bi) - ArBr - AiBi); without scratch the
 // per-tile-split four-product kernel runs.  Same contract as the FP64 zgemm.
 #include "common.cuh"
+#include "fsplit.cuh"
 
 namespace agb {
 
@@ -28,13 +29,12 @@ struct DfArgs {
   z64* partial;
 };
 
-// (re_hi, re_lo, im_hi, im_lo)
+// (re_hi, re_lo, im_hi, im_lo), split on the integer pipe
 __device__ __forceinline__ float4 split_z(z64 v) {
-  float rh = __double2float_rn(v.x);
-  float rl = __double2float_rn(v.x - (double)rh);
-  float ih = __double2float_rn(v.y);
-  float il = __double2float_rn(v.y - (double)ih);
-  return make_float4(rh, rl, ih, il);
+  uint32_t rh, rl, ih, il;
+  split_f32pair((uint64_t)__double_as_longlong(v.x), rh, rl);
+  split_f32pair((uint64_t)__double_as_longlong(v.y), ih, il);
+  return make_float4(__uint_as_float(rh), __uint_as_float(rl), __uint_as_float(ih), __uint_as_float(il));
 }
 
 // (s, c) += (xh + xl) * (yh + yl).  The _rn intrinsics keep the compiler from
@@ -158,9 +158,9 @@ __global__ void df_split3_kernel(const z64* __restrict__ src, int64_t rows, int6
       if (r < rows && k < Kp) {
         z64 v = tile[i][tx];
         dst4[r * Kp + k] = split_z(v);
-        double s = v.x + v.y;
-        float sh = __double2float_rn(s);
-        dst2[r * Kp + k] = make_float2(sh, __double2float_rn(s - (double)sh));
+        uint32_t sh, sl;
+        split_f32pair((uint64_t)__double_as_longlong(v.x + v.y), sh, sl);
+        dst2[r * Kp + k] = make_float2(__uint_as_float(sh), __uint_as_float(sl));
       }
     }
     __syncthreads();
@@ -356,6 +356,19 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
 }
 
 }  // namespace agb
+
+extern "C" size_t agb_zgemm_df64_scratch_bytes(int64_t M, int64_t N, int64_t K) {
+  return agb::dfgemm_scratch_bytes(M, N, K);
+}
+
+extern "C" agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                                        const void* A, int64_t sAm, int64_t sAk, int conjA, const void* B,
+                                        int64_t sBk, int64_t sBn, int conjB, double beta_re, double beta_im, void* C,
+                                        int64_t ldc, void* scratch, size_t scratch_bytes, void* stream) {
+  return agb::dfgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
+                        (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, scratch,
+                        scratch_bytes, (cudaStream_t)stream);
+}
 
 extern "C" agb_status agb_zgemm_df64(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
                                      int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,

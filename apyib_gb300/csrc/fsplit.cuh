@@ -1,0 +1,73 @@
+// Integer-only splits of an FP64 value into float pieces.  GB300 executes
+// double<->float conversions on its narrow FP64 pipe; these use the integer
+// pipe instead (sign / exponent / significand arithmetic on the bit pattern).
+// Values below the FP32 normal range flush to zero.
+#pragma once
+#include <stdint.h>
+
+namespace agb {
+
+// float from sign, unbiased exponent E of the leading bit, and a normalized 24-bit significand sig (bit 23 set),
+// flushed to zero below the normal range.
+__device__ __forceinline__ uint32_t pack_f32(uint32_t s, int E, uint32_t sig) {
+  int fe = E + 127;
+  if (fe <= 0 || sig == 0) return s << 31;
+  if (fe >= 255) return (s << 31) | 0x7f800000u;
+  return (s << 31) | ((uint32_t)fe << 23) | (sig & 0x7fffffu);
+}
+// x = hi + lo + O(2^-22 |x|): hi = TF32 round-to-nearest-away of x, lo = TF32 rounding of (x - hi),
+// computed with integer operations only.
+__device__ __forceinline__ void split_tf32(uint64_t u, uint32_t& hi, uint32_t& lo) {
+  uint32_t s = (uint32_t)(u >> 63);
+  int e = (int)((u >> 52) & 0x7ff);
+  if (e == 0 || e == 0x7ff) { hi = s << 31; lo = s << 31; return; }   // zero / denormal -> 0 (inf/nan not expected)
+  int64_t S = (int64_t)((u & ((1ull << 52) - 1)) | (1ull << 52));     // 53-bit significand, value S * 2^(E-52)
+  int E = e - 1023;
+  int64_t Shi = (S + (1ll << 41)) & ~((1ll << 42) - 1);               // keep 11 bits, round half away
+  int64_t r = S - Shi;                                                // |r| <= 2^41
+  int Eh = E;
+  if (Shi == (1ll << 53)) { Eh = E + 1; Shi >>= 1; }
+  hi = pack_f32(s, Eh, (uint32_t)(Shi >> 29));                        // 24-bit significand (low 13 bits zero)
+  if (r == 0) { lo = s << 31; return; }
+  uint32_t ls = s ^ (r < 0 ? 1u : 0u);
+  uint64_t ar = (uint64_t)(r < 0 ? -r : r);
+  int lz = __clzll(ar);
+  int msb = 63 - lz;                                                  // leading bit position of |r|
+  // value |r| * 2^(E-52); leading bit exponent E - 52 + msb. Normalize to 53 bits then round to 11 bits.
+  uint64_t A = ar << (52 - msb);                                      // leading bit at 52 (msb <= 41)
+  uint64_t Alo = (A + (1ull << 41)) & ~((1ull << 42) - 1);
+  int El = E - 52 + msb;
+  if (Alo == (1ull << 53)) { El += 1; Alo >>= 1; }
+  lo = pack_f32(ls, El, (uint32_t)(Alo >> 29));
+}
+// x = hi + lo with hi = float(x) (nearest-even) and lo = float(x - hi): the double-float split.
+__device__ __forceinline__ void split_f32pair(uint64_t u, uint32_t& hi, uint32_t& lo) {
+  uint32_t s = (uint32_t)(u >> 63);
+  int e = (int)((u >> 52) & 0x7ff);
+  if (e == 0 || e == 0x7ff) { hi = s << 31; lo = s << 31; return; }
+  int64_t S = (int64_t)((u & ((1ull << 52) - 1)) | (1ull << 52));
+  int E = e - 1023;
+  // round to 24 bits, nearest-even on bit 28
+  int64_t keep = S >> 29, rem = S & ((1ll << 29) - 1);
+  int64_t half = 1ll << 28;
+  if (rem > half || (rem == half && (keep & 1))) keep += 1;
+  int64_t Shi = keep << 29;
+  int64_t r = S - Shi;
+  int Eh = E;
+  if (keep == (1ll << 24)) { Eh = E + 1; keep >>= 1; }
+  hi = pack_f32(s, Eh, (uint32_t)keep);
+  if (r == 0) { lo = s << 31; return; }
+  uint32_t ls = s ^ (r < 0 ? 1u : 0u);
+  uint64_t ar = (uint64_t)(r < 0 ? -r : r);
+  int lz = __clzll(ar);
+  int msb = 63 - lz;                                                  // <= 28
+  uint64_t A = ar << (52 - msb);
+  // round to 24 bits nearest-even (|r| has at most 29 bits, so this is exact or one rounding)
+  uint64_t k2 = A >> 29, rm = A & ((1ull << 29) - 1);
+  if (rm > (1ull << 28) || (rm == (1ull << 28) && (k2 & 1))) k2 += 1;
+  int El = E - 52 + msb;
+  if (k2 == (1ull << 24)) { El += 1; k2 >>= 1; }
+  lo = pack_f32(ls, El, (uint32_t)k2);
+}
+
+}  // namespace agb

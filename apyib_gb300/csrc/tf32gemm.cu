@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fsplit.cuh"
 
 namespace agb {
 
@@ -318,11 +319,6 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
   }
 }
 
-__device__ __forceinline__ float tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
 
 // planes[4][rows][Kp]: re_hi, re_lo, im_hi, im_lo of X(row, k) = src[row*s_row + k*s_k], zero padded.
 __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t K, int64_t s_row, int64_t s_k,
@@ -347,15 +343,14 @@ __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t 
       int64_t r = r0 + i, k = k0 + tx;
       if (r >= rows_pad || k >= Kp) continue;
       z64 v = tile[i][tx];
-      float rh = tf32_rna(__double2float_rn(v.x));
-      float rl = tf32_rna(__double2float_rn(v.x - (double)rh));
-      float ih = tf32_rna(__double2float_rn(v.y));
-      float il = tf32_rna(__double2float_rn(v.y - (double)ih));
+      uint32_t rh, rl, ih, il;
+      split_tf32((uint64_t)__double_as_longlong(v.x), rh, rl);
+      split_tf32((uint64_t)__double_as_longlong(v.y), ih, il);
       int64_t off = r * Kp + k;
-      planes[off] = rh;
-      planes[plane + off] = rl;
-      planes[2 * plane + off] = ih;
-      planes[3 * plane + off] = il;
+      planes[off] = __uint_as_float(rh);
+      planes[plane + off] = __uint_as_float(rl);
+      planes[2 * plane + off] = __uint_as_float(ih);
+      planes[3 * plane + off] = __uint_as_float(il);
     }
     __syncthreads();
   }

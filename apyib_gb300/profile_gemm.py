@@ -24,13 +24,19 @@ def main(argv):
         nb = _lib.load().agb_cgemm_tf32x3_scratch_bytes(M, N, K)
         buf, sp, _ = workspace(nb)
         buf.zero_()
+    elif kind == "df64":
+        nb = _lib.load().agb_zgemm_df64_scratch_bytes(M, N, K)
+        buf, sp, _ = workspace(nb)
     for _ in range(2):
         if kind == "tf32x3":
             _lib.call("agb_cgemm_tf32x3", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
                       ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
+        elif kind == "df64":
+            _lib.call("agb_zgemm_df64_ex", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
+                      ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
         else:
-            name = "agb_zgemm_df64" if kind == "df64" else "agb_zgemm"
-            _lib.call(name, M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N, stream_ptr())
+            _lib.call("agb_zgemm", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
+                      stream_ptr())
     if kind == "tf32x3":
         _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
     torch.cuda.synchronize()

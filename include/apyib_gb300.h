@@ -72,6 +72,14 @@ agb_status agb_zgemm_df64(int64_t M, int64_t N, int64_t K, double alpha_re, doub
                           const void* A, int64_t sAm, int64_t sAk, int conjA,
                           const void* B, int64_t sBk, int64_t sBn, int conjB,
                           double beta_re, double beta_im, void* C, int64_t ldc, void* stream);
+/* With agb_zgemm_df64_scratch_bytes(M,N,K) bytes of scratch the operands are split
+ * once and the complex products use three real products (faster path). */
+size_t agb_zgemm_df64_scratch_bytes(int64_t M, int64_t N, int64_t K);
+agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                             const void* A, int64_t sAm, int64_t sAk, int conjA,
+                             const void* B, int64_t sBk, int64_t sBn, int conjB,
+                             double beta_re, double beta_im, void* C, int64_t ldc,
+                             void* scratch, size_t scratch_bytes, void* stream);
 
 /* Same contraction computed as complex FP32 with 3xTF32 split products on the
  * tcgen05 tensor cores (FP32 accumulation in TMEM), FP64 in and out.

@@ -111,3 +111,21 @@ def test_df64_gemm_accuracy(M, N, K):
     ref = A @ B
     err = np.abs(got - ref) / (np.abs(A) @ np.abs(B))
     assert err.max() < 1e-12, err.max()
+
+
+@pytest.mark.parametrize("M,N,K", [(37, 53, 29), (300, 200, 5000), (5, 7, 20000)])
+def test_df64_gemm_presplit_3m_accuracy(M, N, K):
+    """The pre-split three-product double-float path keeps ~1e-13 relative accuracy."""
+    rng = np.random.default_rng(M * 5 + K)
+    A = crandn(rng, M, K)
+    B = crandn(rng, K, N)
+    Ad, Bd = to_dev(A), to_dev(B)
+    C = torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    nb = _lib.load().agb_zgemm_df64_scratch_bytes(M, N, K)
+    buf, sp, _ = workspace(nb)
+    _lib.call("agb_zgemm_df64_ex", M, N, K, 1.0, 0.0, ptr(Ad), K, 1, 0, ptr(Bd), N, 1, 0, 0.0, 0.0, ptr(C), N,
+              ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
+    got = C.cpu().numpy()
+    ref = A @ B
+    err = np.abs(got - ref) / (np.abs(A) @ np.abs(B))
+    assert err.max() < 1e-12, err.max()
