@@ -305,8 +305,11 @@ def solve(plan, params, precision="fp64", print_level=0, history=None, switch_to
             if (it > 1 and abs(dE) < switch_tol) or stalled or capped or conv:
                 # switch to defect correction around an FP64 base residual
                 t_b = t.clone()
+                tb0 = time.perf_counter()
                 r_b = plan.residual(t_b, E, _lib.PREC_DF64 if base_precision == "df64" else _lib.PREC_FP64)
+                torch.cuda.current_stream().synchronize()
                 stats["fp64_residuals"] += 1
+                stats["base_residual_s"] = time.perf_counter() - tb0
                 base = (t_b, E, r_b)
                 phase = "refine"
                 diis = _DIIS(plan)

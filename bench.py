@@ -144,6 +144,56 @@ def run_reference(args, rank, world):
     return 0
 
 
+def ao_kernels(nbf, seed=0):
+    """J/K Fock build and AO->MO transform at nbf basis functions (real AO ERIs from
+    random real symmetric factors, complex unitary C), timed with CUDA events."""
+    import ctypes
+
+    import torch
+
+    from apyib_gb300 import _lib
+    from apyib_gb300.device import ptr, stream_ptr, workspace
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    naux = 3 * nbf
+    A = torch.randn(naux, nbf, nbf, generator=g, dtype=torch.float64)
+    A = (A + A.transpose(1, 2)) / (2 * (naux * nbf) ** 0.5)
+    eri = torch.einsum("Lmn,Lls->mnls", A.cuda(), A.cuda()).contiguous()
+    X = torch.randn(nbf, nbf, generator=g, dtype=torch.complex128)
+    C = torch.linalg.qr(X)[0].cuda().contiguous()
+    D = (C[:, : nbf // 4] @ C[:, : nbf // 4].conj().T).contiguous()
+    h = torch.zeros(nbf, nbf, dtype=torch.complex128, device="cuda")
+    F = torch.empty_like(h)
+    res = {}
+
+    def timed(fn, n=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n / 1e3
+
+    t = timed(lambda: _lib.call("agb_jk_fock", ptr(eri), nbf, ptr(D), ptr(h), 1.0, ptr(F), stream_ptr()))
+    peaks, _ = measured_peaks()
+    gbs = 8.0 * nbf ** 4 / t / 1e9
+    res["jk_fock"] = {"ms": t * 1e3, "eri_GB": 8.0 * nbf ** 4 / 1e9, "achieved_GBps": gbs,
+                      "hbm_peak_GBps": peaks["hbm_gbs"], "frac": gbs / peaks["hbm_gbs"]}
+    out = torch.empty(nbf, nbf, nbf, nbf, dtype=torch.complex128, device="cuda")
+    nb = _lib.load().agb_ao2mo_scratch_bytes(nbf, nbf)
+    buf, sp, _ = workspace(nb)
+    flops = 2.0 * 2 * nbf ** 5 + 3 * 8.0 * nbf ** 5    # real x complex first step, then three complex steps
+    for name, prec in (("fp64", _lib.PREC_FP64), ("tf32x3", _lib.PREC_TF32X3)):
+        t = timed(lambda: _lib.call("agb_ao2mo", ptr(eri), nbf, ptr(C), nbf, ptr(out), ctypes.c_void_p(sp),
+                                    ctypes.c_size_t(nb), prec, stream_ptr()), n=1)
+        res[f"ao2mo_{name}"] = {"ms": t * 1e3, "TFLOPs": flops / t / 1e12}
+    del buf, out, eri
+    torch.cuda.empty_cache()
+    return res
+
+
 def max_over_ranks(x, dist=None):
     """Max of a per-rank scalar over all ranks (identity without a process group)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
@@ -328,6 +378,8 @@ def main():
         out["solve"] = {
             "mixed_solve_s": solve_s, "E_mixed": [Em.real, Em.imag], "iterations": iters,
             "tf32_residuals": stats["tf32_residuals"], "fp64_residuals": stats["fp64_residuals"],
+            "base_residual_s": stats.get("base_residual_s"),
+            "iteration_s": [round(h["seconds"], 4) for h in hist[:-1]],
             "fp64_residual_s": fp64_res_s,
             "fp64_solve_estimate_s": iters * fp64_res_s,
             "fp64_solve_estimate_note": "iterations of the mixed solve x measured FP64 residual time",
@@ -370,6 +422,8 @@ def main():
             "E_fp64": [res3["fp64"][1].real, res3["fp64"][1].imag],
             "iterations": {"fp64": res3["fp64"][2], "mixed": res3["mixed"][2]}}
         del plan3
+    if not args.no_solve and rank == 0:
+        out["ao_kernels_nbf150"] = ao_kernels(150)
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline_oracle()
     if rank == 0:
