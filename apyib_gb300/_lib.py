@@ -80,9 +80,10 @@ SIGNATURES = {
     "agb_cisd_guess": (_int, [_vp, _vp, _vp]),
     "agb_mp2_so": (_int, [_vp, _vp, _vp, _vp, _sz, _vp]),
     "agb_mp2_spatial": (_int, [_vp, _i64, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
-    "agb_ao2mo_scratch_bytes": (_sz, [_i64, _i64]),
+    "agb_ao2mo_scratch_bytes": (_sz, [_i64, _i64, _int]),
     "agb_ao2mo": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _sz, _int, _vp]),
-    "agb_jk_fock": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp]),
+    "agb_jk_fock_scratch_bytes": (_sz, [_i64]),
+    "agb_jk_fock": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
 }
 
 

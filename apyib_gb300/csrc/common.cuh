@@ -10,6 +10,10 @@ namespace agb {
 
 typedef double2 z64;   // complex double, interleaved (re, im)
 
+// Operand-conjugation flag of the internal split kernels: 0 as stored, 1 conjugated,
+// kSrcReal the operand is a real FP64 array (same strides, in doubles; imaginary part zero).
+constexpr int kSrcReal = 2;
+
 __host__ __device__ __forceinline__ z64 zmk(double r, double i) { return make_double2(r, i); }
 __host__ __device__ __forceinline__ z64 zadd(z64 a, z64 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __host__ __device__ __forceinline__ z64 zsub(z64 a, z64 b) { return make_double2(a.x - b.x, a.y - b.y); }

@@ -12,7 +12,7 @@
 // (Re = ArBr - AiBi, Im = (Ar+Ai)(Br+Bi) - ArBr - AiBi); without scratch the
 // per-tile-split four-product kernel runs.  Same contract as the FP64 zgemm.
 #include "common.cuh"
-#include "fsplit.cuh"
+#include "dfloat.cuh"
 
 namespace agb {
 
@@ -28,28 +28,6 @@ struct DfArgs {
   int64_t kchunk;
   z64* partial;
 };
-
-// (re_hi, re_lo, im_hi, im_lo), split on the integer pipe
-__device__ __forceinline__ float4 split_z(z64 v) {
-  uint32_t rh, rl, ih, il;
-  split_f32pair((uint64_t)__double_as_longlong(v.x), rh, rl);
-  split_f32pair((uint64_t)__double_as_longlong(v.y), ih, il);
-  return make_float4(__uint_as_float(rh), __uint_as_float(rl), __uint_as_float(ih), __uint_as_float(il));
-}
-
-// (s, c) += (xh + xl) * (yh + yl).  The _rn intrinsics keep the compiler from
-// contracting the rounded product into the two-sum (which would void it).
-__device__ __forceinline__ void df_mac(float& s, float& c, float xh, float xl, float yh, float yl) {
-  float p = __fmul_rn(xh, yh);
-  float e = fmaf(xh, yh, -p);
-  e = fmaf(xh, yl, e);
-  e = fmaf(xl, yh, e);
-  float t = __fadd_rn(s, p);
-  float z = __fsub_rn(t, s);
-  float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
-  c = __fadd_rn(c, __fadd_rn(err, e));
-  s = t;
-}
 
 __global__ void __launch_bounds__(256) dfgemm_kernel(DfArgs p) {
   __shared__ float4 As[BK][BM + 1];
@@ -148,8 +126,11 @@ __global__ void df_split3_kernel(const z64* __restrict__ src, int64_t rows, int6
       int64_t r, k;
       if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
       z64 v = zmk(0, 0);
-      if (r < rows && k < K) v = src[r * s_row + k * s_k];
-      if (conj) v.y = -v.y;
+      if (r < rows && k < K) {
+        if (conj == kSrcReal) v.x = ((const double*)src)[r * s_row + k * s_k];
+        else v = src[r * s_row + k * s_k];
+      }
+      if (conj == 1) v.y = -v.y;
       if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
     }
     __syncthreads();
@@ -335,6 +316,10 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
     }
     return AGB_OK;
   }
+  if (conjA == kSrcReal || conjB == kSrcReal) {
+    agb_set_error_message("dfgemm: a real operand needs scratch for the pre-split path", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
   int splits = scratch ? zgemm_splits(M, N, K, scratch_bytes) : 1;
   int64_t kchunk = K;
   if (splits > 1) {
@@ -365,6 +350,7 @@ extern "C" agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double 
                                         const void* A, int64_t sAm, int64_t sAk, int conjA, const void* B,
                                         int64_t sBk, int64_t sBn, int conjB, double beta_re, double beta_im, void* C,
                                         int64_t ldc, void* scratch, size_t scratch_bytes, void* stream) {
+  AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
   return agb::dfgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                         (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, scratch,
                         scratch_bytes, (cudaStream_t)stream);
@@ -373,6 +359,7 @@ extern "C" agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double 
 extern "C" agb_status agb_zgemm_df64(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
                                      int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,
                                      int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* stream) {
+  AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
   return agb::dfgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                         (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, nullptr, 0,
                         (cudaStream_t)stream);

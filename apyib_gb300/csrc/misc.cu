@@ -1,6 +1,7 @@
 // Spin-orbital expansion, amplitude pack/unpack, MP2_SO, the AO->MO
 // four-index transform and the one-pass J/K Fock build.
 #include "cisd_plan.h"
+#include "dfloat.cuh"
 
 namespace agb {
 
@@ -11,6 +12,10 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
                         int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                         void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
+agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                     void* scratch, size_t scratch_bytes, cudaStream_t stream);
+size_t dfgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
 
 namespace {
 
@@ -171,56 +176,124 @@ __global__ void conj_kernel(const z64* __restrict__ src, int64_t n, z64* __restr
     dst[e] = zconj(src[e]);
 }
 
-// ---- J/K: one pass over real (mn|ls).  CTA per m; for each x the plane e[x][y][z] = (mx|yz)
-// contributes J[m][x] += sum_yz e D[y][z] and K[m][y] += sum_z e D[x][z].
-constexpr int JK_THREADS = 512;
-__global__ void __launch_bounds__(JK_THREADS) jk_kernel(const double* __restrict__ eri, int n,
-                                                        const z64* __restrict__ D, const z64* __restrict__ h,
-                                                        double scale, z64* __restrict__ F) {
-  extern __shared__ z64 ksh[];  // K[m][y], n entries
-  __shared__ z64 red[JK_THREADS / 32];
-  const int m = blockIdx.x;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = JK_THREADS / 32;
-  for (int y = threadIdx.x; y < n; y += JK_THREADS) ksh[y] = zmk(0, 0);
-  __syncthreads();
-  const int64_t nn = (int64_t)n * n;
-  const double* base = eri + (int64_t)m * n * nn;
-  for (int x = 0; x < n; ++x) {
-    const double* plane = base + (int64_t)x * nn;
-    z64 jacc = zmk(0, 0);
-    for (int y = w; y < n; y += nw) {
-      z64 kacc = zmk(0, 0);
-      const double* row = plane + (int64_t)y * n;
-      for (int z = lane; z < n; z += 32) {
-        double e = row[z];
-        z64 dyz = D[(int64_t)y * n + z], dxz = D[(int64_t)x * n + z];
-        jacc.x = fma(e, dyz.x, jacc.x); jacc.y = fma(e, dyz.y, jacc.y);
-        kacc.x = fma(e, dxz.x, kacc.x); kacc.y = fma(e, dxz.y, kacc.y);
-      }
-      kacc = warp_sum(kacc);
-      if (lane == 0) ksh[y] = zadd(ksh[y], kacc);
-    }
-    jacc = warp_sum(jacc);
-    if (lane == 0) red[w] = jacc;
-    __syncthreads();
-    if (w == 0) {
-      z64 s = lane < nw ? red[lane] : zmk(0, 0);
-      s = warp_sum(s);
-      if (lane == 0) {
-        // F[m][x] = h + scale*(2J - K) ; K added after the loop
-        z64 hv = h ? h[(int64_t)m * n + x] : zmk(0, 0);
-        F[(int64_t)m * n + x] = zmk(hv.x + 2.0 * scale * s.x, hv.y + 2.0 * scale * s.y);
-      }
-    }
-    __syncthreads();
-  }
-  __syncthreads();
-  for (int y = threadIdx.x; y < n; y += JK_THREADS) {
-    z64 f = F[(int64_t)m * n + y];
-    F[(int64_t)m * n + y] = zmk(f.x - scale * ksh[y].x, f.y - scale * ksh[y].y);
+// ---- J/K: one pass over the real (mn|ls), products and sums in double-float on the FP32 pipe
+// (four complex-by-real multiply-adds per integral would otherwise keep the FP64 pipe, not HBM,
+// the bound).  CTA per m.  The rows e[m][x][y][0..n) are walked in groups of JK_Y rows
+// (fixed x, consecutive y): g = yb*n + x, yb = y / JK_Y, and each warp takes one contiguous
+// range of groups.  Lane z-partials accumulate
+//   J[m][x] += sum_yz e D[y][z]   (reduced over the lanes once per group)
+//   K[m][y] += sum_xz e D[x][z]   (kept per lane while the warp stays in one y block)
+// into per-warp slots; the slots are summed in a fixed order, so results are deterministic.
+constexpr int JK_Y = 4;
+
+__global__ void jk_split_kernel(const z64* __restrict__ D, int64_t nn, float4* __restrict__ D4) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x)
+    D4[e] = split_z(D[e]);
+}
+
+__device__ __forceinline__ void df_warp_sum(float& s, float& c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float bs = __shfl_xor_sync(0xffffffffu, s, o), bc = __shfl_xor_sync(0xffffffffu, c, o);
+    df_add(s, c, bs, bc);
   }
 }
 
+__global__ void __launch_bounds__(512) jk_df_kernel(const double* __restrict__ eri, int n,
+                                                    const float4* __restrict__ D4, const z64* __restrict__ h,
+                                                    double scale, z64* __restrict__ F) {
+  extern __shared__ float4 jk_sh[];       // Jw[nw][n], Kw[nw][n]: (re_s, re_c, im_s, im_c)
+  const int nw = blockDim.x >> 5;
+  float4* Jw = jk_sh;
+  float4* Kw = jk_sh + (size_t)nw * n;
+  const int m = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 2 * nw * n; i += blockDim.x) jk_sh[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncthreads();
+  const int nyb = (n + JK_Y - 1) / JK_Y;
+  const int64_t ngroups = (int64_t)nyb * n;
+  const int64_t g0 = ngroups * w / nw, g1 = ngroups * (w + 1) / nw;
+  const double* slab = eri + (int64_t)m * n * n * n;
+  float ks[JK_Y][4];
+#pragma unroll
+  for (int i = 0; i < JK_Y; ++i) ks[i][0] = ks[i][1] = ks[i][2] = ks[i][3] = 0.f;
+  int cur_yb = g0 < g1 ? (int)(g0 / n) : -1;
+  auto flush_k = [&](int yb) {
+#pragma unroll
+    for (int i = 0; i < JK_Y; ++i) {
+      df_warp_sum(ks[i][0], ks[i][1]);
+      df_warp_sum(ks[i][2], ks[i][3]);
+      const int y = yb * JK_Y + i;
+      if (lane == 0 && y < n) {
+        float4 k = Kw[(size_t)w * n + y];
+        df_add(k.x, k.y, ks[i][0], ks[i][1]);
+        df_add(k.z, k.w, ks[i][2], ks[i][3]);
+        Kw[(size_t)w * n + y] = k;
+      }
+      ks[i][0] = ks[i][1] = ks[i][2] = ks[i][3] = 0.f;
+    }
+  };
+  for (int64_t g = g0; g < g1; ++g) {
+    const int yb = (int)(g / n), x = (int)(g % n);
+    if (yb != cur_yb) {
+      flush_k(cur_yb);
+      cur_yb = yb;
+    }
+    float jr = 0.f, jrc = 0.f, ji = 0.f, jic = 0.f;
+    const int y0 = yb * JK_Y;
+    // rows past n re-read row n-1 (in bounds) and contribute zero, so every load is unconditional
+    int64_t roff[JK_Y];
+#pragma unroll
+    for (int i = 0; i < JK_Y; ++i) roff[i] = (int64_t)min(y0 + i, n - 1);
+    const double* xrows = slab + (int64_t)x * n * n;
+    for (int z0 = lane; z0 < n; z0 += 64) {
+      double ev[2][JK_Y];
+      float4 dyv[2][JK_Y], dxv[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int z = min(z0 + 32 * u, n - 1);
+        dxv[u] = __ldg(D4 + (int64_t)x * n + z);
+#pragma unroll
+        for (int i = 0; i < JK_Y; ++i) {
+          ev[u][i] = __ldcs(xrows + roff[i] * n + z);
+          dyv[u][i] = __ldg(D4 + roff[i] * n + z);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const bool zok = z0 + 32 * u < n;
+#pragma unroll
+        for (int i = 0; i < JK_Y; ++i) {
+          float eh, el;
+          split_f32pair_fast((zok && y0 + i < n) ? ev[u][i] : 0.0, eh, el);
+          df_mac(jr, jrc, eh, el, dyv[u][i].x, dyv[u][i].y);
+          df_mac(ji, jic, eh, el, dyv[u][i].z, dyv[u][i].w);
+          df_mac(ks[i][0], ks[i][1], eh, el, dxv[u].x, dxv[u].y);
+          df_mac(ks[i][2], ks[i][3], eh, el, dxv[u].z, dxv[u].w);
+        }
+      }
+    }
+    df_warp_sum(jr, jrc);
+    df_warp_sum(ji, jic);
+    if (lane == 0) {
+      float4 j = Jw[(size_t)w * n + x];
+      df_add(j.x, j.y, jr, jrc);
+      df_add(j.z, j.w, ji, jic);
+      Jw[(size_t)w * n + x] = j;
+    }
+  }
+  if (cur_yb >= 0) flush_k(cur_yb);
+  __syncthreads();
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    double Jr = 0, Ji = 0, Kr = 0, Ki = 0;
+    for (int v = 0; v < nw; ++v) {
+      const float4 j = Jw[(size_t)v * n + p], k = Kw[(size_t)v * n + p];
+      Jr += (double)j.x + (double)j.y; Ji += (double)j.z + (double)j.w;
+      Kr += (double)k.x + (double)k.y; Ki += (double)k.z + (double)k.w;
+    }
+    const z64 hv = h ? h[(int64_t)m * n + p] : zmk(0, 0);
+    F[(int64_t)m * n + p] = zmk(hv.x + scale * (2.0 * Jr - Kr), hv.y + scale * (2.0 * Ji - Ki));
+  }
+}
 }  // namespace
 }  // namespace agb
 
@@ -295,29 +368,35 @@ agb_status agb_mp2_so(agb_cisd_plan* P, void* t, void* E_out, void* partials, si
   return AGB_OK;
 }
 
-size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo) {
+size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision) {
   int64_t big = nbf * nbf * nbf * nmo;
   int64_t mid = nbf * nbf * nmo * nmo;
   int64_t a = big > mid ? big : mid;
   size_t s = sizeof(z64) * (size_t)a;
   s = (s + 255) & ~(size_t)255;
   size_t gs = (size_t)64 << 20;
-  size_t t1 = cgemm_tf32x3_scratch(nbf * nbf * nmo, nmo, nbf);
-  size_t t2 = cgemm_tf32x3_scratch(nbf * nmo * nmo, nmo, nbf);
-  size_t t3 = cgemm_tf32x3_scratch(nmo * nmo * nmo, nmo, nbf);
-  if (t1 > gs) gs = t1;
-  if (t2 > gs) gs = t2;
-  if (t3 > gs) gs = t3;
+  // the four quarter steps: rows (n l s), (l s p), (s p q), (p q r); N = nmo, K = nbf
+  const int64_t rows[4] = {nbf * nbf * nbf, nbf * nbf * nmo, nbf * nmo * nmo, nmo * nmo * nmo};
+  for (int i = 0; i < 4; ++i) {
+    size_t need = 0;
+    if (precision == AGB_PREC_TF32X3) need = cgemm_tf32x3_scratch(rows[i], nmo, nbf);
+    else if (precision == AGB_PREC_DF64) need = dfgemm_scratch_bytes(rows[i], nmo, nbf);
+    if (need > gs) gs = need;
+  }
   return 2 * s + sizeof(z64) * (size_t)(nbf * nmo) + 256 + gs + 256;
 }
 
 // Each quarter step contracts the leading AO index and appends the new MO index
-// last: (m n l s) -> (n l s p) -> (l s p q) -> (s p q r) -> (p q r s).
+// last: (m n l s) -> (n l s p) -> (l s p q) -> (s p q r) -> (p q r s).  The
+// first step multiplies the real AO integrals by the complex C*: a real GEMM on
+// interleaved columns in FP64 mode; in the tensor-core and double-float modes
+// the split kernels read the real array directly (imaginary part zero).
 agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t nmo, void* ERI_MO, void* scratch,
                      size_t scratch_bytes, int precision, void* stream) {
   AGB_ARG_CHECK(ERI_AO && C && ERI_MO && nbf > 0 && nmo > 0, "ao2mo: bad argument");
-  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_TF32X3, "ao2mo: unknown precision");
-  if (!scratch || scratch_bytes < agb_ao2mo_scratch_bytes(nbf, nmo)) {
+  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_TF32X3 || precision == AGB_PREC_DF64,
+                "ao2mo: unknown precision");
+  if (!scratch || scratch_bytes < agb_ao2mo_scratch_bytes(nbf, nmo, precision)) {
     agb_set_error_message("ao2mo: scratch too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;
   }
@@ -334,39 +413,57 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
   if (precision == AGB_PREC_TF32X3) AGB_CUDA_TRY(cudaMemsetAsync(gs, 0, 256, st));  // GEMM status word
   conj_kernel<<<grid_for(nbf * nmo, 256), 256, 0, st>>>((const z64*)C, nbf * nmo, Cc);
   AGB_LAUNCH_CHECK();
-  // step 1 (real x complex as a real GEMM on interleaved columns): Y1[(n l s)][p] = sum_m (mn|ls) C*[m,p]
-  {
+  // out[(rest)][q] = sum_k T[k][(rest)] Cop[k][q]
+  auto step = [&](const z64* T, int64_t Mrest, int kind, const z64* Cop, z64* out) -> agb_status {
+    if (precision == AGB_PREC_TF32X3)
+      return cgemm_tf32x3(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
+                          gs_bytes, st);
+    if (precision == AGB_PREC_DF64)
+      return dfgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
+                       gs_bytes, st);
+    return zgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, 0, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs, gs_bytes,
+                    st);
+  };
+  // step 1: Y1[(n l s)][p] = sum_m (mn|ls) C*[m,p]
+  if (precision == AGB_PREC_FP64) {
     int64_t M = nbf * nbf * nbf, N = 2 * nmo, K = nbf;
     dim3 grid((unsigned)((N + DBN - 1) / DBN), (unsigned)((M + DBM - 1) / DBM));
     AGB_ARG_CHECK((M + DBM - 1) / DBM <= 65535, "ao2mo: nbf too large");
     dgemm_kernel<<<grid, 256, 0, st>>>(M, N, K, ERI_AO, 1, M, (const double*)Cc, N, 1, (double*)Y1, N);
     AGB_LAUNCH_CHECK();
+  } else {
+    AGB_STATUS_TRY(step((const z64*)ERI_AO, nbf * nbf * nbf, kSrcReal, Cc, Y1));
   }
-  auto step = [&](const z64* T, int64_t Mrest, const z64* Cop, z64* out) -> agb_status {
-    // out[(rest)][q] = sum_k T[k][(rest)] Cop[k][q]
-    if (precision == AGB_PREC_TF32X3)
-      return cgemm_tf32x3(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, 0, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
-                          gs_bytes, st);
-    return zgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, 0, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs, gs_bytes,
-                    st);
-  };
   // step 2: Y2[(l s p)][q] = sum_n Y1[n][(l s p)] C[n,q]
-  AGB_STATUS_TRY(step(Y1, nbf * nbf * nmo, (const z64*)C, Y2));
+  AGB_STATUS_TRY(step(Y1, nbf * nbf * nmo, 0, (const z64*)C, Y2));
   // step 3: Y1[(s p q)][r] = sum_l Y2[l][(s p q)] C*[l,r]
-  AGB_STATUS_TRY(step(Y2, nbf * nmo * nmo, Cc, Y1));
+  AGB_STATUS_TRY(step(Y2, nbf * nmo * nmo, 0, Cc, Y1));
   // step 4: ERI_MO[(p q r)][s] = sum_s' Y1[s'][(p q r)] C[s',s]
-  AGB_STATUS_TRY(step(Y1, nmo * nmo * nmo, (const z64*)C, (z64*)ERI_MO));
+  AGB_STATUS_TRY(step(Y1, nmo * nmo * nmo, 0, (const z64*)C, (z64*)ERI_MO));
   return AGB_OK;
 }
 
+size_t agb_jk_fock_scratch_bytes(int64_t nbf) { return sizeof(float4) * (size_t)nbf * (size_t)nbf + 256; }
+
 agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale, void* F,
-                       void* stream) {
+                       void* scratch, size_t scratch_bytes, void* stream) {
   AGB_ARG_CHECK(ERI_AO && D && F && nbf > 0 && nbf < 65536, "jk_fock: bad argument");
-  size_t sh = sizeof(z64) * (size_t)nbf;
-  AGB_ARG_CHECK(sh <= 200 * 1024, "jk_fock: nbf too large for the shared K row");
-  if (sh > 48 * 1024) AGB_CUDA_TRY(cudaFuncSetAttribute(jk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
-  jk_kernel<<<(unsigned)nbf, JK_THREADS, sh, (cudaStream_t)stream>>>(ERI_AO, (int)nbf, (const z64*)D,
-                                                                     (const z64*)h, scale, (z64*)F);
+  if (!scratch || scratch_bytes < agb_jk_fock_scratch_bytes(nbf)) {
+    agb_set_error_message("jk_fock: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  // 16 warps while their J/K slots fit in shared memory, fewer for large nbf
+  int nw = 16;
+  while (nw > 1 && (size_t)2 * nw * nbf * sizeof(float4) > 200 * 1024) nw >>= 1;
+  const size_t sh = (size_t)2 * nw * nbf * sizeof(float4);
+  AGB_ARG_CHECK(sh <= 200 * 1024, "jk_fock: nbf too large for the shared J/K slots");
+  float4* D4 = (float4*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  const int64_t nn = nbf * nbf;
+  jk_split_kernel<<<grid_for(nn, 256), 256, 0, st>>>((const z64*)D, nn, D4);
+  AGB_LAUNCH_CHECK();
+  if (sh > 48 * 1024) AGB_CUDA_TRY(cudaFuncSetAttribute(jk_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  jk_df_kernel<<<(unsigned)nbf, 32 * nw, sh, st>>>(ERI_AO, (int)nbf, D4, (const z64*)h, scale, (z64*)F);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }

@@ -334,8 +334,11 @@ __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t 
       int64_t r, k;
       if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
       z64 v = zmk(0, 0);
-      if (r < nrows && k < K) v = src[r * s_row + k * s_k];
-      if (conj) v.y = -v.y;
+      if (r < nrows && k < K) {
+        if (conj == kSrcReal) v.x = ((const double*)src)[r * s_row + k * s_k];
+        else v = src[r * s_row + k * s_k];
+      }
+      if (conj == 1) v.y = -v.y;
       if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
     }
     __syncthreads();
@@ -527,6 +530,7 @@ agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, do
                             int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn, int conjB,
                             double beta_re, double beta_im, void* C, int64_t ldc, void* scratch, size_t scratch_bytes,
                             void* stream) {
+  AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
   return agb::cgemm_tf32x3(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                            (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
                            scratch, scratch_bytes, (cudaStream_t)stream);

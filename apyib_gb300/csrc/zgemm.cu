@@ -226,6 +226,7 @@ agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, con
 extern "C" agb_status agb_zgemm(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
                                 int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,
                                 int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* stream) {
+  AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
   return agb::zgemm(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                     (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
                     (cudaStream_t)stream);

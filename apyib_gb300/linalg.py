@@ -46,5 +46,8 @@ def jk_fock(ERI_AO, D, h, scale):
     D = D.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
     h = h.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
     F = torch.empty((n, n), dtype=torch.complex128, device=device())
-    _lib.call("agb_jk_fock", ptr(eri), n, ptr(D), ptr(h), float(scale), ptr(F), stream_ptr())
+    nb = _lib.load().agb_jk_fock_scratch_bytes(n)
+    buf, sp, _ = workspace(nb)
+    _lib.call("agb_jk_fock", ptr(eri), n, ptr(D), ptr(h), float(scale), ptr(F), ctypes.c_void_p(sp),
+              ctypes.c_size_t(nb), stream_ptr())
     return F

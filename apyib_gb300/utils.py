@@ -58,13 +58,15 @@ def compute_F_MO(parameters, wfn, C_list, return_torch=False):
 
 
 def compute_ERI_MO(parameters, wfn, C_list, return_torch=False, precision=_lib.PREC_FP64):
-    """apyib/utils.py:258-279: four quarter-step AO->MO transform (complex C, real AO ERIs)."""
+    """apyib/utils.py:258-279: four quarter-step AO->MO transform (complex C, real AO ERIs).
+    precision: _lib.PREC_FP64 (default), PREC_DF64 (double-float GEMMs on the FP32
+    pipe, ~1e-13 relative) or PREC_TF32X3 (tensor cores, ~1e-6 relative)."""
     t = C_list[3]
     C = to_dev(np.asarray(wfn.C)[:, t])
     ERI = to_dev(wfn.H.ERI, torch.float64)
     nbf, nmo = C.shape
     out = torch.empty((nmo, nmo, nmo, nmo), dtype=torch.complex128, device=device())
-    nb = _lib.load().agb_ao2mo_scratch_bytes(nbf, nmo)
+    nb = _lib.load().agb_ao2mo_scratch_bytes(nbf, nmo, int(precision))
     buf, sp, _ = workspace(nb)
     _lib.call("agb_ao2mo", ptr(ERI), nbf, ptr(C), nmo, ptr(out), ctypes.c_void_p(sp), ctypes.c_size_t(nb),
               int(precision), stream_ptr())

@@ -225,16 +225,22 @@ agb_status agb_mp2_spatial(const void* ERI_MO, int64_t nmo, int64_t no, const do
 
 /* ERI_MO[p,q,r,s] = sum C*[m,p] C[n,q] C*[l,r] C[s',s] (mn|ls') for real AO ERIs
  * (nbf^4 doubles) and complex C (nbf x nmo), four quarter steps
- * (apyib/utils.py:274-277).  scratch: agb_ao2mo_scratch_bytes. */
-size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo);
+ * (apyib/utils.py:274-277).  precision: AGB_PREC_FP64 (FP64 pipe),
+ * AGB_PREC_DF64 (double-float GEMMs, ~1e-13 relative) or AGB_PREC_TF32X3
+ * (tensor cores, ~1e-6 relative).  scratch: agb_ao2mo_scratch_bytes for the
+ * same precision. */
+size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision);
 agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t nmo, void* ERI_MO,
                      void* scratch, size_t scratch_bytes, int precision, void* stream);
 
 /* F = h + scale * sum_ls D[l,s] (2 (mn|ls) - (ml|ns)) with real AO ERIs and
- * complex D, h, F (nbf x nbf).  One pass over the ERIs for J and K.
- * apyib/hf_wfn.py:81 (scale 0.5) and apyib/utils.py:241,249 (scale 1). */
+ * complex D, h (may be NULL: zero), F (nbf x nbf).  One pass over the ERIs for
+ * J and K, products and sums in double-float arithmetic (~1e-14 relative);
+ * deterministic.  apyib/hf_wfn.py:81 (scale 0.5) and apyib/utils.py:241,249
+ * (scale 1).  scratch: agb_jk_fock_scratch_bytes(nbf) (the split density). */
+size_t agb_jk_fock_scratch_bytes(int64_t nbf);
 agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale,
-                       void* F, void* stream);
+                       void* F, void* scratch, size_t scratch_bytes, void* stream);
 
 #ifdef __cplusplus
 }

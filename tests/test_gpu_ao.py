@@ -93,3 +93,19 @@ def test_mixed_precision_through_ci_wfn(path):
     np.testing.assert_allclose(t2, g["t2_cisd"], atol=1e-8)
     E, t2 = ci_wfn(dict(p, method="CID_SO"), wfn).solve_CID_SO()
     assert abs(E - g["E_cid"]) < 1e-9
+
+
+@pytest.mark.parametrize("prec,tol", [(_lib.PREC_DF64, 1e-12), (_lib.PREC_TF32X3, 2e-6)])
+def test_transform_precision_modes(prec, tol):
+    """The double-float and 3xTF32 transforms (the first quarter step reads the real
+    AO integrals directly) against the reference's ERI_MO fixture."""
+    g = dict(np.load(FILES[0]))
+    fc = int(g["nfzc"]) > 0
+    wfn = hf_wfn(make(g))
+    wfn.C = g["C"]
+    wfn.eps = g["eps"]
+    p = params("CISD_SO", fc)
+    C_list, _ = utils.get_slices(p, wfn)
+    ERI_MO = utils.compute_ERI_MO(p, wfn, C_list, precision=prec)
+    scale = np.abs(g["ERI_MO"]).max()
+    np.testing.assert_allclose(ERI_MO, g["ERI_MO"], atol=tol * scale)

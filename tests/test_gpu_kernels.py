@@ -76,16 +76,26 @@ def test_tf32x3_gemm_alpha_beta_and_transposed_b():
     assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5
 
 
-def test_jk_fock_matches_oracle():
-    rng = np.random.default_rng(3)
-    n = 19
-    A = rng.standard_normal((40, n, n))
-    A = A + A.transpose(0, 2, 1)
-    eri = np.einsum("Lmn,Lls->mnls", A, A) / 40
+@pytest.mark.parametrize("n,symmetric", [(1, True), (19, True), (45, True), (70, True), (33, False)])
+def test_jk_fock_matches_oracle(n, symmetric):
+    """Double-float J/K against the FP64 NumPy restatement; n = 45, 70 leave a ragged
+    last block of rows, n = 33 a ragged last lane round, and the non-symmetric case
+    checks that no integral symmetry is assumed."""
+    rng = np.random.default_rng(3 + n)
+    if symmetric:
+        A = rng.standard_normal((40, n, n))
+        A = A + A.transpose(0, 2, 1)
+        eri = np.einsum("Lmn,Lls->mnls", A, A) / 40
+    else:
+        eri = rng.standard_normal((n, n, n, n))
     D = crandn(rng, n, n)
     h = crandn(rng, n, n)
     F = jk_fock(to_dev(eri, torch.float64), to_dev(D), to_dev(h), 0.5).cpu().numpy()
-    np.testing.assert_allclose(F, port.jk_fock(h, eri, D, 0.5), atol=1e-11)
+    ref = port.jk_fock(h, eri, D, 0.5)
+    scale = np.abs(eri).max() * np.abs(D).max() * n * n
+    np.testing.assert_allclose(F, ref, atol=1e-13 * scale)
+    F2 = jk_fock(to_dev(eri, torch.float64), to_dev(D), to_dev(h), 0.5).cpu().numpy()
+    np.testing.assert_array_equal(F, F2)        # deterministic
 
 
 def test_so_expansion_matches_oracle():
