@@ -23,6 +23,7 @@ AGB_ERR_WORKSPACE = 5
 PREC_FP64 = 0
 PREC_TF32X3 = 1
 PREC_DF64 = 2
+PREC_OZAKI = 3
 
 PLAN_MIXED = 1
 PLAN_NO_SINGLES = 2
@@ -50,6 +51,9 @@ SIGNATURES = {
     "agb_zgemm_df64_scratch_bytes": (_sz, [_i64, _i64, _i64]),
     "agb_zgemm_df64_ex": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d,
                                  _vp, _i64, _vp, _sz, _vp]),
+    "agb_zgemm_oz_scratch_bytes": (_sz, [_i64, _i64, _i64]),
+    "agb_zgemm_oz": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
+                            _i64, _vp, _sz, _vp]),
     "agb_cgemm_tf32x3_scratch_bytes": (_sz, [_i64, _i64, _i64]),
     "agb_cgemm_tf32x3": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
                                 _i64, _vp, _sz, _vp]),

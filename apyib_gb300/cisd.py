@@ -14,9 +14,11 @@ Precision modes:
     r(t) = r64(t_b) + L32(t - t_b) - E_b (t - t_b) - (E - E_b) t,
     i.e. only the small amplitude change goes through the FP32 tensor cores
     (defect correction).  DIIS, the update and all sums stay FP64.  The base
-    residual's GEMMs run in double-float on the FP32 pipe (``base_precision
-    ='df64'``, ~2^-44 relative, several times faster than GB300's FP64 pipe)
-    or in FP64 (``'fp64'``); its elementwise work is FP64 either way.
+    residual's large GEMMs run on the bf16 tensor cores with six-slice Ozaki
+    splitting (``base_precision='ozaki'``, ~1e-12 of sum |a||b|), its small
+    ones in double-float; ``'df64'`` runs every GEMM in double-float on the
+    FP32 pipe (~2^-44 relative) and ``'fp64'`` on the FP64 pipe; the
+    elementwise work is FP64 in every mode.
 """
 from __future__ import annotations
 
@@ -87,15 +89,16 @@ class CISDPlan:
         _lib.call("agb_cisd_blocks_from_so", self._h, ptr(g), stream_ptr())
 
     def blocks_from_factors(self, B, precision=_lib.PREC_FP64):
-        """Blocks from Hermitian factors; precision PREC_FP64 or PREC_DF64 (double-float
-        products, ~1e-13 relative, several times faster on GB300)."""
+        """Blocks from Hermitian factors; precision PREC_FP64, PREC_DF64 (double-float
+        products, ~1e-13 relative, several times faster on GB300) or PREC_OZAKI (the
+        large products on the bf16 tensor cores, ~1e-12 of sum |a||b|)."""
         Bd = B.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
         naux = Bd.shape[0]
         nb = _lib.load().agb_cisd_factor_scratch_bytes(self._h, naux)
         buf, sptr, _ = workspace(nb)
         _lib.call("agb_cisd_blocks_from_factors", self._h, ptr(Bd), ctypes.c_int64(naux), _vp(sptr),
                   ctypes.c_size_t(nb), int(precision), stream_ptr())
-        torch.cuda.current_stream().synchronize()
+        self.check_status()
         del buf
 
     # ------------------------------------------------------------ kernels
@@ -227,8 +230,11 @@ def _save_checkpoint(path, plan, t, E, it):
     os.replace(tmp, path)
 
 
+_BASE_PREC = {"ozaki": _lib.PREC_OZAKI, "df64": _lib.PREC_DF64, "fp64": _lib.PREC_FP64}
+
+
 def solve(plan, params, precision="fp64", print_level=0, history=None, switch_tol=1e-8, max_mixed=None,
-          base_precision="df64", checkpoint=None, checkpoint_every=5, resume=False):
+          base_precision="ozaki", checkpoint=None, checkpoint_every=5, resume=False):
     """Jacobi + DIIS CISD_SO (plan.singles) or CID_SO iteration.
 
     Returns (E, t) with t the packed amplitude vector on the device.  The
@@ -306,8 +312,8 @@ def solve(plan, params, precision="fp64", print_level=0, history=None, switch_to
                 # switch to defect correction around an FP64 base residual
                 t_b = t.clone()
                 tb0 = time.perf_counter()
-                r_b = plan.residual(t_b, E, _lib.PREC_DF64 if base_precision == "df64" else _lib.PREC_FP64)
-                torch.cuda.current_stream().synchronize()
+                r_b = plan.residual(t_b, E, _BASE_PREC[base_precision])
+                plan.check_status()
                 stats["fp64_residuals"] += 1
                 stats["base_residual_s"] = time.perf_counter() - tb0
                 base = (t_b, E, r_b)

@@ -31,6 +31,14 @@ size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
 size_t tf32_planes_bytes(int64_t rows, int64_t K);
 size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K);
 size_t dfgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
+size_t ozgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
+int64_t ozgemm_tiles(int64_t M, int64_t N);
+agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                     void* scratch, size_t scratch_bytes, cudaStream_t stream);
+// GEMMs with at least this many 128x128 output tiles take the Ozaki tensor-core path in
+// AGB_PREC_OZAKI mode; smaller ones (few tiles, long K) the split-K double-float kernel.
+constexpr int64_t kOzMinTiles = 152;
 agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
                             float* dst, cudaStream_t stream);
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
@@ -538,6 +546,10 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
       if (s > gs) gs = s;
       size_t d = 256 + agb::dfgemm_scratch_bytes(M, N, K);
       if (d > gs) gs = d;
+      if (agb::ozgemm_tiles(M, N) >= agb::kOzMinTiles) {
+        size_t z = agb::ozgemm_scratch_bytes(M, N, K);
+        if (z > gs) gs = z;
+      }
     };
     upd(o, v, o, false, false);
     upd(o, v, v, false, false);
@@ -609,7 +621,10 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
     return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
                             P->gemm_scratch_bytes - off, st);
   }
-  if (prec == AGB_PREC_DF64)
+  if (prec == AGB_PREC_OZAKI && ozgemm_tiles(M, N) >= kOzMinTiles)
+    return ozgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, P->gemm_scratch,
+                     P->gemm_scratch_bytes, st);
+  if (prec == AGB_PREC_DF64 || prec == AGB_PREC_OZAKI)
     return dfgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, (char*)P->gemm_scratch + 256,
                      P->gemm_scratch_bytes - 256, st);
   // FP64 split-K partials start past the 256-byte status header of the scratch.
@@ -787,8 +802,8 @@ size_t agb_cisd_factor_scratch_bytes(const agb_cisd_plan* P, int64_t naux) {
 agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* P, const void* Bf, int64_t naux, void* scratch,
                                         size_t scratch_bytes, int precision, void* stream) {
   AGB_ARG_CHECK(P && P->ws && Bf && naux > 0, "blocks_from_factors: bad argument");
-  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_DF64,
-                "blocks_from_factors: precision must be AGB_PREC_FP64 or AGB_PREC_DF64");
+  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_DF64 || precision == AGB_PREC_OZAKI,
+                "blocks_from_factors: precision must be AGB_PREC_FP64, AGB_PREC_DF64 or AGB_PREC_OZAKI");
   if (!scratch || scratch_bytes < agb_cisd_factor_scratch_bytes(P, naux)) {
     agb_set_error_message("blocks_from_factors: scratch too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;
@@ -814,7 +829,11 @@ agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* P, const void* Bf, int64_
     const z64* A = sub[c0 == 'v'][c1 == 'v'];
     const z64* B = sub[c2 == 'v'][c3 == 'v'];
     int64_t M = rlen(P, c0) * rlen(P, c1), N = rlen(P, c2) * rlen(P, c3);
-    if (precision == AGB_PREC_DF64)
+    if (precision == AGB_PREC_OZAKI && ozgemm_tiles(M, N) >= kOzMinTiles &&
+        ozgemm_scratch_bytes(M, N, naux) <= P->gemm_scratch_bytes)
+      return ozgemm_ex(M, N, naux, zmk(1, 0), A, naux, 1, 0, B, 1, naux, 0, zmk(0, 0), out, N, P->gemm_scratch,
+                       P->gemm_scratch_bytes, st);
+    if (precision == AGB_PREC_DF64 || precision == AGB_PREC_OZAKI)
       return dfgemm_ex(M, N, naux, zmk(1, 0), A, naux, 1, 0, B, 1, naux, 0, zmk(0, 0), out, N,
                        (char*)P->gemm_scratch + 256, P->gemm_scratch_bytes - 256, st);
     return zgemm_ex(M, N, naux, zmk(1, 0), A, naux, 1, 0, B, 1, naux, 0, zmk(0, 0), out, N,
@@ -844,9 +863,11 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
                              void* stream) {
   AGB_ARG_CHECK(P && P->ws && tv && rv, "residual: bad argument");
   AGB_ARG_CHECK(!P->mp2_only, "residual: plan created with AGB_PLAN_MP2");
-  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || prec == AGB_PREC_TF32X3 || prec == AGB_PREC_DF64,
+  AGB_ARG_CHECK(prec == AGB_PREC_FP64 || prec == AGB_PREC_TF32X3 || prec == AGB_PREC_DF64 ||
+                    prec == AGB_PREC_OZAKI,
                 "residual: unknown precision");
-  AGB_ARG_CHECK(prec != AGB_PREC_TF32X3 || P->mixed, "residual: plan created without AGB_PLAN_MIXED");
+  AGB_ARG_CHECK((prec != AGB_PREC_TF32X3 && prec != AGB_PREC_OZAKI) || P->mixed,
+                "residual: plan created without AGB_PLAN_MIXED");
   cudaStream_t st = (cudaStream_t)stream;
   const int o = P->o, v = P->v;
   const int64_t ov = P->ov, po = P->po, pv = P->pv, n1 = P->n1;

@@ -1,0 +1,492 @@
+// FP64-accurate complex GEMM on the bf16 tensor cores (Ozaki splitting).
+//
+// Each FP64 row x_r (a row of A, or a column of B) is scaled by 2^-(E_r+1), E_r the
+// largest binary exponent in the row, and rounded to a 42-bit fixed-point
+// integer X (|x - 2^(E_r+1-42) X| <= 2^(E_r-42)).  X is cut into six balanced
+// 7-bit digits, X = sum_s d_s 2^(35-7s) with |d_0| <= 128 and |d_s| <= 64, and
+// slice s stores b_s = d_s 2^-7s in bf16 (exact: at most 8 significant bits),
+// so x = 2^f_r sum_s b_s with f_r = E_r + 1 - 7 and
+//     x_i . y_j = 2^(f_i + f_j) sum_{s,t} b_s c_t .
+// The 21 slice pairs with s + t <= 5 are multiplied by tcgen05.mma kind::f16
+// (bf16 in, FP32 accumulate); the dropped pairs and the rounding leave
+// ~2^-41 of |x_i||y_j| per term.  The sum of group g = s + t is a multiple of
+// 2^-7g bounded by 2^14 (g = 0, 1), 2^14 + 2^12 (g = 2) and 2^14 + 2^13 (g = 3)
+// units per k, so groups 0..3 are EXACT in FP32 over 512 k (< 2^24 units): they
+// accumulate in their own TMEM columns over one 512-k chunk, the epilogue drains
+// them into int64 registers (exact) and the next chunk restarts them.  Groups
+// 4 and 5 (scale <= 2^-28) share a fifth accumulator over the whole K.  The
+// tensor core accumulates in FP32 with truncation (round toward zero), so only
+// this small tail may round: group 3 kept in the tail gave 8x the error.
+//
+// Complex operands use three real products (3M): P1 = Re.Re, P2 = Im.Im,
+// P3 = (Re+Im).(Re+Im); C = alpha (P1 - P2 + i (P3 - P1 - P2)) + beta C, each
+// product's epilogue adding alpha * (1 - i, -1 - i, i)[part] * P into C.
+//
+// Tiles: one CTA per 128x96 output tile (five 96-column accumulators fill 480 of
+// TMEM's 512 columns), 2-stage TMA pipeline of 6 A (128 x 32 bf16) and 6 B
+// (96 x 32 bf16) slice tiles, 64-byte swizzle, 84 KB per stage; warp 0 loads,
+// warp 1 issues the MMAs from one thread, warps 2-9 drain TMEM (two warps per
+// lane quadrant, 48 columns each).  Every mbarrier wait is bounded; a timeout
+// records an error word at the start of the scratch and the kernel returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "common.cuh"
+#include "tc05.cuh"
+
+namespace agb {
+
+namespace {
+using namespace tc05;
+
+constexpr int OZ_S = 6;                             // slices per operand
+constexpr int BM = 128, BN = 96, BK = 32;           // BK in bf16 elements (64 bytes)
+constexpr int NACC = 5;                             // exact groups 0..3, tail
+constexpr int CHUNK_KB = 16;                        // k-blocks per exact chunk (512 k)
+constexpr int STAGES = 2;
+constexpr int A_TILE_BYTES = BM * BK * 2;           // 8 KB per A slice tile
+constexpr int B_TILE_BYTES = BN * BK * 2;           // 6 KB per B slice tile
+constexpr int STAGE_BYTES = OZ_S * (A_TILE_BYTES + B_TILE_BYTES);   // 84 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 320;
+constexpr unsigned TMEM_COLS = 512;                 // G0 | G1 | G2 | G3 | tail, 96 columns each
+constexpr int EPI_COLS = BN / 2;                    // columns per epilogue warp
+constexpr int kGroupM = 12;
+
+// Instruction descriptor: D = F32, A = B = BF16 (kind::f16), K-major both, N = 96, M = 128.
+__host__ __device__ constexpr uint32_t make_idesc_bf16() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+struct OzParams {
+  int64_t M, N;
+  int nkb;                   // k-blocks of BK
+  const int* fA;             // per-row scale exponents f_r
+  const int* fB;
+  z64* C;                    // complex output [M][ldc]
+  int64_t ldc;
+  z64 coef;                  // C = (use_beta ? beta C : C) + coef * P  (first part: C = coef * P without beta)
+  z64 beta;
+  int mode;                  // 0: overwrite, 1: beta C + coef P, 2: C + coef P
+  int* err;
+  int64_t rowsA, rowsB;      // padded rows per slice plane
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, OzParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty_bar = full_bar + STAGES;
+  uint64_t* chunk_bar = empty_bar + STAGES;   // MMA -> epilogue: the chunk's MMAs completed
+  uint64_t* drained_bar = chunk_bar + 1;      // epilogue -> MMA: exact accumulators read (8 warps)
+  uint32_t* tmem_slot = (uint32_t*)(drained_bar + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntn = gridDim.x, ntm = gridDim.y;
+  const int lin = blockIdx.y * ntn + blockIdx.x;
+  const int gsz = kGroupM * ntn;
+  const int first_m = (lin / gsz) * kGroupM;
+  const int gm = min(ntm - first_m, kGroupM);
+  const int tile_m = first_m + (lin % gsz) % gm;
+  const int tile_n = (lin % gsz) / gm;
+  const int nk = p.nkb;
+  const int nchunks = (nk + CHUNK_KB - 1) / CHUNK_KB;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(chunk_bar, 1);
+    mbar_init(drained_bar, 8);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+        const int kx = kb * BK;
+        for (int sl = 0; sl < OZ_S; ++sl) {
+          tma_load_2d(st + sl * A_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(sl * p.rowsA + tile_m * BM));
+          tma_load_2d(st + OZ_S * A_TILE_BYTES + sl * B_TILE_BYTES, &mapB, &full_bar[s], kx,
+                      (int)(sl * p.rowsB + tile_n * BN));
+        }
+        issued = kb + 1;
+      }
+      if (*abort_flag) {
+        for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb) {
+          long long t0 = clock64();
+          while (!mbar_try_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u) &&
+                 clock64() - t0 < kWaitCycles) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = make_idesc_bf16();
+      for (int kb = 0; kb < nk; ++kb) {
+        const int kc = kb % CHUNK_KB, chunk = kb / CHUNK_KB;
+        if (kc == 0 && chunk > 0) {
+          // the epilogue must have read the previous chunk's exact accumulators
+          if (!mbar_wait(drained_bar, (uint32_t)(chunk - 1) & 1u, p.err, abort_flag, 4)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        const int s = kb % STAGES;
+        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 16; ++ks) {
+#pragma unroll
+          for (int sa = 0; sa < OZ_S; ++sa) {
+#pragma unroll
+            for (int tb = 0; tb + sa < OZ_S; ++tb) {
+              const int g = sa + tb;
+              const int d = g < NACC - 1 ? g : NACC - 1;
+              const uint64_t a = make_desc(st + sa * A_TILE_BYTES + ks * 32);
+              const uint64_t b = make_desc(st + OZ_S * A_TILE_BYTES + tb * B_TILE_BYTES + ks * 32);
+              // first write of an exact group in a chunk, or of the tail in the whole K, overwrites
+              const bool first =
+                  sa == 0 && ks == 0 && ((g < NACC - 1 && kc == 0) || (g == NACC - 1 && kb == 0));
+              mma_bf16(tmem_base + (uint32_t)(d * BN), a, b, idesc, first ? 0u : 1u);
+            }
+          }
+        }
+        mma_commit(&empty_bar[s]);
+        if (kc == CHUNK_KB - 1 || kb == nk - 1) mma_commit(chunk_bar);
+      }
+    }
+  } else {
+    // epilogue: warps 2..9; TMEM lane quadrant q = warp % 4, column half h
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * EPI_COLS);
+    long long acc[EPI_COLS];   // sum of the exact groups in units of 2^-21
+#pragma unroll
+    for (int j = 0; j < EPI_COLS; ++j) acc[j] = 0;
+    bool ok = nk > 0;
+    for (int c = 0; c < nchunks && ok; ++c) {
+      int okw = 0;
+      if (lane == 0) okw = mbar_wait(chunk_bar, (uint32_t)c & 1u, p.err, abort_flag, 3) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c4 = 0; c4 < EPI_COLS / 16; ++c4) {
+        float g0[16], g1[16], g2[16], g3[16];
+        tmem_ld16(lane_base + c4 * 16, g0);
+        tmem_ld16(lane_base + BN + c4 * 16, g1);
+        tmem_ld16(lane_base + 2 * BN + c4 * 16, g2);
+        tmem_ld16(lane_base + 3 * BN + c4 * 16, g3);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long long i0 = __float2int_rn(g0[j]);
+          const long long i1 = __float2int_rn(g1[j] * 128.0f);
+          const long long i2 = __float2int_rn(g2[j] * 16384.0f);
+          const long long i3 = __float2int_rn(g3[j] * 2097152.0f);
+          acc[c4 * 16 + j] += (i0 << 21) + (i1 << 14) + (i2 << 7) + i3;
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(drained_bar);
+    }
+    if (ok) {
+      const int64_t m = (int64_t)tile_m * BM + q * 32 + lane;
+      const int64_t n0 = (int64_t)tile_n * BN + h * EPI_COLS;
+      const int fa = m < p.M ? p.fA[m] : 0;
+#pragma unroll
+      for (int c4 = 0; c4 < EPI_COLS / 16; ++c4) {
+        float tl[16];
+        tmem_ld16(lane_base + (NACC - 1) * BN + c4 * 16, tl);
+        if (m < p.M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int64_t n = n0 + c4 * 16 + j;
+            if (n < p.N) {
+              // 2^(fa + fb) as a double built from its exponent field
+              const double sc = __longlong_as_double((long long)(fa + p.fB[n] + 1023) << 52);
+              const double v = ((double)acc[c4 * 16 + j] * 4.76837158203125e-07 + (double)tl[j]) * sc;   // I 2^-21 + tail
+              z64* c = p.C + m * p.ldc + n;
+              z64 out = zmk(p.coef.x * v, p.coef.y * v);
+              if (p.mode == 1) out = zadd(out, zmul(p.beta, *c));
+              else if (p.mode == 2) out = zadd(out, *c);
+              *c = out;
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS));
+  }
+}
+
+// Value of part `part` (0 Re, 1 Im, 2 Re + Im) of X(r, k) = src[r*s_row + k*s_k]; conj == 1 negates Im,
+// conj == kSrcReal reads a real array.
+__device__ __forceinline__ double oz_part(const z64* src, int64_t off, int conj, int part) {
+  if (conj == kSrcReal) return part == 1 ? 0.0 : ((const double*)src)[off];
+  const z64 v = src[off];
+  const double im = conj == 1 ? -v.y : v.y;
+  return part == 0 ? v.x : (part == 1 ? im : v.x + im);
+}
+
+// Largest biased FP64 exponent per row (emax must start at zero).
+__global__ void oz_rowexp_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
+                                 int conj, int part, int* __restrict__ emax) {
+  __shared__ int tile[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
+  const int64_t tiles_k = (K + 31) / 32, tiles = ((rows + 31) / 32) * tiles_k;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_k) * 32, k0 = (t % tiles_k) * 32;
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r, k;
+      if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
+      int e = 0;
+      if (r < rows && k < K) e = (__double2hiint(oz_part(src, r * s_row + k * s_k, conj, part)) >> 20) & 0x7ff;
+      if (kfast) tile[i][tx] = e; else tile[tx][i] = e;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+      int e = tile[i][tx];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+      if (tx == 0 && r0 + i < rows && e > 0) atomicMax(&emax[r0 + i], e);
+    }
+    __syncthreads();
+  }
+}
+
+// bf16 bits of d * 2^-7s (exact: |d| <= 128).
+__device__ __forceinline__ uint16_t oz_digit_bf16(long long d, float scale) {
+  const float f = __fsub_rn(__int_as_float(0x4B400000 + (int)d), 12582912.0f);   // exactly d
+  return (uint16_t)(__float_as_uint(__fmul_rn(f, scale)) >> 16);
+}
+
+// Slices [OZ_S][rows_pad][Kp] (bf16, K-major, zero padded) and row scale exponents f_r.
+__global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
+                                int conj, int part, int64_t rows_pad, int64_t Kp, const int* __restrict__ emax,
+                                int* __restrict__ fexp, uint16_t* __restrict__ slices) {
+  __shared__ double tile[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
+  const int64_t tiles_k = Kp / 32, tiles = (rows_pad / 32) * tiles_k;
+  const int64_t plane = rows_pad * Kp;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_k) * 32, k0 = (t % tiles_k) * 32;
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r, k;
+      if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
+      double v = 0.0;
+      if (r < rows && k < K) v = oz_part(src, r * s_row + k * s_k, conj, part);
+      if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+      const int64_t r = r0 + i, k = k0 + tx;
+      const int eb = r < rows ? emax[r] : 0;
+      if (k0 == 0 && tx == 0 && r < rows_pad) fexp[r] = eb > 0 ? eb - 1023 + 1 - 7 : 0;
+      const double v = tile[i][tx];
+      const uint32_t hw = (uint32_t)__double2hiint(v), lw = (uint32_t)__double2loint(v);
+      const int ex = (int)((hw >> 20) & 0x7ffu);
+      long long X = 0;
+      const int shift = 11 + (eb - ex);
+      if (ex > 0 && eb > 0 && shift < 64) {
+        const unsigned long long M = ((unsigned long long)(hw & 0xfffffu) << 32 | lw) | (1ull << 52);
+        X = (long long)((M + (1ull << (shift - 1))) >> shift);   // nearest (|X| <= 2^42 keeps |d_0| <= 128)
+        if (hw >> 31) X = -X;
+      }
+      // balanced base-2^7 digits of X (|X| < 2^42)
+      long long d[OZ_S];
+#pragma unroll
+      for (int s = 0; s < OZ_S - 1; ++s) {
+        const int sh = 35 - 7 * s;
+        d[s] = (X + (1ll << (sh - 1))) >> sh;
+        X -= d[s] << sh;
+      }
+      d[OZ_S - 1] = X;
+      const int64_t off = r * Kp + k;
+      float sc = 1.0f;
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) {
+        slices[s * plane + off] = oz_digit_bf16(d[s], sc);
+        sc *= 0.0078125f;   // 2^-7
+      }
+    }
+    __syncthreads();
+  }
+}
+
+int64_t rup(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+bool encode_slices(CUtensorMap* map, uint16_t* base, int64_t rows_total, int64_t Kp, int box_rows) {
+  auto enc = tma_encode_fn();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
+  cuuint64_t strides[1] = {(cuuint64_t)(Kp * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1u, 1u};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+struct OzLayout {
+  int64_t Mp, Np, Kp;
+  size_t sA, sB, eA, eB, fA, fB, total;   // byte offsets from the scratch base
+};
+
+OzLayout oz_layout(int64_t M, int64_t N, int64_t K) {
+  OzLayout L;
+  L.Mp = rup(M, BM);
+  L.Np = rup(N, BN);
+  L.Kp = rup(K, BK);
+  size_t off = 256;   // status word
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  L.sA = take((size_t)OZ_S * L.Mp * L.Kp * 2);
+  L.sB = take((size_t)OZ_S * L.Np * L.Kp * 2);
+  L.eA = take((size_t)L.Mp * 4);
+  L.eB = take((size_t)L.Np * 4);
+  L.fA = take((size_t)L.Mp * 4);
+  L.fB = take((size_t)L.Np * 4);
+  L.total = off;
+  return L;
+}
+
+}  // namespace
+
+// Output tiles of the Ozaki GEMM (the dispatcher sends GEMMs with fewer than a wave
+// of tiles to the double-float kernel, which splits K).
+int64_t ozgemm_tiles(int64_t M, int64_t N) { return (rup(M, BM) / BM) * (rup(N, BN) / BN); }
+
+size_t ozgemm_scratch_bytes(int64_t M, int64_t N, int64_t K) {
+  if (M <= 0 || N <= 0 || K <= 0) return 256;
+  return oz_layout(M, N, K).total;
+}
+
+// C = alpha op(A) op(B) + beta C to ~1e-12 of sum |a||b| on the bf16 tensor cores.
+// scratch: ozgemm_scratch_bytes(M, N, K), 256-byte aligned; its first int is the
+// kernel's error word (read by agb_scratch_status).
+agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                     void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  AGB_ARG_CHECK(M >= 0 && N >= 0 && K >= 0, "ozgemm: negative size");
+  if (M == 0 || N == 0) return AGB_OK;
+  AGB_ARG_CHECK(K > 0, "ozgemm: K must be positive");
+  AGB_ARG_CHECK(A && B && C && scratch, "ozgemm: null pointer");
+  AGB_ARG_CHECK(((uintptr_t)scratch & 255) == 0, "ozgemm: scratch must be 256-byte aligned");
+  const OzLayout L = oz_layout(M, N, K);
+  if (scratch_bytes < L.total) {
+    agb_set_error_message("ozgemm: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  AGB_ARG_CHECK(L.Mp / BM <= 65535, "ozgemm: M too large for the grid");
+  AGB_ARG_CHECK(OZ_S * L.Mp < (1ll << 31) && OZ_S * L.Np < (1ll << 31), "ozgemm: too many rows for a tensor map");
+  char* base = (char*)scratch;
+  uint16_t* sA = (uint16_t*)(base + L.sA);
+  uint16_t* sB = (uint16_t*)(base + L.sB);
+  int* eA = (int*)(base + L.eA);
+  int* eB = (int*)(base + L.eB);
+  int* fA = (int*)(base + L.fA);
+  int* fB = (int*)(base + L.fB);
+  CUtensorMap mA, mB;
+  if (!encode_slices(&mA, sA, OZ_S * L.Mp, L.Kp, BM) || !encode_slices(&mB, sB, OZ_S * L.Np, L.Kp, BN)) {
+    agb_set_error_message("ozgemm: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
+    return AGB_ERR_CUDA;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    AGB_CUDA_TRY(cudaFuncSetAttribute(ozgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_set = true;
+  }
+  auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int part, int64_t rows_pad,
+                   int* emax, int* fexp, uint16_t* dst) -> agb_status {
+    AGB_CUDA_TRY(cudaMemsetAsync(emax, 0, (size_t)rows_pad * 4, stream));
+    int64_t t1 = ((rows + 31) / 32) * ((K + 31) / 32);
+    oz_rowexp_kernel<<<(int)(t1 < 152 * 32 ? t1 : 152 * 32), 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part,
+                                                                                emax);
+    AGB_LAUNCH_CHECK();
+    int64_t t2 = (rows_pad / 32) * (L.Kp / 32);
+    oz_slice_kernel<<<(int)(t2 < 152 * 32 ? t2 : 152 * 32), 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part,
+                                                                              rows_pad, L.Kp, emax, fexp, dst);
+    AGB_LAUNCH_CHECK();
+    return AGB_OK;
+  };
+  OzParams p;
+  p.M = M; p.N = N; p.nkb = (int)(L.Kp / BK); p.fA = fA; p.fB = fB; p.C = C; p.ldc = ldc; p.beta = beta;
+  p.err = (int*)base; p.rowsA = L.Mp; p.rowsB = L.Np;
+  dim3 grid((unsigned)(L.Np / BN), (unsigned)(L.Mp / BM));
+  // 3M coefficients of P1 = Re.Re, P2 = Im.Im, P3 = (Re+Im).(Re+Im)
+  const z64 coef[3] = {zmk(1, -1), zmk(-1, -1), zmk(0, 1)};
+  const bool use_beta = beta.x != 0.0 || beta.y != 0.0;
+  for (int part = 0; part < 3; ++part) {
+    AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, part, L.Mp, eA, fA, sA));
+    AGB_STATUS_TRY(slice(B, N, sBn, sBk, conjB, part, L.Np, eB, fB, sB));
+    p.coef = zmul(alpha, coef[part]);
+    p.mode = part > 0 ? 2 : (use_beta ? 1 : 0);
+    ozgemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
+    AGB_LAUNCH_CHECK();
+  }
+  return AGB_OK;
+}
+
+}  // namespace agb
+
+extern "C" {
+
+size_t agb_zgemm_oz_scratch_bytes(int64_t M, int64_t N, int64_t K) { return agb::ozgemm_scratch_bytes(M, N, K); }
+
+agb_status agb_zgemm_oz(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
+                        int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn, int conjB,
+                        double beta_re, double beta_im, void* C, int64_t ldc, void* scratch, size_t scratch_bytes,
+                        void* stream) {
+  AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  return agb::ozgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
+                        (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, scratch,
+                        scratch_bytes, (cudaStream_t)stream);
+}
+
+}  // extern "C"

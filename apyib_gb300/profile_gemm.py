@@ -1,6 +1,6 @@
 """Run one complex GEMM of a given shape twice (for ncu).
 
-    python -m apyib_gb300.profile_gemm M N K [tf32x3|df64|fp64]
+    python -m apyib_gb300.profile_gemm M N K [tf32x3|df64|oz|fp64]
 
 A: [M,K] complex128 row-major, B: [N,K] (used transposed), random normal.
 """
@@ -27,20 +27,37 @@ def main(argv):
     elif kind == "df64":
         nb = _lib.load().agb_zgemm_df64_scratch_bytes(M, N, K)
         buf, sp, _ = workspace(nb)
-    for _ in range(2):
+    elif kind == "oz":
+        nb = _lib.load().agb_zgemm_oz_scratch_bytes(M, N, K)
+        buf, sp, _ = workspace(nb)
+        buf[:256].zero_()
+
+    def run():
         if kind == "tf32x3":
             _lib.call("agb_cgemm_tf32x3", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
                       ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
         elif kind == "df64":
             _lib.call("agb_zgemm_df64_ex", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
                       ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
+        elif kind == "oz":
+            _lib.call("agb_zgemm_oz", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
+                      ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
         else:
             _lib.call("agb_zgemm", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
                       stream_ptr())
-    if kind == "tf32x3":
+
+    for _ in range(2):
+        run()
+    if kind in ("tf32x3", "oz"):
         _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
     torch.cuda.synchronize()
-    print("ok", kind, M, N, K)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    print("ok", kind, M, N, K, f"{ms:.3f} ms", f"{8.0 * M * N * K / ms / 1e9:.1f} TFLOP/s (8MNK)")
 
 
 if __name__ == "__main__":

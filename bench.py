@@ -12,7 +12,8 @@ W = 8 * (o^2 v^4 / 2 + o^3 v^3 + o^4 v^2 / 2 + 5 o^2 v^3 + 5 o^3 v^2) flops
 (7.71e13 at 60/240), whatever the kernels actually execute.
 
 Also reported (measured once per run, outside the timed steps): the full
-mixed-precision solve (3xTF32 iterations, one FP64 base residual, defect
+mixed-precision solve (3xTF32 iterations, one FP64-accurate base residual with
+Ozaki-split bf16 tensor-core GEMMs, defect
 correction) to the reference's convergence test, the FP64 residual time, the
 FP64 residual norm at the mixed solution (a-posteriori check), and the
 reference-path CPU time (the NumPy oracle) on a bounded sample.
@@ -261,9 +262,10 @@ def main():
     t_setup = time.perf_counter()
     plan = CISDPlan(o, v, mixed=True)
     plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
-    # integral blocks from the factors with double-float GEMMs (~1e-13 relative; the FP64
-    # pipe would take ~5x longer); every solve below uses these same blocks
-    plan.blocks_from_factors(torch.as_tensor(prob.B), precision=_lib.PREC_DF64)
+    # integral blocks from the factors: the large products on the bf16 tensor cores with
+    # six-slice Ozaki splitting (~1e-12 of sum |a||b|), the rest in double-float; every
+    # solve below uses these same blocks
+    plan.blocks_from_factors(torch.as_tensor(prob.B), precision=_lib.PREC_OZAKI)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
     del prob
@@ -421,7 +423,7 @@ def main():
         eps3 = np.concatenate([np.repeat(prob3.eps_o, 2), np.repeat(prob3.eps_v, 2)])
         plan3 = CISDPlan(o3, v3, mixed=True)
         plan3.set_fock(torch.as_tensor(prob3.fock_so()), eps3)
-        plan3.blocks_from_factors(torch.as_tensor(prob3.B), precision=_lib.PREC_DF64)
+        plan3.blocks_from_factors(torch.as_tensor(prob3.B), precision=_lib.PREC_OZAKI)
         res3 = {}
         for prec in ("fp64", "mixed"):
             h3 = []

@@ -45,6 +45,8 @@ typedef int agb_status;
 #define AGB_PREC_FP64 0        /* FP64 CUDA-core arithmetic */
 #define AGB_PREC_TF32X3 1      /* complex FP32 via 3xTF32 tcgen05 MMAs, FP32 accumulate */
 #define AGB_PREC_DF64 2        /* double-float (2 x FP32, ~48-bit) GEMMs on the FP32 pipe, FP64 elsewhere */
+#define AGB_PREC_OZAKI 3       /* FP64-accurate GEMMs from six 7-bit bf16 slices per operand on the tcgen05
+                                  tensor cores (exact FP32 group sums drained into int64), FP64 elsewhere */
 
 /* Library version (major*10000 + minor*100 + patch). */
 int agb_version(void);
@@ -80,6 +82,20 @@ agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double alpha_re, d
                              const void* B, int64_t sBk, int64_t sBn, int conjB,
                              double beta_re, double beta_im, void* C, int64_t ldc,
                              void* scratch, size_t scratch_bytes, void* stream);
+/* C = alpha op(A) op(B) + beta C (agb_zgemm's contract) to ~1e-12 of sum |a||b|:
+ * each row of A and column of B is scaled by a power of two and cut into six
+ * 7-bit digits stored as bf16 slices; the 21 slice products that carry 42 bits
+ * run as tcgen05 kind::f16 MMAs whose low-order group sums stay exact in FP32
+ * over 512-long K chunks and are drained into int64; complex products use three
+ * real products.  scratch: agb_zgemm_oz_scratch_bytes(M, N, K), 256-byte aligned,
+ * its first word the kernel's error word (agb_scratch_status).  Exponents of
+ * A and B entries must stay within 2^+-500 of one another's row scales. */
+size_t agb_zgemm_oz_scratch_bytes(int64_t M, int64_t N, int64_t K);
+agb_status agb_zgemm_oz(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                        const void* A, int64_t sAm, int64_t sAk, int conjA,
+                        const void* B, int64_t sBk, int64_t sBn, int conjB,
+                        double beta_re, double beta_im, void* C, int64_t ldc,
+                        void* scratch, size_t scratch_bytes, void* stream);
 
 /* Same contraction computed as complex FP32 with 3xTF32 split products on the
  * tcgen05 tensor cores (FP32 accumulation in TMEM), FP64 in and out.
@@ -145,7 +161,9 @@ agb_status agb_cisd_set_fock(agb_cisd_plan* plan, const void* F_SO, const double
 agb_status agb_cisd_blocks_from_mo(agb_cisd_plan* plan, const void* ERI_MO, void* stream);
 agb_status agb_cisd_blocks_from_so(agb_cisd_plan* plan, const void* ERI_SO, void* stream);
 size_t agb_cisd_factor_scratch_bytes(const agb_cisd_plan* plan, int64_t naux);
-/* precision: AGB_PREC_FP64, or AGB_PREC_DF64 for the factor products in double-float. */
+/* precision: AGB_PREC_FP64, AGB_PREC_DF64 for the factor products in double-float,
+ * or AGB_PREC_OZAKI for them on the tensor cores (large products; the rest in
+ * double-float).  Status of the tensor-core products: agb_cisd_status. */
 agb_status agb_cisd_blocks_from_factors(agb_cisd_plan* plan, const void* Bf, int64_t naux,
                                         void* scratch, size_t scratch_bytes, int precision, void* stream);
 
