@@ -68,6 +68,15 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
       : "memory");
 }
 
+// tcgen05.ld of 16 columns without the wait (several loads, then one tcgen05.wait::ld).
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -169,7 +178,9 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
         const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
         if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        // descriptors of the stage's first A tile; the others differ only in the start-address
+        // field (byte offset / 16; no carry out of the 14-bit field within a 227 KB window)
+        const uint64_t d0 = make_desc(smem_u32(smem + s * STAGE_BYTES));
 #pragma unroll
         for (int ks = 0; ks < BK / 16; ++ks) {
 #pragma unroll
@@ -178,8 +189,8 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
             for (int tb = 0; tb + sa < OZ_S; ++tb) {
               const int g = sa + tb;
               const int d = g < NACC - 1 ? g : NACC - 1;
-              const uint64_t a = make_desc(st + sa * A_TILE_BYTES + ks * 32);
-              const uint64_t b = make_desc(st + OZ_S * A_TILE_BYTES + tb * B_TILE_BYTES + ks * 32);
+              const uint64_t a = d0 + (uint64_t)((sa * A_TILE_BYTES + ks * 32) >> 4);
+              const uint64_t b = d0 + (uint64_t)((OZ_S * A_TILE_BYTES + tb * B_TILE_BYTES + ks * 32) >> 4);
               // first write of an exact group in a chunk, or of the tail in the whole K, overwrites
               const bool first =
                   sa == 0 && ks == 0 && ((g < NACC - 1 && kc == 0) || (g == NACC - 1 && kb == 0));
@@ -207,17 +218,18 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int c4 = 0; c4 < EPI_COLS / 16; ++c4) {
-        float g0[16], g1[16], g2[16], g3[16];
-        tmem_ld16(lane_base + c4 * 16, g0);
-        tmem_ld16(lane_base + BN + c4 * 16, g1);
-        tmem_ld16(lane_base + 2 * BN + c4 * 16, g2);
-        tmem_ld16(lane_base + 3 * BN + c4 * 16, g3);
+        uint32_t g0[16], g1[16], g2[16], g3[16];
+        tmem_ld16_async(lane_base + c4 * 16, g0);
+        tmem_ld16_async(lane_base + BN + c4 * 16, g1);
+        tmem_ld16_async(lane_base + 2 * BN + c4 * 16, g2);
+        tmem_ld16_async(lane_base + 3 * BN + c4 * 16, g3);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const long long i0 = __float2int_rn(g0[j]);
-          const long long i1 = __float2int_rn(g1[j] * 128.0f);
-          const long long i2 = __float2int_rn(g2[j] * 16384.0f);
-          const long long i3 = __float2int_rn(g3[j] * 2097152.0f);
+          const long long i0 = __float2int_rn(__uint_as_float(g0[j]));
+          const long long i1 = __float2int_rn(__uint_as_float(g1[j]) * 128.0f);
+          const long long i2 = __float2int_rn(__uint_as_float(g2[j]) * 16384.0f);
+          const long long i3 = __float2int_rn(__uint_as_float(g3[j]) * 2097152.0f);
           acc[c4 * 16 + j] += (i0 << 21) + (i1 << 14) + (i2 << 7) + i3;
         }
       }
