@@ -13,6 +13,7 @@
 #include <atomic>
 
 #include "cisd_plan.h"
+#include "dfloat.cuh"
 
 namespace agb {
 
@@ -24,6 +25,8 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
 agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
                  cudaStream_t stream);
+agb_status zgemv_df(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
+                    cudaStream_t stream);
 agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
                         int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                         void* scratch, size_t scratch_bytes, cudaStream_t stream);
@@ -429,23 +432,45 @@ struct DotArgs {
   int ny;
 };
 
+// First index >= lo of the grid-stride sequence k0, k0 + stride, ...
+__device__ __forceinline__ int64_t stride_start(int64_t k0, int64_t stride, int64_t lo) {
+  return k0 >= lo ? k0 : k0 + (lo - k0 + stride - 1) / stride * stride;
+}
+
+// Weighted Gram row: out_j = w(k) sum_k conj(y_j[k]) x[k], w = w1 on the t1 part (k < n1), w2 on t2.
+// Products and running sums in double-float on the FP32 pipe (~2^-44 relative; GB300's FP64
+// pipe would bound this HBM stream), per-thread totals in FP64, fixed reduction order.
 template <int NY>
 __global__ void __launch_bounds__(256) dots_kernel(DotArgs A, z64* partial) {
   z64 acc[NY];
 #pragma unroll
   for (int j = 0; j < NY; ++j) acc[j] = zmk(0, 0);
-  int64_t n = A.n1 + A.n2;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    z64 x = A.x[k];
-    double w = k < A.n1 ? A.w1 : A.w2;
+  const int64_t n = A.n1 + A.n2, stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int part = 0; part < 2; ++part) {
+    float s[NY][4];
+#pragma unroll
+    for (int j = 0; j < NY; ++j) s[j][0] = s[j][1] = s[j][2] = s[j][3] = 0.f;
+    const int64_t hi = part ? n : A.n1;
+    for (int64_t k = stride_start(k0, stride, part ? A.n1 : 0); k < hi; k += stride) {
+      const float4 x = split_z_fast(A.x[k]);
+#pragma unroll
+      for (int j = 0; j < NY; ++j) {
+        if (j < A.ny) {
+          const float4 y = split_z_fast(A.ys[j][k]);
+          // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
+          df_mac(s[j][0], s[j][1], y.x, y.y, x.x, x.y);
+          df_mac(s[j][0], s[j][1], y.z, y.w, x.z, x.w);
+          df_mac(s[j][2], s[j][3], y.x, y.y, x.z, x.w);
+          df_mac(s[j][2], s[j][3], -y.z, -y.w, x.x, x.y);
+        }
+      }
+    }
+    const double w = part ? A.w2 : A.w1;
 #pragma unroll
     for (int j = 0; j < NY; ++j) {
-      if (j < A.ny) {
-        z64 y = A.ys[j][k];
-        // conj(y) * x
-        acc[j].x += w * (y.x * x.x + y.y * x.y);
-        acc[j].y += w * (y.x * x.y - y.y * x.x);
-      }
+      acc[j].x += w * df_to_double(s[j][0], s[j][1]);
+      acc[j].y += w * df_to_double(s[j][2], s[j][3]);
     }
   }
   block_reduce_store<NY>(acc, partial);
@@ -461,6 +486,9 @@ struct CombArgs {
   const z64* ew;   // energy weights [F_ov | <ij||ab>_p]
 };
 
+// t_new = sum_j c_j y_j (FP64: the convergence test compares successive iterates, so the
+// combination must not add noise above FP64's), E = sum t_new ew, s1 = sum_{t1} (t_old - t_new)^2
+// and s2 = 4 sum_{t2} (t_old - t_new)^2 (apyib/utils.py:138, ci_wfn.py:355,361-365).
 __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) {
   z64 acc[3] = {zmk(0, 0), zmk(0, 0), zmk(0, 0)};  // E, s1, s2
   int64_t n = A.n1 + A.n2;
@@ -895,8 +923,10 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     AGB_LAUNCH_CHECK();
     AGB_STATUS_TRY(gemm(P, prec, o, v, o, zmk(-1, 0), P->Foo, 1, o, t1, v, 1, one, r1, v, st));
     AGB_STATUS_TRY(gemm(P, prec, o, v, v, one, t1, v, 1, P->Fvv, 1, v, one, r1, v, st));
-    AGB_STATUS_TRY(zgemv(ov, ov, one, P->VT, ov, t1, one, r1, st));
-    AGB_STATUS_TRY(zgemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
+    // FP64 mode keeps the FP64 pipe; the other modes take the double-float GEMV (~2^-44)
+    auto gemv = prec == AGB_PREC_FP64 ? zgemv : zgemv_df;
+    AGB_STATUS_TRY(gemv(ov, ov, one, P->VT, ov, t1, one, r1, st));
+    AGB_STATUS_TRY(gemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
     AGB_STATUS_TRY(gemm(P, prec, o, v, (int64_t)o * pv, one, P->t2h, (int64_t)o * pv, 1, P->WvovvH, 1,
                         (int64_t)o * pv, one, r1, v, st, nullptr, P->P_Wvovv));
     AGB_STATUS_TRY(gemm(P, prec, o, v, po * v, one, P->WooovP, po * v, 1, P->t2q, v, 1, one, r1, v, st, P->P_Wooov));

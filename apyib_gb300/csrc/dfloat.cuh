@@ -39,4 +39,32 @@ __device__ __forceinline__ void df_add(float& s, float& c, float bs, float bc) {
   s = t;
 }
 
+// Streamed complex value as (re_hi, re_lo, im_hi, im_lo) with the cheap split (~2^-46 relative).
+__device__ __forceinline__ float4 split_z_fast(z64 v) {
+  float4 r;
+  split_f32pair_fast(v.x, r.x, r.y);
+  split_f32pair_fast(v.y, r.z, r.w);
+  return r;
+}
+
+// Exact double of a float, integer pipe only (FP32 subnormals give zero).
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint64_t s = (uint64_t)(u >> 31) << 63;
+  if (e == 0) return __longlong_as_double((long long)s);
+  return __longlong_as_double((long long)(s | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29)));
+}
+
+// hi + lo as a double (one FP64 add).
+__device__ __forceinline__ double df_to_double(float hi, float lo) { return f2d_exact(hi) + f2d_exact(lo); }
+
+// Renormalise a float pair so that |lo| <= ulp(hi)/2 (two-sum of its parts).
+__device__ __forceinline__ void df_norm(float& s, float& c) {
+  const float t = __fadd_rn(s, c);
+  const float z = __fsub_rn(t, s);
+  c = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(c, z));
+  s = t;
+}
+
 }  // namespace agb

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fsplit.cuh"
 #include "tc05.cuh"
 
@@ -220,6 +221,11 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
     if (ok && nk > 0) {
       const int64_t m = (int64_t)tile_m * BM + q * 32 + lane;
       const bool use_beta = (p.beta.x != 0.0 || p.beta.y != 0.0);
+      // FP32 -> FP64 by exponent rebias on the integer pipe, and no complex scaling in the
+      // common alpha = 1, beta in {0, 1} case: GB300's FP64 pipe would otherwise bound the
+      // epilogue of short-K GEMMs
+      const bool unit_alpha = p.alpha.x == 1.0 && p.alpha.y == 0.0;
+      const bool unit_beta = p.beta.x == 1.0 && p.beta.y == 0.0;
 #pragma unroll 1
       for (int c = 0; c < BN / 32; ++c) {
         float vr[32], vi[32];
@@ -232,14 +238,16 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
             z64* dst = p.partial + ((int64_t)split * p.M + m) * p.N + n0;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-              if (n0 + j < p.N) dst[j] = zmk((double)vr[j], (double)vi[j]);
+              if (n0 + j < p.N) dst[j] = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
           } else {
             z64* dst = p.C + m * p.ldc + n0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               if (n0 + j < p.N) {
-                z64 out = zmul(p.alpha, zmk((double)vr[j], (double)vi[j]));
-                if (use_beta) out = zadd(out, zmul(p.beta, dst[j]));
+                z64 out = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
+                if (!unit_alpha) out = zmul(p.alpha, out);
+                if (unit_beta) out = zadd(out, dst[j]);
+                else if (use_beta) out = zadd(out, zmul(p.beta, dst[j]));
                 dst[j] = out;
               }
             }

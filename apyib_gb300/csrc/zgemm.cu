@@ -5,6 +5,7 @@
 // thread, operands staged through shared memory with the load order chosen by
 // which operand stride is unit (coalesced either way).
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace agb {
 
@@ -211,12 +212,51 @@ __global__ void zgemv_kernel(int64_t M, int64_t K, z64 alpha, const z64* __restr
     }
   }
 }
+// y = alpha A x + beta y with the products and sums in double-float on the FP32 pipe
+// (~2^-44 relative): one warp per row, FP64 only for the per-row result.
+__global__ void zgemv_df_kernel(int64_t M, int64_t K, z64 alpha, const z64* __restrict__ A, int64_t lda,
+                                const z64* __restrict__ x, z64 beta, z64* y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t m = warp; m < M; m += nwarps) {
+    float re = 0.f, rec = 0.f, im = 0.f, imc = 0.f;
+    const z64* a = A + m * lda;
+    for (int64_t k = lane; k < K; k += 32) {
+      const float4 av = split_z_fast(a[k]);
+      const float4 xv = split_z_fast(x[k]);
+      // a x = (ar xr - ai xi) + i (ar xi + ai xr)
+      df_mac(re, rec, av.x, av.y, xv.x, xv.y);
+      df_mac(re, rec, -av.z, -av.w, xv.z, xv.w);
+      df_mac(im, imc, av.x, av.y, xv.z, xv.w);
+      df_mac(im, imc, av.z, av.w, xv.x, xv.y);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      df_add(re, rec, __shfl_xor_sync(0xffffffffu, re, off), __shfl_xor_sync(0xffffffffu, rec, off));
+      df_add(im, imc, __shfl_xor_sync(0xffffffffu, im, off), __shfl_xor_sync(0xffffffffu, imc, off));
+    }
+    if (lane == 0) {
+      z64 out = zmul(alpha, zmk(df_to_double(re, rec), df_to_double(im, imc)));
+      if (beta.x != 0.0 || beta.y != 0.0) out = zadd(out, zmul(beta, y[m]));
+      y[m] = out;
+    }
+  }
+}
 }  // namespace
 
 agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
                  cudaStream_t stream) {
   if (M == 0) return AGB_OK;
   zgemv_kernel<<<grid_for(M * 32, 256), 256, 0, stream>>>(M, K, alpha, A, lda, x, beta, y);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status zgemv_df(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
+                    cudaStream_t stream) {
+  if (M == 0) return AGB_OK;
+  zgemv_df_kernel<<<grid_for(M * 32, 256), 256, 0, stream>>>(M, K, alpha, A, lda, x, beta, y);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }

@@ -139,3 +139,26 @@ def test_df64_gemm_presplit_3m_accuracy(M, N, K):
     ref = A @ B
     err = np.abs(got - ref) / (np.abs(A) @ np.abs(B))
     assert err.max() < 1e-12, err.max()
+
+
+@pytest.mark.parametrize("ny,n1,n2,w1,w2", [(3, 50, 7000, 1.0, 4.0), (7, 0, 100000, 1.0, 4.0),
+                                            (12, 1234, 54321, 0.3, 2.5), (1, 9, 0, 2.0, 1.0)])
+def test_vec_dots_matches_numpy(ny, n1, n2, w1, w2):
+    """DIIS Gram row (double-float products and sums) against NumPy: ~1e-14 of sum |x||y|."""
+    rng = np.random.default_rng(ny + n1)
+    n = n1 + n2
+    x = crandn(rng, n)
+    ys = [crandn(rng, n) for _ in range(ny)]
+    xd = to_dev(x)
+    yd = [to_dev(y) for y in ys]
+    arr = (ctypes.c_void_p * ny)(*[y.data_ptr() for y in yd])
+    out = torch.zeros(16, dtype=torch.complex128, device="cuda")
+    nb = _lib.load().agb_vec_partials_bytes(ny)
+    buf, sp, _ = workspace(nb)
+    _lib.call("agb_vec_dots", n1, n2, w1, w2, ptr(xd), arr, ny, ptr(out), ctypes.c_void_p(sp), ctypes.c_size_t(nb),
+              stream_ptr())
+    got = out[:ny].cpu().numpy()
+    w = np.concatenate([np.full(n1, w1), np.full(n2, w2)])
+    ref = np.array([np.sum(w * y.conj() * x) for y in ys])
+    bound = np.array([np.sum(w * np.abs(y) * np.abs(x)) for y in ys])
+    assert np.all(np.abs(got - ref) <= 1e-13 * bound), np.abs(got - ref) / bound
