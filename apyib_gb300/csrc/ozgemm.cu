@@ -32,7 +32,6 @@
 #include <cudaTypedefs.h>
 
 #include "common.cuh"
-#include "dfloat.cuh"
 #include "tc05.cuh"
 
 namespace agb {
@@ -92,7 +91,6 @@ struct OzParams {
   z64 coef;                  // C = (use_beta ? beta C : C) + coef * P  (first part: C = coef * P without beta)
   z64 beta;
   int mode;                  // 0: overwrite, 1: beta C + coef P, 2: C + coef P
-  int unit_coef;             // coef components are -1, 0 or 1 (alpha = 1): sign changes, no products
   int* err;
   int64_t rowsA, rowsB;      // padded rows per slice plane
 };
@@ -252,27 +250,11 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
           for (int j = 0; j < 16; ++j) {
             const int64_t n = n0 + c4 * 16 + j;
             if (n < p.N) {
-              // I 2^-21 + tail, then times 2^(fa + fb) by an exponent add; FP64 conversions done on the
-              // integer pipe (|I| < 2^51: exact through the 1.5 * 2^52 offset; FP32 tail by rebias)
-              const long long I = acc[c4 * 16 + j];
-              const double dI = (I < (1ll << 51) && I > -(1ll << 51))
-                                    ? __longlong_as_double(I + 0x4338000000000000LL) - 6755399441055744.0
-                                    : (double)I;
-              double v = fma(dI, 4.76837158203125e-07, f2d_exact(tl[j]));
-              const long long vb = __double_as_longlong(v);
-              const long long eb = (vb >> 52) & 0x7ff;
-              const int sh = fa + p.fB[n];
-              v = (eb > 0 && eb + sh > 0 && eb + sh < 0x7ff) ? __longlong_as_double(vb + ((long long)sh << 52))
-                                                             : ldexp(v, sh);
+              // 2^(fa + fb) as a double built from its exponent field
+              const double sc = __longlong_as_double((long long)(fa + p.fB[n] + 1023) << 52);
+              const double v = ((double)acc[c4 * 16 + j] * 4.76837158203125e-07 + (double)tl[j]) * sc;   // I 2^-21 + tail
               z64* c = p.C + m * p.ldc + n;
-              z64 out;
-              if (p.unit_coef) {
-                const long long nb = __double_as_longlong(v) ^ (long long)0x8000000000000000ULL;
-                out.x = p.coef.x == 0.0 ? 0.0 : (p.coef.x > 0.0 ? v : __longlong_as_double(nb));
-                out.y = p.coef.y == 0.0 ? 0.0 : (p.coef.y > 0.0 ? v : __longlong_as_double(nb));
-              } else {
-                out = zmk(p.coef.x * v, p.coef.y * v);
-              }
+              z64 out = zmk(p.coef.x * v, p.coef.y * v);
               if (p.mode == 1) out = zadd(out, zmul(p.beta, *c));
               else if (p.mode == 2) out = zadd(out, *c);
               *c = out;
@@ -496,7 +478,6 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
     AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, part, L.Mp, eA, fA, sA));
     AGB_STATUS_TRY(slice(B, N, sBn, sBk, conjB, part, L.Np, eB, fB, sB));
     p.coef = zmul(alpha, coef[part]);
-    p.unit_coef = alpha.x == 1.0 && alpha.y == 0.0;
     p.mode = part > 0 ? 2 : (use_beta ? 1 : 0);
     ozgemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
     AGB_LAUNCH_CHECK();

@@ -13,6 +13,8 @@
  *
  * Reference cross-walk (apyib project paths):
  *   agb_zgemm / agb_cgemm_tf32x3   opt_einsum contractions of apyib/ci_wfn.py:309-334
+ *   agb_zgemm_df64 / agb_zgemm_oz  the same contractions at FP64 accuracy off the FP64 pipe
+ *                                  (double-float on the FP32 pipe; Ozaki-split bf16 tensor cores)
  *   agb_compute_f_so               apyib/utils.py:283-313 (compute_F_SO)
  *   agb_compute_eri_so             apyib/utils.py:317-365 (compute_ERI_SO)
  *   agb_cisd_blocks_*              the <pq||rs> block slices formed in apyib/ci_wfn.py:284,309-334
