@@ -277,11 +277,45 @@ struct AsmArgs {
 
 constexpr int TS = 32;  // (a,b) tile edge
 
+// Element arithmetic of the assembly: FP64 (z64), or FP32 (float2) for 3xTF32 residuals, whose
+// GEMM terms carry FP32-level error anyway (FP64 loads rounded to float on the integer pipe,
+// the result widened exactly).
+__device__ __forceinline__ float f64_to_f32(double x) {
+  float h, l;
+  split_f32pair_fast(x, h, l);
+  return __fadd_rn(h, l);
+}
+template <typename T> __device__ __forceinline__ T ldz(const z64* p);
+template <> __device__ __forceinline__ z64 ldz<z64>(const z64* p) { return *p; }
+template <> __device__ __forceinline__ float2 ldz<float2>(const z64* p) {
+  const z64 v = *p;
+  return make_float2(f64_to_f32(v.x), f64_to_f32(v.y));
+}
+template <typename T> __device__ __forceinline__ T cz(z64 v);
+template <> __device__ __forceinline__ z64 cz<z64>(z64 v) { return v; }
+template <> __device__ __forceinline__ float2 cz<float2>(z64 v) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ z64 tz(z64 v) { return v; }
+__device__ __forceinline__ z64 tz(float2 v) { return zmk(f2d_exact(v.x), f2d_exact(v.y)); }
+__device__ __forceinline__ z64 vadd(z64 a, z64 b) { return zadd(a, b); }
+__device__ __forceinline__ z64 vsub(z64 a, z64 b) { return zsub(a, b); }
+__device__ __forceinline__ z64 vneg(z64 a) { return zneg(a); }
+__device__ __forceinline__ z64 vmul(z64 a, z64 b) { return zmul(a, b); }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 vneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ T zzero();
+template <> __device__ __forceinline__ z64 zzero<z64>() { return zmk(0, 0); }
+template <> __device__ __forceinline__ float2 zzero<float2>() { return make_float2(0.f, 0.f); }
+
 // One CTA per (pair p(ij), upper-triangle tile of (a,b)).  Terms whose source
 // is indexed [b][a] are summed first along a (coalesced) into shared memory
 // and read transposed; the rest are read along b.
+template <typename T>
 __global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
-  __shared__ z64 tr[TS][TS + 1];
+  __shared__ T tr[TS][TS + 1];
   const int ntile = (A.v + TS - 1) / TS;
   // decode tile pair (ta <= tb) from blockIdx.x
   int tp = blockIdx.x, ta = 0;
@@ -297,13 +331,13 @@ __global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
   // Phase 1: transposed terms T[b][a] for b in tile tb, a in tile ta (coalesced along a).
   for (int rb = ty; rb < TS; rb += 8) {
     int b = b0 + rb, a = a0 + tx;
-    z64 s = zmk(0, 0);
+    T s = zzero<T>();
     if (a < v && b < v) {
       // -X[(i,b),(j,a)] + X[(j,b),(i,a)]
-      s = zneg(A.X[((int64_t)i * v + b) * A.ov + (int64_t)j * v + a]);
-      s = zadd(s, A.X[((int64_t)j * v + b) * A.ov + (int64_t)i * v + a]);
-      if (A.singles) s = zsub(s, A.Zq[p * vv + (int64_t)b * v + a]);      // -Zq[p][b][a]
-      if (!A.f_diag) s = zsub(s, A.Gq[p * vv + (int64_t)b * v + a]);      // -Gq[p][b][a]
+      s = vneg(ldz<T>(A.X + ((int64_t)i * v + b) * A.ov + (int64_t)j * v + a));
+      s = vadd(s, ldz<T>(A.X + ((int64_t)j * v + b) * A.ov + (int64_t)i * v + a));
+      if (A.singles) s = vsub(s, ldz<T>(A.Zq + p * vv + (int64_t)b * v + a));      // -Zq[p][b][a]
+      if (!A.f_diag) s = vsub(s, ldz<T>(A.Gq + p * vv + (int64_t)b * v + a));      // -Gq[p][b][a]
     }
     tr[rb][tx] = s;
   }
@@ -314,29 +348,29 @@ __global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
     if (a >= v || b >= v || b <= a) continue;
     int64_t q = pair_index(a, b, v);
     int64_t pq = p * A.pv + q;
-    z64 s = tr[tx][ra];
-    s = zadd(s, A.PQ[pq]);
-    s = zadd(s, A.X[((int64_t)i * v + a) * A.ov + (int64_t)j * v + b]);
-    s = zsub(s, A.X[((int64_t)j * v + a) * A.ov + (int64_t)i * v + b]);
+    T s = tr[tx][ra];
+    s = vadd(s, ldz<T>(A.PQ + pq));
+    s = vadd(s, ldz<T>(A.X + ((int64_t)i * v + a) * A.ov + (int64_t)j * v + b));
+    s = vsub(s, ldz<T>(A.X + ((int64_t)j * v + a) * A.ov + (int64_t)i * v + b));
     if (A.singles) {
-      s = zadd(s, A.Zq[p * vv + (int64_t)a * v + b]);
-      s = zadd(s, A.Yh[((int64_t)i * A.o + j) * A.pv + q]);
-      s = zsub(s, A.Yh[((int64_t)j * A.o + i) * A.pv + q]);
+      s = vadd(s, ldz<T>(A.Zq + p * vv + (int64_t)a * v + b));
+      s = vadd(s, ldz<T>(A.Yh + ((int64_t)i * A.o + j) * A.pv + q));
+      s = vsub(s, ldz<T>(A.Yh + ((int64_t)j * A.o + i) * A.pv + q));
     }
-    z64 t = A.t2p[pq];
+    T t = ldz<T>(A.t2p + pq);
     if (A.f_diag) {
       // sum_c F[b,c] t2[ijac] + F[a,c] t2[ijcb] - F[k,j] t2[ikab] - F[k,i] t2[kjab] with F diagonal
-      z64 fs = zadd(zadd(A.Fvv[(int64_t)a * v + a], A.Fvv[(int64_t)b * v + b]),
-                    zneg(zadd(A.Foo[(int64_t)i * A.o + i], A.Foo[(int64_t)j * A.o + j])));
-      s = zadd(s, zmul(fs, t));
+      const T fs = vsub(vadd(ldz<T>(A.Fvv + (int64_t)a * v + a), ldz<T>(A.Fvv + (int64_t)b * v + b)),
+                        vadd(ldz<T>(A.Foo + (int64_t)i * A.o + i), ldz<T>(A.Foo + (int64_t)j * A.o + j)));
+      s = vadd(s, vmul(fs, t));
     } else {
-      s = zadd(s, A.Gq[p * vv + (int64_t)a * v + b]);
-      s = zadd(s, A.H2h[((int64_t)j * A.o + i) * A.pv + q]);
-      s = zsub(s, A.H2h[((int64_t)i * A.o + j) * A.pv + q]);
+      s = vadd(s, ldz<T>(A.Gq + p * vv + (int64_t)a * v + b));
+      s = vadd(s, ldz<T>(A.H2h + ((int64_t)j * A.o + i) * A.pv + q));
+      s = vsub(s, ldz<T>(A.H2h + ((int64_t)i * A.o + j) * A.pv + q));
     }
-    if (A.use_const) s = zadd(s, A.R0p[pq]);
-    if (A.use_e) s = zsub(s, zmul(A.E, t));
-    A.r2p[pq] = s;
+    if (A.use_const) s = vadd(s, ldz<T>(A.R0p + pq));
+    if (A.use_e) s = vsub(s, vmul(cz<T>(A.E), t));
+    A.r2p[pq] = tz(s);
   }
 }
 
@@ -958,7 +992,8 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     A.singles = P->singles; A.f_diag = P->f_diag; A.r2p = r2p;
     int nt = (v + TS - 1) / TS;
     dim3 grid(nt * (nt + 1) / 2, (unsigned)po);
-    assemble_r2_kernel<<<grid, 256, 0, st>>>(A);
+    if (prec == AGB_PREC_TF32X3) assemble_r2_kernel<float2><<<grid, 256, 0, st>>>(A);
+    else assemble_r2_kernel<z64><<<grid, 256, 0, st>>>(A);
     AGB_LAUNCH_CHECK();
   }
   return AGB_OK;

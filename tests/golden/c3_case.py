@@ -1,4 +1,4 @@
-"""Inputs and probe layout of the o/v = 40/160 residual fixture (so_40_160_c3res.npz),
+"""Inputs and probe layout of the o/v = 40/160 residual fixture (c3res_40_160.npz),
 shared by its generator (make_golden_c3.py, which runs the reference) and the GPU test
 (which must not load the reference)."""
 import hashlib
@@ -7,7 +7,7 @@ import numpy as np
 
 O, V, SEED = 40, 160, 21
 NPROBE = 4096
-FIXTURE = f"so_{O}_{V}_c3res.npz"
+FIXTURE = f"c3res_{O}_{V}.npz"
 
 
 def digest(*arrs):

@@ -1,4 +1,4 @@
-"""Generate ``so_40_160_c3res.npz``: one CISD_SO iteration of the UNMODIFIED
+"""Generate ``c3res_40_160.npz``: one CISD_SO iteration of the UNMODIFIED
 reference (apyib/ci_wfn.py:263-337, loaded by ``ref_loader`` with a stub psi4)
 at o/v = 40/160 spin orbitals, nso = 200, naux = 800 — the residual-scale
 parity case at the size class of the o/v = 40/160 workload.
