@@ -514,28 +514,60 @@ struct CombArgs {
   int64_t n1, n2;
   const z64* ys[kMaxVec];
   double c[2 * kMaxVec];
+  z64 csum;        // sum_j c_j
   int ny;
   const z64* t_old;
   z64* t_new;
   const z64* ew;   // energy weights [F_ov | <ij||ab>_p]
 };
 
-// t_new = sum_j c_j y_j (FP64: the convergence test compares successive iterates, so the
-// combination must not add noise above FP64's), E = sum t_new ew, s1 = sum_{t1} (t_old - t_new)^2
-// and s2 = 4 sum_{t2} (t_old - t_new)^2 (apyib/utils.py:138, ci_wfn.py:355,361-365).
+// t_new = sum_j c_j y_j, E = sum t_new ew, s1 = sum_{t1} (t_old - t_new)^2 and
+// s2 = 4 sum_{t2} (t_old - t_new)^2 (apyib/utils.py:138, ci_wfn.py:355,361-365).
+// t_new = (sum_j c_j) y_0 + sum_{j>0} c_j (y_j - y_0): the first term and the differences in
+// FP64, the small difference sum in double-float (its error, ~2^-44 of sum |c_j| |y_j - y_0|,
+// vanishes as DIIS iterates converge), so t_new keeps FP64 accuracy where the convergence test
+// needs it; the squares in double-float from the FP64 differences, E in FP64.  t_old / t_new
+// and any y_j may alias: each element is read before it is written.
 __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) {
+  __shared__ float4 cs[kMaxVec];
+  if (threadIdx.x < A.ny) cs[threadIdx.x] = split_z(zmk(A.c[2 * threadIdx.x], A.c[2 * threadIdx.x + 1]));
+  __syncthreads();
   z64 acc[3] = {zmk(0, 0), zmk(0, 0), zmk(0, 0)};  // E, s1, s2
-  int64_t n = A.n1 + A.n2;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    z64 t = zmk(0, 0);
-    for (int j = 0; j < A.ny; ++j) zfma(t, zmk(A.c[2 * j], A.c[2 * j + 1]), A.ys[j][k]);
-    z64 old = A.t_old[k];
-    A.t_new[k] = t;
-    z64 dlt = zsub(old, t);
-    z64 d2 = zmul(dlt, dlt);
-    z64 e = zmul(t, A.ew[k]);
-    acc[0] = zadd(acc[0], e);
-    if (k < A.n1) acc[1] = zadd(acc[1], d2); else acc[2] = zadd(acc[2], d2);
+  const int64_t n = A.n1 + A.n2, stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int part = 0; part < 2; ++part) {
+    float q[4] = {0.f, 0.f, 0.f, 0.f};
+    const int64_t hi = part ? n : A.n1;
+    for (int64_t k = stride_start(k0, stride, part ? A.n1 : 0); k < hi; k += stride) {
+      const z64 y0 = A.ys[0][k];
+      z64 t = zmul(A.csum, y0);
+      if (A.ny > 1) {
+        float dr = 0.f, drc = 0.f, di = 0.f, dic = 0.f;
+        for (int j = 1; j < A.ny; ++j) {
+          const float4 d = split_z_fast(zsub(A.ys[j][k], y0));
+          const float4 c = cs[j];
+          // c d = (cr dr - ci di) + i (cr di + ci dr)
+          df_mac(dr, drc, c.x, c.y, d.x, d.y);
+          df_mac(dr, drc, -c.z, -c.w, d.z, d.w);
+          df_mac(di, dic, c.x, c.y, d.z, d.w);
+          df_mac(di, dic, c.z, c.w, d.x, d.y);
+        }
+        t.x += df_to_double(dr, drc);
+        t.y += df_to_double(di, dic);
+      }
+      const z64 old = A.t_old[k];
+      const z64 w = A.ew[k];
+      A.t_new[k] = t;
+      acc[0] = zadd(acc[0], zmul(t, w));
+      const float4 e = split_z_fast(zsub(old, t));
+      // (old - t)^2, unconjugated
+      df_mac(q[0], q[1], e.x, e.y, e.x, e.y);
+      df_mac(q[0], q[1], -e.z, -e.w, e.z, e.w);
+      df_mac(q[2], q[3], 2.f * e.x, 2.f * e.y, e.z, e.w);
+    }
+    const z64 qs = zmk(df_to_double(q[0], q[1]), df_to_double(q[2], q[3]));
+    if (part) acc[2] = zadd(acc[2], qs);
+    else acc[1] = zadd(acc[1], qs);
   }
   acc[2] = zscale(acc[2], 4.0);
   block_reduce_store<3>(acc, partial);
@@ -1125,6 +1157,8 @@ agb_status agb_cisd_combine(agb_cisd_plan* P, const void* const* ys, const doubl
     A.c[2 * j] = j < ny ? coefs[2 * j] : 0.0;
     A.c[2 * j + 1] = j < ny ? coefs[2 * j + 1] : 0.0;
   }
+  A.csum = zmk(0, 0);
+  for (int j = 0; j < ny; ++j) A.csum = zadd(A.csum, zmk(coefs[2 * j], coefs[2 * j + 1]));
   A.t_old = (const z64*)t_old; A.t_new = (z64*)t_new; A.ew = P->EW;
   combine_kernel<<<kRedBlocks, 256, 0, st>>>(A, (z64*)partials);
   AGB_LAUNCH_CHECK();
