@@ -263,3 +263,98 @@ class CISDEnergyCore(torch.autograd.Function):
 
 def cisd_energy_core(h_AO, wfn, params, precision="fp64"):
     return CISDEnergyCore.apply(h_AO, wfn, params, precision)
+
+
+# ---------------------------------------------------------------------------
+# Gradient with respect to the MO coefficients (orbital-response right-hand side)
+
+def _spin_summed(D, G, o, v):
+    """Spatial densities of the SO ones (alpha even, beta odd): E = sum_PQ F_MO[P,Q] D_sp[P,Q]
+    + sum_PQRS (PQ|RS)_MO Gc[P,Q,R,S], with (PR|QS) = <PQ|RS> for equal spins on P,R and Q,S."""
+    D_sp = D[0::2, 0::2] + D[1::2, 1::2]
+    Gd = gamma_full(G, o, v)
+    n = (o + v) // 2
+    Gc = torch.zeros((n, n, n, n), dtype=torch.complex128, device=Gd.device)
+    for s1 in (0, 1):
+        for s2 in (0, 1):
+            Gc += Gd[s1::2, s2::2, s1::2, s2::2].permute(0, 2, 1, 3)
+    return D_sp, Gc
+
+
+def _back(X, Cm, axis):
+    """Replace the MO index `axis` of X by an AO index: out[..m..] = sum_P Cm[m,P] X[..P..]."""
+    Xp = X.movedim(axis, 0)
+    rest = tuple(Xp.shape[1:])
+    out = zmm(Cm, Xp.reshape(Xp.shape[0], -1).contiguous())
+    return out.reshape((Cm.shape[0],) + rest).movedim(0, axis).contiguous()
+
+
+def _contract3(T, H, axis):
+    """X[a,P] = sum over the other three AO indices of T[...a...] H[...P...] (index `axis`)."""
+    Tm = T.movedim(axis, 0).reshape(T.shape[axis], -1).contiguous()
+    Hm = H.movedim(axis, 0).reshape(H.shape[axis], -1).contiguous()
+    return zmm(Tm, Hm, transB=True)
+
+
+def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64"):
+    """Wirtinger derivatives (E, dE/dC, dE/dC*) of the CISD_SO correlation energy with
+    respect to the MO coefficients C (nbf x nbf), at fixed AO integrals and fixed
+    orbital energies, with C entering through F_MO = C_t^H (h + G[C_fc C_fc^H] +
+    G[C_o C_o^H]) C_t and (PQ|RS) = sum C*_mP C_nQ C*_lR C_sS (mn|ls) (apyib/utils.py:
+    217-279).  A first-order change dC gives dE = sum(dE/dC * dC) + sum(dE/dC* * conj(dC)):
+    the right-hand side of an orbital-response (Z-vector) equation.  Uses the
+    Hellmann-Feynman densities of the converged amplitudes (apyib/ci_wfn.py:382-411)
+    and the 8-fold symmetry of the real AO integrals."""
+    from .linalg import jk_fock
+    from .utils import compute_ERI_MO, compute_F_SO, get_slices
+    C_list, _ = get_slices(params, wfn)
+    f, oc, _, t = C_list
+    C = to_dev(np.asarray(wfn.C))
+    ERI = to_dev(wfn.H.ERI, torch.float64)
+    h = h_AO.detach() if isinstance(h_AO, torch.Tensor) else to_dev(h_AO)
+    F_MO = _fock_mo(h, ERI, C, C_list, params["freeze_core"])
+    ERI_MO = compute_ERI_MO(params, wfn, C_list, return_torch=True)
+    eps = np.asarray(wfn.eps)
+    eps_o, eps_v = eps[C_list[1]], eps[C_list[2]]
+    o, v = 2 * len(eps_o), 2 * len(eps_v)
+    plan = CISDPlan(o, v, mixed=(precision == "mixed"))
+    plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True),
+                  np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)]))
+    plan.blocks_from_mo(ERI_MO)
+    E, tamp = solve(plan, params, precision=precision)
+    D, G = densities(plan, tamp)
+    D_sp, Gc = _spin_summed(D, G, o, v)
+    nbf = C.shape[0]
+    Ct = C[:, t].contiguous()
+    Ctc = Ct.conj().resolve_conj().contiguous()
+    # F_AO at C (h + G[D_fc] + G[D_occ])
+    hf = h
+    if params["freeze_core"]:
+        Cf = C[:, f].contiguous()
+        hf = jk_fock(ERI, zmm(Cf, Cf, transB=True, conjB=True), h, 1.0)
+    Co = C[:, oc].contiguous()
+    F_AO = jk_fock(ERI, zmm(Co, Co, transB=True, conjB=True), hf, 1.0)
+    dC = torch.zeros((nbf, nbf), dtype=torch.complex128, device=C.device)
+    dCc = torch.zeros_like(dC)
+    # through the MO transform of the Fock matrix
+    dC[:, t] += zmm(zmm(F_AO, Ctc, transA=True), D_sp)
+    dCc[:, t] += zmm(zmm(F_AO, Ct), D_sp, transB=True)
+    # through the occupied (and frozen-core) densities inside F_AO: W = dE/dD_AO
+    Y = zmm(zmm(Ctc, D_sp), Ct, transB=True)
+    W = jk_fock(ERI, Y, torch.zeros_like(Y), 1.0)
+    dC[:, oc] += zmm(W, Co.conj().resolve_conj())
+    dCc[:, oc] += zmm(W, Co, transA=True)
+    if params["freeze_core"]:
+        dC[:, f] += zmm(W, Cf.conj().resolve_conj())
+        dCc[:, f] += zmm(W, Cf, transA=True)
+    # through the four-index transform: one index left in MO, three back-transformed
+    T = ERI.to(torch.complex128)
+    H1 = _back(_back(_back(Gc, Ct, 1), Ctc, 2), Ct, 3)      # [P, n, l, s]
+    dCc[:, t] += _contract3(T, H1, 0)
+    H2 = _back(_back(_back(Gc, Ctc, 0), Ctc, 2), Ct, 3)     # [m, Q, l, s]
+    dC[:, t] += _contract3(T, H2, 1)
+    H3 = _back(_back(_back(Gc, Ctc, 0), Ct, 1), Ct, 3)      # [m, n, R, s]
+    dCc[:, t] += _contract3(T, H3, 2)
+    H4 = _back(_back(_back(Gc, Ctc, 0), Ct, 1), Ctc, 2)     # [m, n, l, S]
+    dC[:, t] += _contract3(T, H4, 3)
+    return complex(E), dC, dCc
