@@ -97,14 +97,26 @@ def test_nondiagonal_fock_solve_matches_oracle():
     assert np.abs(t2.cpu().numpy() - t2r).max() < 1e-9
 
 
-@pytest.mark.parametrize("base", ["df64", "fp64"])
-def test_mixed_precision_reaches_fp64_energy(base):
+@pytest.mark.parametrize("base,singles,offdiag", [("ozaki", True, False), ("df64", True, False),
+                                                   ("fp64", True, False), ("ozaki", False, False),
+                                                   ("ozaki", True, True)])
+def test_mixed_precision_reaches_fp64_energy(base, singles, offdiag):
+    """Mixed solves (3xTF32 iterations, defect correction around one FP64-accurate residual)
+    reach the FP64 solve for every base precision, for CID, and with a non-diagonal complex
+    Fock matrix (every Fock term of the residual active)."""
     from apyib_gb300.cisd import solve
     prob = synthetic.so_factors(20, 80, seed=7)
     F = prob.fock_so()
+    if offdiag:
+        n = F.shape[0]
+        rng = np.random.default_rng(8)
+        X = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * 0.01
+        mask = np.add.outer(np.arange(n) % 2, np.arange(n) % 2) % 2 == 0
+        F = F + (X + X.conj().T) * mask
     p = dict(P, e_convergence=1e-12, d_convergence=1e-10)
-    E64, _, t2_64 = solve_so_system(F, prob.eps_o, prob.eps_v, p, B=prob.B)
-    plan = CISDPlan(prob.o, prob.v, mixed=True)
+    res = solve_so_system(F, prob.eps_o, prob.eps_v, p, B=prob.B, singles=singles)
+    E64, t2_64 = res[0], res[-1]
+    plan = CISDPlan(prob.o, prob.v, singles=singles, mixed=True)
     eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
     plan.set_fock(torch.as_tensor(F), eps_so)
     plan.blocks_from_factors(torch.as_tensor(prob.B))
