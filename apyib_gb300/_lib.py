@@ -32,12 +32,25 @@ PLAN_MP2 = 4
 RES_CONST = 1
 RES_ETERM = 2
 
+OEI_OVERLAP, OEI_KINETIC, OEI_POTENTIAL, OEI_DIPOLE, OEI_NABLA, OEI_ANGMOM = range(6)
+AO_ROW_MAX = 16            # coefficients per row of agb_ao_transform_axis
+
 _c = ctypes
 _vp = _c.c_void_p
 _i64 = _c.c_int64
 _d = _c.c_double
 _int = _c.c_int
 _sz = _c.c_size_t
+
+
+
+class Basis(_c.Structure):
+    """agb_basis: a contracted Gaussian basis, every array a device pointer."""
+    _fields_ = [("natom", _int), ("nshell", _int), ("ncart", _int), ("lmax", _int),
+                ("atom_xyz", _vp), ("atom_charge", _vp), ("shell_l", _vp), ("shell_atom", _vp),
+                ("shell_nprim", _vp), ("shell_prim0", _vp), ("shell_cart0", _vp), ("bf_shell", _vp),
+                ("exps", _vp), ("coefs", _vp)]
+
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -88,6 +101,9 @@ SIGNATURES = {
     "agb_ao2mo": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _sz, _int, _vp]),
     "agb_jk_fock_scratch_bytes": (_sz, [_i64]),
     "agb_jk_fock": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
+    "agb_ao_one_electron": (_int, [_c.POINTER(Basis), _int, _c.POINTER(_d), _vp, _vp]),
+    "agb_ao_eri": (_int, [_c.POINTER(Basis), _vp, _vp]),
+    "agb_ao_transform_axis": (_int, [_vp, _i64, _int, _i64, _int, _vp, _vp, _vp, _vp, _vp]),
 }
 
 

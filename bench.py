@@ -323,15 +323,23 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    marks = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     e0.record()
-    for _ in range(args.steps):
+    for k in range(args.steps):
+        marks[k][0].record()
         state["t"].copy_(host_t, non_blocking=True)
+        marks[k][1].record()
         iteration()
+        marks[k][2].record()
         host_out.copy_(state["t"], non_blocking=True)
+        marks[k][3].record()
         host_t, host_out = host_out, host_t
     e1.record()
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist)
+    h2d_ms = float(np.mean([m[0].elapsed_time(m[1]) for m in marks]))
+    d2h_ms = float(np.mean([m[2].elapsed_time(m[3]) for m in marks]))
+    e2e_iter_ms = float(np.mean([m[1].elapsed_time(m[2]) for m in marks]))
     nbytes = plan.n * 16
 
     peaks, peak_kind = measured_peaks()
@@ -348,7 +356,10 @@ def main():
                    "o": o, "v": v, "naux": 4 * (o + v), "l2": "inputs > L2 (ERI blocks ~45 GB in HBM)",
                    "parallelism": f"replicas x{world}", "alg_flops_per_step": W},
         "e2e": {"value": aggregate_throughput(world, W, e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                # per-step phases on the stream: pinned host -> HBM copy, the iteration, HBM -> pinned host
+                "h2d_ms": h2d_ms, "iteration_ms": e2e_iter_ms, "d2h_ms": d2h_ms,
+                "h2d_GBps": nbytes / h2d_ms / 1e6, "d2h_GBps": nbytes / d2h_ms / 1e6},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
                      "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",

@@ -25,6 +25,8 @@
  *   agb_mp2_so                     apyib/mp2_wfn.py:82-85 (solve_MP2_SO)
  *   agb_ao2mo                      apyib/utils.py:274-277 (compute_ERI_MO)
  *   agb_jk_fock                    apyib/hf_wfn.py:81 and apyib/utils.py:241,249
+ *   agb_ao_one_electron / _eri     psi4 MintsHelper integrals of apyib/hamiltonian.py:32-55
+ *                                  (one-electron ones restated in apyib/integrals.py:9-146)
  */
 #ifndef APYIB_GB300_H
 #define APYIB_GB300_H
@@ -261,6 +263,57 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
 size_t agb_jk_fock_scratch_bytes(int64_t nbf);
 agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale,
                        void* F, void* scratch, size_t scratch_bytes, void* stream);
+
+/* ------------------------------------------------------ AO integrals -- */
+
+/* A contracted Gaussian basis on a molecule.  Every array is device memory.
+ * Cartesian functions of a shell of angular momentum l are ordered
+ * for i in 0..l, for j in 0..i: x^(l-i) y^(i-j) z^j, and coefs carry the
+ * primitive normalisation (apyib/integrals.py:107-119 reads psi4's shells the
+ * same way).  Shells have l <= 3 (lmax is checked). */
+typedef struct agb_basis {
+  int natom;
+  int nshell;
+  int ncart;                 /* Cartesian functions */
+  int lmax;                  /* largest shell angular momentum */
+  const double* atom_xyz;    /* [natom][3], bohr */
+  const double* atom_charge; /* [natom] nuclear charges */
+  const int* shell_l;        /* [nshell] */
+  const int* shell_atom;     /* [nshell] centre of each shell */
+  const int* shell_nprim;    /* [nshell] */
+  const int* shell_prim0;    /* [nshell] first primitive in exps / coefs */
+  const int* shell_cart0;    /* [nshell] first Cartesian function */
+  const int* bf_shell;       /* [ncart] shell of each Cartesian function */
+  const double* exps;        /* primitive exponents */
+  const double* coefs;       /* normalised contraction coefficients */
+} agb_basis;
+
+#define AGB_OEI_OVERLAP 0    /* S                       1 component  */
+#define AGB_OEI_KINETIC 1    /* -1/2 nabla^2            1 component  */
+#define AGB_OEI_POTENTIAL 2  /* -sum_C Z_C / |r - C|    1 component  */
+#define AGB_OEI_DIPOLE 3     /* -(r - O)                3 components (electron charge included) */
+#define AGB_OEI_NABLA 4      /* d/dr acting on the ket  3 components */
+#define AGB_OEI_ANGMOM 5     /* -(r - O) x nabla        3 components */
+
+/* One-electron integrals over the Cartesian functions, out[comp][ncart][ncart]
+ * (FP64).  origin (host, 3 doubles; NULL = 0) is the origin O of the dipole and
+ * angular-momentum operators.  psi4's MintsHelper ao_overlap / ao_kinetic /
+ * ao_potential / ao_dipole / ao_nabla / ao_angular_momentum
+ * (apyib/hamiltonian.py:32-55), restated by apyib/integrals.py:9-146. */
+agb_status agb_ao_one_electron(const agb_basis* basis, int kind, const double* origin, double* out,
+                               void* stream);
+
+/* Electron-repulsion integrals (mn|ls) over the Cartesian functions, chemist
+ * order, all ncart^4 values (FP64).  psi4's MintsHelper ao_eri
+ * (apyib/hamiltonian.py:34). */
+agb_status agb_ao_eri(const agb_basis* basis, double* out, void* stream);
+
+/* Basis change along one axis: out[a][s][b] = sum_k coef[s][k] in[a][cart0[s] + k][b]
+ * for a < pre, s < nout, k < len[s] (<= 16), b < post; in has nin functions on the
+ * axis.  Takes Cartesian functions to pure (solid-harmonic) ones. */
+agb_status agb_ao_transform_axis(const double* in, int64_t pre, int nin, int64_t post, int nout,
+                                 const int* cart0, const int* len, const double* coef, double* out,
+                                 void* stream);
 
 #ifdef __cplusplus
 }
