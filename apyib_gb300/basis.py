@@ -71,6 +71,22 @@ class Molecule(object):
     def nuclear_dipole(self):
         return (self.Z[:, None] * self.xyz).sum(axis=0)
 
+    def set_geometry(self, xyz):
+        """New Cartesian coordinates in bohr (psi4's Molecule.set_geometry)."""
+        xyz = np.asarray(getattr(xyz, "np", xyz), dtype=np.float64).reshape(-1, 3)
+        if xyz.shape[0] != self.natom():
+            raise ValueError("set_geometry: wrong number of atoms")
+        self.xyz = xyz.copy()
+
+    def create_psi4_string_from_molecule(self):
+        """A geometry string that parse_geometry reads back to the same molecule
+        (bohr, frame fixed; coordinates in full double precision)."""
+        lines = [f"{self.charge} {self.multiplicity}"]
+        for sym, r in zip(self.symbols, self.xyz):
+            lines.append(f"{sym.capitalize()} {float(r[0])!r} {float(r[1])!r} {float(r[2])!r}")
+        lines += ["units bohr", "no_com", "no_reorient", "symmetry c1"]
+        return "\n".join(lines) + "\n"
+
     def nuclear_repulsion_energy(self, dipole_field=(0.0, 0.0, 0.0)):
         """sum_{A<B} Z_A Z_B / R_AB + field . sum_A Z_A R_A (psi4's Molecule method,
         called by apyib/hamiltonian.py:58-61 with the negated electric field)."""
@@ -468,6 +484,22 @@ class BasisSet:
                 cart += sh.ncart
         b = cls(name, molecule, shells, pure, freeze_core)
         b._n, b._ncart = bf, cart
+        return b
+
+    def union(self, other):
+        """Both bases as one (self's functions first), on the atoms of both
+        molecules; the cross block of a union overlap is <self|other>."""
+        mol = Molecule(self.molecule.symbols + other.molecule.symbols,
+                       np.concatenate([self.molecule.Z, other.molecule.Z]),
+                       np.concatenate([self.molecule.xyz, other.molecule.xyz]))
+        if self.pure != other.pure:
+            raise ValueError("union of a pure and a Cartesian basis")
+        na = self.molecule.natom()
+        shells = [Shell(sh.l, sh.atom, sh.center, sh.exps, sh.coefs, sh.bf0, sh.cart0) for sh in self.shells]
+        shells += [Shell(sh.l, sh.atom + na, sh.center, sh.exps, sh.coefs, sh.bf0 + self._n, sh.cart0 + self._ncart)
+                   for sh in other.shells]
+        b = BasisSet(self.name, mol, shells, self.pure, self.freeze_core)
+        b._n, b._ncart = self._n + other._n, self._ncart + other._ncart
         return b
 
     def cart_to_ao(self):

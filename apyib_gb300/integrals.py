@@ -100,8 +100,15 @@ class MintsHelper(object):
         return [m[k] for k in range(3)] if return_torch else [_host(m[k]) for k in range(3)]
 
     # ------------------------------------------------------------------ psi4 names
-    def ao_overlap(self, return_torch=False):
-        return self._single(_lib.OEI_OVERLAP, return_torch)
+    def ao_overlap(self, bs1=None, bs2=None, return_torch=False):
+        """<bs1|bs2> (psi4's two-basis form); the basis of this helper when omitted."""
+        if bs1 is None and bs2 is None:
+            return self._single(_lib.OEI_OVERLAP, return_torch)
+        bs1 = self.basis if bs1 is None else bs1
+        bs2 = self.basis if bs2 is None else bs2
+        n1 = bs1.nbf()
+        m = MintsHelper(bs1.union(bs2))._oei(_lib.OEI_OVERLAP)[0][:n1, n1:].contiguous()
+        return m if return_torch else _host(m)
 
     def ao_kinetic(self, return_torch=False):
         return self._single(_lib.OEI_KINETIC, return_torch)

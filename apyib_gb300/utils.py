@@ -120,3 +120,33 @@ def solve_general_DIIS(parameters, res_vec, t_vec, e_iter, t_iter, iteration, mi
     cd = torch.as_tensor(c.reshape(-1, 1)).to(device())
     t_new = zmm(t_iter, cd).reshape(-1)
     return t_new, e_iter, t_iter
+
+
+def compute_mo_overlap(ndocc, nbf, bra_basis, bra_wfn, ket_basis, ket_wfn, return_torch=False):
+    """apyib/utils.py:370-388: <bra MO p | ket MO q> = C_bra^H S(bra, ket) C_ket, with
+    the AO overlap between two bases (two geometries) on the GPU."""
+    from .integrals import MintsHelper
+    if bra_basis is ket_basis:
+        S = MintsHelper(bra_basis).ao_overlap(return_torch=True)
+    else:
+        S = MintsHelper(bra_basis).ao_overlap(bra_basis, ket_basis, return_torch=True)
+    S = S.to(torch.complex128)
+    X = zmm(S, to_dev(ket_wfn))
+    out = zmm(to_dev(bra_wfn), X, transA=True, conjA=True)
+    return _ret(out, return_torch)
+
+
+def compute_so_overlap(nbf, mo_overlap, return_torch=False):
+    """apyib/utils.py:393-423: spin-orbital overlap, alpha even / beta odd, zero
+    between spins (the same spin integration as compute_F_SO)."""
+    return compute_F_SO(None, mo_overlap, return_torch)
+
+
+def compute_phase(ndocc, nbf, unperturbed_basis, unperturbed_wfn, ket_basis, ket_wfn):
+    """apyib/utils.py:427-446: divide each ket MO by the phase of its overlap with
+    the same unperturbed MO, phase = S_mm / sqrt(S_mm conj(S_mm))."""
+    S = compute_mo_overlap(ndocc, nbf, unperturbed_basis, unperturbed_wfn, ket_basis, ket_wfn)
+    d = np.diagonal(S)
+    N = np.sqrt(d * np.conjugate(d))
+    phase = d / N
+    return np.asarray(ket_wfn) * (phase ** -1)[None, :]
