@@ -1,0 +1,312 @@
+"""Finite-difference atomic axial tensors from wavefunction overlaps
+(apyib/aats.py:19-1067), with the determinant sums turned into contractions.
+
+The reference evaluates every term <Phi_bra | Phi_ket> between reference,
+singly and doubly excited determinants of two wavefunctions as the
+determinant of the occupied block of their spin-orbital MO overlap S with rows
+and columns swapped (apyib/aats.py:120-131), one determinant per excitation
+pair: O(o^4 v^4) determinants for the doubles/doubles term.  Here, with
+A = S_oo, B = S_vo A^-1, C = A^-1 S_ov and G = S_vv - S_vo A^-1 S_ov (the Schur
+complement), the matrix determinant lemma gives for bra rows i_r -> a_r and
+ket columns k_s -> c_s
+
+    det S[bra, ket] = det(A) det | B[a_r, i_r']   -G[a_r, c_s'] |
+                                 | A^-1[k_s, i_r']  C[k_s, c_s'] |
+
+(at most 4x4), and summing it against antisymmetric amplitudes leaves a few
+GEMM-shaped contractions per term, O(o^2 v^2 (o + v)) in all.  With weights
+1 (singles) and 1/4 (doubles) per side, X1 = x.B, Y1 = y.C,
+X2 = x_ijab B_ai B_bj, Y2 = y_klcd C_kc C_ld, Yc_kc = y_klcd C_ld,
+Xb_jb = x_ijab B_ai and F(u) = A^-T u G^T:
+
+    00: 1         01: Y1        02: Y2/2       10: X1        20: X2/2
+    11: X1 Y1 + x.F(y)          12: X1 Y2/2 + x.F(Yc)
+    21: Xb.F(y) + X2 Y1/2       22: X2 Y2/4 + Xb.F(Yc) + (x.(A^-T A^-T G G) y)/4
+
+all times det(A).  The terms I_00 ... I_DS and their sum are then assembled
+exactly as apyib/aats.py:161-555 does, with the same normalisations
+(apyib/aats.py:134-158) and the same prefactor Im(I) / (4 h_R h_B).  MO
+overlaps between geometries/fields come from the GPU integral source
+(utils.compute_mo_overlap), the contractions run through the library's GEMM
+(``linalg.zmm``); det(A) and A^-1 (occupied x occupied) are formed on the host
+in FP64, as the SCF's small dense algebra is.
+
+Spatial-orbital AATs (apyib/aats.py:646-1067) are the same quantity: the
+closed-shell amplitudes are expanded to spin orbitals (alpha even, beta odd)
+and the spin-orbital terms evaluated.  Frozen core: excitations run over the
+active occupied orbitals; the determinants include the frozen ones.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .device import device, to_dev
+from .linalg import zmm
+from .utils import compute_mo_overlap, compute_so_overlap
+
+
+# ----------------------------------------------------------------------------- amplitudes
+def so_amplitudes(t1, t2, spatial):
+    """Spin-orbital (t1, t2) device tensors; spatial closed-shell amplitudes
+    t2[i,j,a,b] = t_{i alpha j beta}^{a alpha b beta} are expanded."""
+    t2 = None if t2 is None or np.isscalar(t2) else to_dev(t2)
+    t1 = None if t1 is None or np.isscalar(t1) else to_dev(t1)
+    if not spatial:
+        return t1, t2
+    o, _, v, _ = t2.shape
+    T2 = torch.zeros((2 * o, 2 * o, 2 * v, 2 * v), dtype=torch.complex128, device=device())
+    tba = t2.transpose(2, 3)                  # t[i,j,b,a]
+    T2[0::2, 1::2, 0::2, 1::2] = t2
+    T2[1::2, 0::2, 1::2, 0::2] = t2
+    T2[0::2, 1::2, 1::2, 0::2] = -tba
+    T2[1::2, 0::2, 0::2, 1::2] = -tba
+    T2[0::2, 0::2, 0::2, 0::2] = t2 - tba
+    T2[1::2, 1::2, 1::2, 1::2] = t2 - tba
+    T1 = None
+    if t1 is not None:
+        T1 = torch.zeros((2 * o, 2 * v), dtype=torch.complex128, device=device())
+        T1[0::2, 0::2] = t1
+        T1[1::2, 1::2] = t1
+    return T1, T2
+
+
+def _axis(T, M, ax):
+    """M applied along axis ``ax`` of T: out[.., p, ..] = sum_q M[p, q] T[.., q, ..]."""
+    Tm = T.movedim(ax, 0)
+    shp = Tm.shape
+    out = zmm(M.contiguous(), Tm.reshape(shp[0], -1).contiguous())
+    return out.reshape((M.shape[0],) + tuple(shp[1:])).movedim(0, ax)
+
+
+class _Factors:
+    """det(A), A^-1, B, C, G of one spin-orbital overlap, restricted to the active
+    occupied orbitals [f, o) for the excitation indices."""
+
+    def __init__(self, S, o, f):
+        S = to_dev(S)
+        A = S[:o, :o].cpu().numpy()
+        Ainv = np.linalg.inv(A)
+        self.det = complex(np.linalg.det(A))
+        Ai = torch.as_tensor(Ainv).to(device())
+        SOV = S[:o, o:].contiguous()
+        SVO = S[o:, :o].contiguous()
+        C = zmm(Ai, SOV)                                   # o x v
+        B = zmm(SVO, Ai)                                   # v x o
+        self.G = (S[o:, o:] - zmm(SVO, C)).contiguous()    # v x v
+        self.B = B[:, f:].contiguous()                     # v x o_act
+        self.C = C[f:, :].contiguous()                     # o_act x v
+        self.AiT = Ai[f:, f:].transpose(0, 1).contiguous()  # (A^-1)^T on active indices
+
+    def F(self, u):
+        """A^-T u G^T for u (o_act x v)."""
+        return zmm(zmm(self.AiT, u.contiguous()), self.G, transB=True)
+
+    def q(self, r, x, s, y):
+        """sum over bra excitations (rank r, amplitudes x) and ket excitations
+        (rank s, amplitudes y) of weight * <bra|ket>, weights 1 and 1/4."""
+        if r == 0 and s == 0:
+            return self.det
+        X1 = X2 = Y1 = Y2 = Xb = Yc = None
+        if r == 1:
+            X1 = torch.sum(x * self.B.transpose(0, 1))
+        elif r == 2:
+            Xb = _axis(x, self.B.transpose(0, 1), 2).diagonal(dim1=0, dim2=2).sum(-1)   # Xb[j, b] = sum_ia x_ijab B_ai
+            X2 = torch.sum(Xb * self.B.transpose(0, 1))
+        if s == 1:
+            Y1 = torch.sum(y * self.C)
+        elif s == 2:
+            Yc = _axis(y, self.C.transpose(0, 1), 1).diagonal(dim1=1, dim2=3).sum(-1)  # Yc[k, c] = sum_ld y_klcd C_ld
+            Y2 = torch.sum(Yc * self.C)
+        if r == 0:
+            val = Y1 if s == 1 else 0.5 * Y2
+        elif s == 0:
+            val = X1 if r == 1 else 0.5 * X2
+        elif r == 1 and s == 1:
+            val = X1 * Y1 + torch.sum(x * self.F(y))
+        elif r == 1 and s == 2:
+            val = 0.5 * X1 * Y2 + torch.sum(x * self.F(Yc))
+        elif r == 2 and s == 1:
+            val = torch.sum(Xb * self.F(y)) + 0.5 * X2 * Y1
+        else:
+            yt = _axis(_axis(y, self.AiT, 0), self.AiT, 1)
+            yt = _axis(_axis(yt, self.G, 2), self.G, 3)
+            val = 0.25 * X2 * Y2 + torch.sum(Xb * self.F(Yc)) + 0.25 * torch.sum(x * yt)
+        return self.det * complex(val.item())
+
+
+class AAT(object):
+    """apyib/aats.py:19-118 with the same arguments; overlaps on the GPU."""
+
+    def __init__(self, parameters, wfn, unperturbed_wfn, unperturbed_basis, unperturbed_T, nuc_pos_wfn, nuc_neg_wfn,
+                 nuc_pos_basis, nuc_neg_basis, nuc_pos_T, nuc_neg_T, mag_pos_wfn, mag_neg_wfn, mag_pos_basis,
+                 mag_neg_basis, mag_pos_T, mag_neg_T, nuc_pert_strength, mag_pert_strength):
+        self.parameters = parameters
+        self.nbf = wfn.nbf
+        self.ndocc = wfn.ndocc
+        self.nfzc = wfn.H.basis_set.n_frozen_core()
+        self.natom = wfn.H.molecule.natom()
+        nbf, no = self.nbf, self.ndocc
+
+        def so(bra_b, bra_c, ket_b, ket_c):
+            return compute_so_overlap(nbf, compute_mo_overlap(no, nbf, bra_b, bra_c, ket_b, ket_c, return_torch=True),
+                                      return_torch=True)
+        ub, uc = unperturbed_basis, unperturbed_wfn
+        n3 = 3 * self.natom
+        ov = {}
+        correlated = parameters["method"] != "RHF"
+        if correlated:
+            ov["uu"] = so(ub, uc, ub, uc)
+            for b in range(3):
+                ov["up", b] = so(ub, uc, mag_pos_basis[b], mag_pos_wfn[b])
+                ov["un", b] = so(ub, uc, mag_neg_basis[b], mag_neg_wfn[b])
+            for a in range(n3):
+                ov["pu", a] = so(nuc_pos_basis[a], nuc_pos_wfn[a], ub, uc)
+                ov["nu", a] = so(nuc_neg_basis[a], nuc_neg_wfn[a], ub, uc)
+        for a in range(n3):
+            for b in range(3):
+                ov["pp", a, b] = so(nuc_pos_basis[a], nuc_pos_wfn[a], mag_pos_basis[b], mag_pos_wfn[b])
+                ov["pn", a, b] = so(nuc_pos_basis[a], nuc_pos_wfn[a], mag_neg_basis[b], mag_neg_wfn[b])
+                ov["np", a, b] = so(nuc_neg_basis[a], nuc_neg_wfn[a], mag_pos_basis[b], mag_pos_wfn[b])
+                ov["nn", a, b] = so(nuc_neg_basis[a], nuc_neg_wfn[a], mag_neg_basis[b], mag_neg_wfn[b])
+        self._init_common(ov, unperturbed_T, nuc_pos_T, nuc_neg_T, mag_pos_T, mag_neg_T, nuc_pert_strength,
+                          mag_pert_strength)
+
+    @classmethod
+    def from_overlaps(cls, parameters, ndocc, nbf, nfzc, natom, overlaps, unperturbed_T, nuc_pos_T, nuc_neg_T,
+                      mag_pos_T, mag_neg_T, nuc_pert_strength, mag_pert_strength):
+        """Build from spin-orbital overlap matrices keyed 'uu', ('up', b), ('un', b),
+        ('pu', a), ('nu', a), ('pp', a, b), ('pn', a, b), ('np', a, b), ('nn', a, b)."""
+        self = cls.__new__(cls)
+        self.parameters = parameters
+        self.ndocc, self.nbf, self.nfzc, self.natom = ndocc, nbf, nfzc, natom
+        self._init_common(overlaps, unperturbed_T, nuc_pos_T, nuc_neg_T, mag_pos_T, mag_neg_T, nuc_pert_strength,
+                          mag_pert_strength)
+        return self
+
+    def _init_common(self, ov, uT, npT, nnT, mpT, mnT, h, b):
+        o, f = 2 * self.ndocc, 2 * self.nfzc
+        self._f = {k: _Factors(S, o, f) for k, S in ov.items()}
+        self.nuc_pert_strength, self.mag_pert_strength = h, b
+        method = self.parameters["method"]
+        self.spatial = method in ("MP2", "CID", "CISD")
+        self.singles = method in ("CISD", "CISD_SO")
+        self.doubles = method != "RHF"
+
+        def amps(T):
+            if not self.doubles:
+                return (1.0, None, None)
+            t1, t2 = so_amplitudes(T[1] if self.singles else None, T[2], self.spatial)
+            return (complex(T[0]), t1, t2)
+        self.uT = amps(uT)
+        self.npT = [amps(T) for T in npT] if self.doubles else None
+        self.nnT = [amps(T) for T in nnT] if self.doubles else None
+        self.mpT = [amps(T) for T in mpT] if self.doubles else None
+        self.mnT = [amps(T) for T in mnT] if self.doubles else None
+
+    # ------------------------------------------------------------------ normalisation
+    def _norm(self, T):
+        t0, t1, t2 = T
+        s = t0 ** 2
+        if t2 is not None:
+            s = s + 0.25 * complex(torch.sum(t2.conj() * t2).item())
+        if self.singles and t1 is not None:
+            s = s + complex(torch.sum(t1.conj() * t1).item())
+        return 1 / np.sqrt(s)
+
+    def compute_normalization(self, alpha, beta, normalization):
+        """apyib/aats.py:134-158 (and :653-672 for spatial amplitudes)."""
+        if self.parameters["method"] == "RHF" or normalization == "intermediate":
+            return 1, 1, 1, 1, 1
+        return (self._norm(self.uT), self._norm(self.npT[alpha]), self._norm(self.nnT[alpha]),
+                self._norm(self.mpT[beta]), self._norm(self.mnT[beta]))
+
+    # ------------------------------------------------------------------ terms
+    def _pref(self):
+        return 1 / (4 * self.nuc_pert_strength * self.mag_pert_strength)
+
+    def _four(self, alpha, beta, r, x, s, y, N):
+        """x, y against the pp, pn, np, nn overlaps with their normalisations."""
+        _, N_np, N_nn, N_mp, N_mn = N
+        f = self._f
+        return (f["pp", alpha, beta].q(r, x, s, y) * N_np * N_mp - f["pn", alpha, beta].q(r, x, s, y) * N_np * N_mn
+                - f["np", alpha, beta].q(r, x, s, y) * N_nn * N_mp + f["nn", alpha, beta].q(r, x, s, y) * N_nn * N_mn)
+
+    def _amp(self, alpha, beta, rank):
+        """(t, t*, dt/dH, dt/dR*) of the given excitation rank (1 or 2)."""
+        k = rank
+        t = self.uT[k]
+        return (t, t.conj(), self.mpT[beta][k] - self.mnT[beta][k], (self.npT[alpha][k] - self.nnT[alpha][k]).conj())
+
+    def _term(self, alpha, beta, r, s, normalization):
+        N = self.compute_normalization(alpha, beta, normalization)
+        Nu, N_np, N_nn, N_mp, N_mn = N
+        f = self._f
+        if r == 0 and s == 0:
+            I = self._four(alpha, beta, 0, None, 0, None, N)
+            return self._pref() * I.imag
+        I = 0
+        if r == 0:
+            t, _, tdH, _ = self._amp(alpha, beta, s)
+            I += f["pu", alpha].q(0, None, s, tdH) * N_np * Nu - f["nu", alpha].q(0, None, s, tdH) * N_nn * Nu
+            I += self._four(alpha, beta, 0, None, s, t, N)
+        elif s == 0:
+            _, tc, _, tdR = self._amp(alpha, beta, r)
+            I += f["up", beta].q(r, tdR, 0, None) * Nu * N_mp - f["un", beta].q(r, tdR, 0, None) * Nu * N_mn
+            I += self._four(alpha, beta, r, tc, 0, None, N)
+        else:
+            _, tc, _, tdR = self._amp(alpha, beta, r)
+            t, _, tdH, _ = self._amp(alpha, beta, s)
+            I += f["uu"].q(r, tdR, s, tdH) * Nu * Nu
+            I += f["up", beta].q(r, tdR, s, t) * Nu * N_mp - f["un", beta].q(r, tdR, s, t) * Nu * N_mn
+            I += f["pu", alpha].q(r, tc, s, tdH) * N_np * Nu - f["nu", alpha].q(r, tc, s, tdH) * N_nn * Nu
+            I += self._four(alpha, beta, r, tc, s, t, N)
+        return self._pref() * I.imag
+
+    def compute_SO_I_00(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 0, 0, normalization)
+
+    def compute_SO_I_0D(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 0, 2, normalization)
+
+    def compute_SO_I_D0(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 2, 0, normalization)
+
+    def compute_SO_I_DD(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 2, 2, normalization)
+
+    def compute_SO_I_0S(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 0, 1, normalization)
+
+    def compute_SO_I_S0(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 1, 0, normalization)
+
+    def compute_SO_I_SS(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 1, 1, normalization)
+
+    def compute_SO_I_SD(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 1, 2, normalization)
+
+    def compute_SO_I_DS(self, alpha, beta, normalization):
+        return self._term(alpha, beta, 2, 1, normalization)
+
+    def compute_SO_aats(self, alpha, beta, normalization="full"):
+        """apyib/aats.py:520-555: the sum of the terms the method has."""
+        terms = [(0, 0)]
+        if self.doubles:
+            terms += [(0, 2), (2, 0), (2, 2)]
+        if self.singles:
+            terms += [(0, 1), (1, 0), (1, 1), (1, 2), (2, 1)]
+        return sum(self._term(alpha, beta, r, s, normalization) for r, s in terms)
+
+    def compute_spatial_aats(self, alpha, beta, normalization="full"):
+        """apyib/aats.py:646-1067: the same tensor from closed-shell amplitudes."""
+        return self.compute_SO_aats(alpha, beta, normalization)
+
+    def compute_aat_tensor(self, normalization="full"):
+        """All 3N x 3 elements."""
+        out = np.zeros((3 * self.natom, 3))
+        for a in range(3 * self.natom):
+            for b in range(3):
+                out[a, b] = self.compute_SO_aats(a, b, normalization)
+        return out

@@ -19,12 +19,16 @@ Conventions (those of psi4's shell objects, as apyib/integrals.py:35-50 reads th
     m = 0, +1, -1, +2, -2, ..., each of unit norm, formed from the Cartesian
     functions above; a basis set is pure or Cartesian as a whole.
 
-The built-in data are the published contractions (STO-3G: Hehre, Stewart and
-Pople, J. Chem. Phys. 51, 2657 (1969); 6-31G: Hehre, Ditchfield and Pople,
+The built-in data are the published contractions (STO-3G and STO-6G: Hehre,
+Stewart and Pople, J. Chem. Phys. 51, 2657 (1969); 6-31G: Hehre, Ditchfield and Pople,
 J. Chem. Phys. 56, 2257 (1972), Ditchfield, Hehre and Pople, J. Chem. Phys. 54,
 724 (1971); 6-31G(d) polarisation exponent 0.8 on O: Hariharan and Pople,
 Theor. Chim. Acta 28, 213 (1973); cc-pVDZ: Dunning, J. Chem. Phys. 90, 1007 (1989))
-for the elements apyib's energy tests use.  Further sets are added at run time
+for the elements apyib's energy tests use.  The last three exponents of the
+oxygen STO-6G 2sp shell are from the same least-squares fit of the 2s and 2p
+Slater functions (shared exponents, zeta = 2.25) re-done in high precision; it
+reproduces the published first three exponents to 3e-8 and all twelve
+contraction coefficients.  Further sets are added at run time
 with ``register_basis(name, text)`` from Gaussian-94 formatted text, the
 format of psi4's basis library files.
 """
@@ -217,6 +221,37 @@ SP   3   1.00
 ****
 """)
 
+
+
+register_basis("sto-6g", """
+spherical
+****
+H     0
+S   6   1.00
+     35.52322122             0.00916359628
+      6.513143725            0.04936149294
+      1.822142904            0.16853830490
+      0.625955266            0.37056279970
+      0.243076747            0.41649152980
+      0.100112428            0.13033408410
+****
+O     0
+S   6   1.00
+   1355.584234               0.00916359628
+    248.5448855              0.04936149294
+     69.53390229             0.16853830490
+     23.88677211             0.37056279970
+      9.275932609            0.41649152980
+      3.820341298            0.13033408410
+SP   6   1.00
+     52.18776196            -0.01325278809           0.003759696623
+     10.32932006            -0.04699171014           0.03767936984
+      3.210344977           -0.03378537151           0.1738967435
+      1.235135423            0.2502417861            0.4180364347
+      0.5364201589           0.5951172526            0.4258595477
+      0.2458806068           0.2407061763            0.1017082955
+****
+""")
 
 
 _631G_D_O = """
