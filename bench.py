@@ -204,6 +204,80 @@ def ao_kernels(nbf, seed=0):
     return res
 
 
+H2O_GEOM = """
+O 0.0  0.0     0.1173
+H 0.0  0.7572 -0.4692
+H 0.0 -0.7572 -0.4692
+units angstrom
+no_com
+no_reorient
+symmetry c1
+"""
+
+
+def water_workloads():
+    """Water cc-pVDZ with a 1e-4 a.u. magnetic field along z (complex orbitals), from
+    the geometry string through the public API: the CISD_SO solve in FP64 and in
+    mixed precision, and the finite-difference AAT tensor (9 nuclear coordinates x
+    3 field components, steps 1e-4 bohr and 1e-5 a.u.: 24 displaced CISD solves,
+    the MO overlaps and the determinant-overlap terms as contractions).  Beside it,
+    the reference's determinant path for the same tensor: the number of o x o
+    determinants its loops evaluate (apyib/aats.py:161-555) times the rate of
+    batched 10 x 10 complex determinants measured here on the host (an estimate:
+    the path itself would run for months)."""
+    import torch
+
+    from apyib_gb300.aats import AAT
+    from apyib_gb300.energy import energy
+    from apyib_gb300.fin_diff import finite_difference
+    from apyib_gb300.hamiltonian import Hamiltonian
+    from apyib_gb300.hf_wfn import hf_wfn
+
+    p = dict(geom=H2O_GEOM, basis="cc-pVDZ", method="CISD_SO", e_convergence=1e-10, d_convergence=1e-10,
+             DIIS=True, max_iterations=120, freeze_core=False, F_el=[0.0, 0.0, 0.0], F_mag=[0.0, 0.0, 1e-4])
+    energy(dict(p, method="RHF"))                      # warm-up: library load, first kernels
+    res = {}
+    for prec in ("fp64", "mixed"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E_list, T_list, C, basis = energy(dict(p, precision=prec))
+        torch.cuda.synchronize()
+        res[prec] = (time.perf_counter() - t0, complex(E_list[1]))
+    out = {"cisd_fp64_s": res["fp64"][0], "cisd_mixed_s": res["mixed"][0],
+           "E_cisd": [res["fp64"][1].real, res["fp64"][1].imag],
+           "abs_dE_mixed_vs_fp64": abs(res["mixed"][1] - res["fp64"][1]),
+           "note": "nso = 48: launch-bound at this size; the solves include integrals and RHF"}
+    h, b = 1e-4, 1e-5
+    E_list, T_list, C, basis = energy(p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fd = finite_difference(p, basis, C)
+    inputs = fd.compute_AAT(h, b)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    A = AAT(p, hf_wfn(Hamiltonian(p)), C, basis, T_list, *inputs, h, b)
+    aat = A.compute_aat_tensor("full")
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    o, v = 10, 38
+    ov = o * v
+    dets_per_element = 4 + 2 * 6 * ov * ov + 9 * ov ** 4 + 2 * 9 * ov ** 3 + 9 * ov * ov + 2 * 6 * ov
+    rng = np.random.default_rng(0)
+    M = rng.standard_normal((20000, o, o)) + 1j * rng.standard_normal((20000, o, o))
+    np.linalg.det(M[:100])
+    c0 = time.perf_counter()
+    np.linalg.det(M)
+    rate = len(M) / (time.perf_counter() - c0)
+    out["aat_fd"] = {"total_s": t2 - t0, "displaced_solves": len(inputs[0]) * 2 + 6, "solves_s": t1 - t0,
+                     "overlaps_and_terms_s": t2 - t1, "elements": int(aat.size), "max_abs_element": float(
+                         np.abs(aat).max()),
+                     "reference_determinants": 27 * dets_per_element,
+                     "reference_estimate_s": 27 * dets_per_element / rate,
+                     "cpu_det_rate_per_s": rate, "cpu_cores": 1,
+                     "cpu_sample": "20000 batched 10x10 complex determinants (numpy), one host thread"}
+    return out
+
+
 def max_over_ranks(x, dist=None):
     """Max of a per-rank scalar over all ranks (identity without a process group)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
@@ -452,6 +526,7 @@ def main():
         del plan3
     if not args.no_solve and rank == 0:
         out["ao_kernels_nbf150"] = ao_kernels(150)
+        out["h2o_ccpvdz_bz"] = water_workloads()
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline_oracle()
     if rank == 0:
