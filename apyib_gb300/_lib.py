@@ -32,7 +32,7 @@ PLAN_MP2 = 4
 RES_CONST = 1
 RES_ETERM = 2
 
-OEI_OVERLAP, OEI_KINETIC, OEI_POTENTIAL, OEI_DIPOLE, OEI_NABLA, OEI_ANGMOM = range(6)
+OEI_OVERLAP, OEI_KINETIC, OEI_POTENTIAL, OEI_DIPOLE, OEI_NABLA, OEI_ANGMOM, OEI_OVERLAP_HALF = range(7)
 AO_ROW_MAX = 16            # coefficients per row of agb_ao_transform_axis
 
 _c = ctypes
@@ -103,6 +103,8 @@ SIGNATURES = {
     "agb_jk_fock": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
     "agb_ao_one_electron": (_int, [_c.POINTER(Basis), _int, _c.POINTER(_d), _vp, _vp]),
     "agb_ao_eri": (_int, [_c.POINTER(Basis), _vp, _vp]),
+    "agb_ao_one_electron_deriv": (_int, [_c.POINTER(Basis), _int, _vp, _vp]),
+    "agb_ao_eri_deriv": (_int, [_c.POINTER(Basis), _vp, _vp]),
     "agb_ao_transform_axis": (_int, [_vp, _i64, _int, _i64, _int, _vp, _vp, _vp, _vp, _vp]),
 }
 

@@ -125,6 +125,41 @@ class MintsHelper(object):
     def ao_angular_momentum(self, origin=None, return_torch=False):
         return self._triple(_lib.OEI_ANGMOM, origin, return_torch)
 
+    # ------------------------------------------------------------------ nuclear derivatives
+    def oei_deriv_all(self, kind):
+        """[natom, 3, nbf, nbf] device tensor of d(integral)/dR for OVERLAP, KINETIC,
+        POTENTIAL or OVERLAP_HALF (bra derivative only)."""
+        nc, na = self.basis.ncart(), self.basis.molecule.natom()
+        out = torch.empty((na, 3, nc, nc), dtype=torch.float64, device=device())
+        _lib.call("agb_ao_one_electron_deriv", ctypes.byref(self._c), kind, ptr(out), stream_ptr())
+        return self._to_ao(out, 2)
+
+    def eri_deriv_all(self):
+        """[natom, 3, nbf, nbf, nbf, nbf] device tensor of d(mn|ls)/dR."""
+        nc, na = self.basis.ncart(), self.basis.molecule.natom()
+        out = torch.empty((na, 3, nc, nc, nc, nc), dtype=torch.float64, device=device())
+        _lib.call("agb_ao_eri_deriv", ctypes.byref(self._c), ptr(out), stream_ptr())
+        return self._to_ao(out, 4)
+
+    _KINDS = {"OVERLAP": _lib.OEI_OVERLAP, "KINETIC": _lib.OEI_KINETIC, "POTENTIAL": _lib.OEI_POTENTIAL}
+
+    def ao_oei_deriv1(self, oei_type, atom, return_torch=False):
+        """psi4's ao_oei_deriv1: [d/dx, d/dy, d/dz] of OVERLAP / KINETIC / POTENTIAL for one atom."""
+        m = self.oei_deriv_all(self._KINDS[oei_type.upper()])[atom]
+        return [m[c] for c in range(3)] if return_torch else [_host(m[c]) for c in range(3)]
+
+    def ao_tei_deriv1(self, atom, return_torch=False):
+        """psi4's ao_tei_deriv1: [d/dx, d/dy, d/dz] of the ERIs for one atom."""
+        m = self.eri_deriv_all()[atom]
+        return [m[c] for c in range(3)] if return_torch else [_host(m[c]) for c in range(3)]
+
+    def ao_overlap_half_deriv1(self, side, atom, return_torch=False):
+        """psi4's ao_overlap_half_deriv1: <d mu/dR | nu> ('LEFT') or <mu | d nu/dR> ('RIGHT')."""
+        m = self.oei_deriv_all(_lib.OEI_OVERLAP_HALF)[atom]
+        if side.upper() == "RIGHT":
+            m = m.transpose(-1, -2).contiguous()
+        return [m[c] for c in range(3)] if return_torch else [_host(m[c]) for c in range(3)]
+
     def ao_eri(self, return_torch=False):
         nc = self.basis.ncart()
         out = torch.empty((nc, nc, nc, nc), dtype=torch.float64, device=device())

@@ -294,6 +294,8 @@ typedef struct agb_basis {
 #define AGB_OEI_DIPOLE 3     /* -(r - O)                3 components (electron charge included) */
 #define AGB_OEI_NABLA 4      /* d/dr acting on the ket  3 components */
 #define AGB_OEI_ANGMOM 5     /* -(r - O) x nabla        3 components */
+#define AGB_OEI_OVERLAP_HALF 6  /* <d mu / dR | nu>: derivative of the bra function only
+                                   (agb_ao_one_electron_deriv only) */
 
 /* One-electron integrals over the Cartesian functions, out[comp][ncart][ncart]
  * (FP64).  origin (host, 3 doubles; NULL = 0) is the origin O of the dipole and
@@ -307,6 +309,17 @@ agb_status agb_ao_one_electron(const agb_basis* basis, int kind, const double* o
  * order, all ncart^4 values (FP64).  psi4's MintsHelper ao_eri
  * (apyib/hamiltonian.py:34). */
 agb_status agb_ao_eri(const agb_basis* basis, double* out, void* stream);
+
+/* Nuclear first derivatives over the Cartesian functions, out[atom][x,y,z][ncart][ncart]
+ * (zeroed by the call) for kind AGB_OEI_OVERLAP, AGB_OEI_KINETIC, AGB_OEI_POTENTIAL
+ * (basis-function centres and the attracting nucleus both move) or
+ * AGB_OEI_OVERLAP_HALF.  psi4's MintsHelper ao_oei_deriv1 / ao_overlap_half_deriv1
+ * (apyib/analytic_aats.py:96-104). */
+agb_status agb_ao_one_electron_deriv(const agb_basis* basis, int kind, double* out, void* stream);
+
+/* Nuclear first derivatives of the ERIs, out[atom][x,y,z][ncart^4] (chemist order,
+ * zeroed by the call).  psi4's MintsHelper ao_tei_deriv1 (apyib/analytic_aats.py:100). */
+agb_status agb_ao_eri_deriv(const agb_basis* basis, double* out, void* stream);
 
 /* Basis change along one axis: out[a][s][b] = sum_k coef[s][k] in[a][cart0[s] + k][b]
  * for a < pre, s < nout, k < len[s] (<= 16), b < post; in has nin functions on the
