@@ -241,7 +241,7 @@ class CISDEnergyCore(torch.autograd.Function):
         eps = np.asarray(wfn.eps)
         eps_o, eps_v = eps[C_list[1]], eps[C_list[2]]
         o, v = 2 * len(eps_o), 2 * len(eps_v)
-        plan = CISDPlan(o, v, mixed=(precision == "mixed"))
+        plan = CISDPlan(o, v, singles=params["method"] in ("CISD", "CISD_SO"), mixed=(precision == "mixed"))
         eps_so = np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)])
         plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True), eps_so)
         plan.blocks_from_mo(ERI_MO)
@@ -296,7 +296,7 @@ def _contract3(T, H, axis):
     return zmm(Tm, Hm, transB=True)
 
 
-def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64"):
+def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64", return_intermediates=False):
     """Wirtinger derivatives (E, dE/dC, dE/dC*) of the CISD_SO correlation energy with
     respect to the MO coefficients C (nbf x nbf), at fixed AO integrals and fixed
     orbital energies, with C entering through F_MO = C_t^H (h + G[C_fc C_fc^H] +
@@ -317,7 +317,7 @@ def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64"):
     eps = np.asarray(wfn.eps)
     eps_o, eps_v = eps[C_list[1]], eps[C_list[2]]
     o, v = 2 * len(eps_o), 2 * len(eps_v)
-    plan = CISDPlan(o, v, mixed=(precision == "mixed"))
+    plan = CISDPlan(o, v, singles=params["method"] in ("CISD", "CISD_SO"), mixed=(precision == "mixed"))
     plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True),
                   np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)]))
     plan.blocks_from_mo(ERI_MO)
@@ -357,4 +357,8 @@ def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64"):
     dCc[:, t] += _contract3(T, H3, 2)
     H4 = _back(_back(_back(Gc, Ctc, 0), Ct, 1), Ctc, 2)     # [m, n, l, S]
     dC[:, t] += _contract3(T, H4, 3)
+    if return_intermediates:
+        # AO densities of the correlation energy at fixed orbitals: dE = sum Y dF_AO + sum G_AO d(mn|ls)
+        G_AO = _back(H4, Ct, 3)
+        return complex(E), dC, dCc, {"Y": Y, "G_AO": G_AO, "Co": Co, "Cf": Cf if params["freeze_core"] else None}
     return complex(E), dC, dCc

@@ -1,0 +1,150 @@
+"""Analytic nuclear gradients of the RHF, CID_SO and CISD_SO energies at zero field.
+
+The finite-difference route (fin_diff.compute_Nuclear_Gradient) needs 2 x 3N
+complete calculations; this one needs one: the SCF, the CI solve, its
+Hellmann-Feynman densities (adjoint.densities) and the derivative integrals
+(integrals.MintsHelper.oei_deriv_all / eri_deriv_all), plus the coupled-perturbed
+Hartree-Fock (CPHF) orbital response, as apyib/analytic_aats.py:84-88, 902-992
+organises its zero-field (real-orbital) derivatives:
+
+  dE/dR = dE_RHF/dR + dE_corr/dR
+  dE_RHF/dR = sum D h^R + sum D (J^R/2 - K^R/4)[D] - sum W S^R + dE_nuc/dR
+              (D = 2 C_o C_o^T, W = 2 C_o eps_o C_o^T)
+  dE_corr/dR = sum Y (h^R + G^R[C_o C_o^T]) + sum Gamma_AO (mn|ls)^R          (skeleton)
+             + sum (dE/dC + dE/dC*) C U^R                                        (orbital response)
+
+with Y, Gamma_AO the correlation densities in the AO basis and dE/dC the
+MO-coefficient gradient (adjoint.mo_coefficient_gradient), and U^R the orbital
+response: U_ai from the closed-shell CPHF equations
+  (eps_a - eps_i) U_ai + sum_bj [4(ai|bj) - (ab|ij) - (aj|ib)] U_bj
+      = -(F^R_ai - eps_i S^R_ai - sum_kl S^R_kl [2(ai|kl) - (ak|il)]),
+U_pq = -S^R_pq / 2 within the occupied and within the virtual space (the CI
+energy is invariant to those rotations when no orbital is frozen) and
+U_ia = -S^R_ia - U_ai.  The CPHF matrix (n_vir n_occ square) is solved on the
+host in FP64 for all 3N perturbations at once, like the SCF's small dense
+algebra; the integrals, transforms and contractions run on the GPU.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import to_dev
+from .integrals import MintsHelper
+from .linalg import jk_fock, zmm
+
+
+def _real_orbitals(C):
+    """Remove the arbitrary complex phase of each MO (zero field: the orbitals are real
+    up to a phase) and return real C."""
+    C = np.asarray(C)
+    k = np.argmax(np.abs(C), axis=0)
+    ph = C[k, np.arange(C.shape[1])]
+    Cr = C * (np.abs(ph) / ph)[None, :]
+    if np.abs(Cr.imag).max() > 1e-10:
+        raise ValueError("analytic gradients need real orbitals (zero field)")
+    return Cr.real.copy()
+
+
+def nuclear_repulsion_deriv1(mol):
+    """d E_nuc / dR (natom, 3) (psi4's Molecule.nuclear_repulsion_energy_deriv1)."""
+    R, Z = mol.xyz, mol.Z.astype(float)
+    g = np.zeros_like(R)
+    for a in range(len(Z)):
+        for b in range(len(Z)):
+            if a != b:
+                d = R[a] - R[b]
+                g[a] -= Z[a] * Z[b] * d / np.linalg.norm(d) ** 3
+    return g
+
+
+def nuclear_gradient(parameters, precision="fp64", return_parts=False):
+    """Analytic dE/dR (natom, 3) of parameters['method'] in RHF, CID_SO, CISD_SO (or the
+    spatial CID / CISD, the same energies) at zero electric and magnetic field."""
+    from .adjoint import mo_coefficient_gradient
+    from .hamiltonian import Hamiltonian
+    from .hf_wfn import hf_wfn
+
+    method = parameters["method"]
+    if method not in ("RHF", "CID", "CISD", "CID_SO", "CISD_SO"):
+        raise ValueError(f"analytic gradients exist for RHF, CID and CISD, not {method}")
+    if any(f != 0.0 for f in parameters["F_el"]) or any(f != 0.0 for f in parameters["F_mag"]):
+        raise ValueError("analytic gradients are implemented at zero field")
+    if method != "RHF" and parameters.get("freeze_core"):
+        raise ValueError("analytic correlated gradients are implemented without frozen core")
+    H = Hamiltonian(parameters)
+    wfn = hf_wfn(H)
+    E_scf, C = wfn.solve_SCF(parameters)
+    C = _real_orbitals(C)
+    wfn.C = C
+    nbf, no = wfn.nbf, wfn.ndocc
+    natom = H.molecule.natom()
+    eps = np.asarray(wfn.eps).real
+    m = MintsHelper(H.basis_set)
+    Sd = m.oei_deriv_all(_lib.OEI_OVERLAP)                       # [natom, 3, n, n]
+    hd = m.oei_deriv_all(_lib.OEI_KINETIC) + m.oei_deriv_all(_lib.OEI_POTENTIAL)
+    Gd = m.eri_deriv_all()                                       # [natom, 3, n, n, n, n]
+    Cd = to_dev(C, torch.float64)
+    Co = Cd[:, :no].contiguous()
+    Dh = (Co @ Co.T).contiguous()                                # C_o C_o^T
+    Wd = 2.0 * Co @ torch.diag(torch.as_tensor(eps[:no]).to(Co)) @ Co.T
+    Dc = (2.0 * Dh).to(torch.complex128)
+    zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=Co.device)
+    g_hf = np.zeros((natom, 3))
+    GR = {}
+    for K in range(natom):
+        for c in range(3):
+            GR[K, c] = Gd[K, c].contiguous()
+            two_e = jk_fock(GR[K, c], Dc, zero, 0.25).real
+            g_hf[K, c] = float(torch.sum(2.0 * Dh * hd[K, c]) + torch.sum(2.0 * Dh * two_e) - torch.sum(Wd * Sd[K, c]))
+    g_hf += nuclear_repulsion_deriv1(H.molecule)
+    if method == "RHF":
+        return (g_hf, {"E": complex(E_scf) + H.E_nuc}) if return_parts else g_hf
+
+    params = dict(parameters, method=method if method.endswith("_SO") else method + "_SO")
+    h_AO = torch.as_tensor(np.asarray(H.T) + np.asarray(H.V)).to(Co.device).to(torch.complex128)
+    E_corr, dEdC, dEdCc, inter = mo_coefficient_gradient(h_AO, wfn, params, precision=precision,
+                                                         return_intermediates=True)
+    Y, G_AO = inter["Y"], inter["G_AO"]
+    dEdC_r = (dEdC + dEdCc).real                                 # real orbitals, real responses
+    # CPHF with all-MO integrals (real)
+    from .utils import compute_ERI_MO
+    ERI = compute_ERI_MO(params, wfn, [slice(0, 0), slice(0, no), slice(no, nbf), slice(0, nbf)],
+                         return_torch=True).real.cpu().numpy()
+    o, v = slice(0, no), slice(no, nbf)
+    nv = nbf - no
+    # A[a,i,b,j] = 4(ai|bj) - (ab|ij) - (aj|ib)
+    A = (4.0 * ERI[v, o, v, o] - ERI[v, v, o, o].transpose(0, 2, 1, 3) - ERI[v, o, o, v].transpose(0, 2, 3, 1))
+    A = A.reshape(nv * no, nv * no)
+    A[np.diag_indices_from(A)] += (eps[no:][:, None] - eps[:no][None, :]).reshape(-1)
+    Ch = C
+    rhs, S_mo = [], {}
+    skel = np.zeros((natom, 3))
+    for K in range(natom):
+        for c in range(3):
+            dF_AO = hd[K, c].to(torch.complex128) + jk_fock(GR[K, c], Dh.to(torch.complex128), zero, 1.0)
+            skel[K, c] = float((torch.sum(Y * dF_AO) + torch.sum(G_AO * GR[K, c])).real)
+            F_mo = Ch.T @ dF_AO.real.cpu().numpy() @ Ch
+            S = Ch.T @ Sd[K, c].cpu().numpy() @ Ch
+            S_mo[K, c] = S
+            B = F_mo[v, o] - S[v, o] * eps[None, :no] \
+                - np.einsum("kl,aikl->ai", S[o, o], 2.0 * ERI[v, o, o, o] - ERI[v, o, o, o].transpose(0, 2, 1, 3))
+            rhs.append(-B.reshape(-1))
+    Uvo = np.linalg.solve(A, np.stack(rhs, axis=1))
+    orb = np.zeros((natom, 3))
+    n = 0
+    for K in range(natom):
+        for c in range(3):
+            S = S_mo[K, c]
+            U = -0.5 * S.copy()
+            U[v, o] = Uvo[:, n].reshape(nv, no)
+            U[o, v] = -S[o, v] - U[v, o].T
+            dC = zmm(Cd.to(torch.complex128), torch.as_tensor(U).to(Cd.device).to(torch.complex128)).real
+            orb[K, c] = float(torch.sum(dEdC_r * dC))
+            n += 1
+    g = g_hf + skel + orb
+    if return_parts:
+        return g, {"hf": g_hf, "skeleton": skel, "orbital": orb, "E_corr": E_corr,
+                   "E": complex(E_scf) + H.E_nuc + E_corr}
+    return g

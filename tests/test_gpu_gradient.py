@@ -1,0 +1,35 @@
+"""Analytic nuclear gradients (apyib_gb300.gradient: one SCF + one CI solve, the
+Hellmann-Feynman densities, derivative integrals and the CPHF orbital response)
+against central finite differences of complete GPU calculations
+(fin_diff.compute_Nuclear_Gradient at 1e-3 and 5e-4 bohr, Richardson-combined),
+for RHF, CID and CISD (spin-orbital and spatial) of water away from its
+equilibrium geometry, to 1e-6 relative."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from apyib_gb300.energy import energy  # noqa: E402
+from apyib_gb300.fin_diff import finite_difference  # noqa: E402
+from apyib_gb300.gradient import nuclear_gradient  # noqa: E402
+from tests.golden.reference_energies import H2O, PARAMS  # noqa: E402
+
+CASES = [("STO-3G", "RHF"), ("STO-3G", "CISD_SO"), ("STO-3G", "CID"), ("6-31G", "CISD"), ("cc-pVDZ", "RHF"),
+         ("cc-pVDZ", "CID_SO")]
+
+
+@pytest.mark.parametrize("basis,method", CASES, ids=[f"{b}-{m}" for b, m in CASES])
+def test_analytic_gradient_matches_finite_differences(basis, method):
+    p = dict(PARAMS, geom=H2O, basis=basis, method=method, freeze_core=False)
+    g, parts = nuclear_gradient(p, return_parts=True)
+    E_list, _, C, bs = energy(p)
+    E = complex(E_list[0]) + complex(E_list[1]) + E_list[2]
+    assert abs(parts["E"] - E) < 1e-10
+    fd = finite_difference(p, bs, C)
+    g1 = fd.compute_Nuclear_Gradient(1e-3)[0]
+    g2 = fd.compute_Nuclear_Gradient(5e-4)[0]
+    gfd = (4 * g2 - g1) / 3
+    err = np.abs(g - gfd).max()
+    assert err <= 1e-6 * np.abs(gfd).max() + 1e-9, (basis, method, err, g, gfd)
+    assert np.abs(g.sum(axis=0)).max() < 1e-9                      # translational invariance
