@@ -23,18 +23,31 @@ __device__ __forceinline__ double s1(const double S[3][EM][EM], int k, int i, in
   return (i >= 0 && j >= 0) ? S[k][i][j] : 0.0;
 }
 
-// Overlap or kinetic integral of the primitive pair for powers pa, pb (the tables
-// hold the pair's one-dimensional overlaps; bexp is the ket exponent).
+// Overlap, kinetic or dipole (-(r - 0), three components) integrals of the primitive
+// pair for powers pa, pb (the tables hold the pair's one-dimensional overlaps; bexp
+// is the ket exponent, A the bra centre).  Returns the number of components.
 template <int EM>
-__device__ double oei_value(int kind, const int pa[3], const int pb[3], double bexp, const double S[3][EM][EM]) {
-  const double sx = s1<EM>(S, 0, pa[0], pb[0]), sy = s1<EM>(S, 1, pa[1], pb[1]), sz = s1<EM>(S, 2, pa[2], pb[2]);
-  if (kind != AGB_OEI_KINETIC) return sx * sy * sz;
+__device__ int oei_value(int kind, const int pa[3], const int pb[3], double bexp, const double A[3],
+                         const double S[3][EM][EM], double out[3]) {
+  const double ss[3] = {s1<EM>(S, 0, pa[0], pb[0]), s1<EM>(S, 1, pa[1], pb[1]), s1<EM>(S, 2, pa[2], pb[2])};
+  if (kind == AGB_OEI_DIPOLE) {
+    for (int k = 0; k < 3; ++k) {
+      const double mom = s1<EM>(S, k, pa[k] + 1, pb[k]) + A[k] * ss[k];
+      out[k] = -mom * ss[(k + 1) % 3] * ss[(k + 2) % 3];
+    }
+    return 3;
+  }
+  if (kind != AGB_OEI_KINETIC) {
+    out[0] = ss[0] * ss[1] * ss[2];
+    return 1;
+  }
   double lap[3];
   for (int k = 0; k < 3; ++k)
     lap[k] = pb[k] * (pb[k] - 1) * s1<EM>(S, k, pa[k], pb[k] - 2) -
              2.0 * bexp * (2 * pb[k] + 1) * s1<EM>(S, k, pa[k], pb[k]) +
              4.0 * bexp * bexp * s1<EM>(S, k, pa[k], pb[k] + 2);
-  return -0.5 * (lap[0] * sy * sz + sx * lap[1] * sz + sx * sy * lap[2]);
+  out[0] = -0.5 * (lap[0] * ss[1] * ss[2] + ss[0] * lap[1] * ss[2] + ss[0] * ss[1] * lap[2]);
+  return 1;
 }
 
 __device__ __forceinline__ double herm_sum(const double* Ex, const double* Ey, const double* Ez, int nx, int ny,
@@ -57,7 +70,8 @@ __global__ void oei_deriv_kernel(agb_basis b, int kind, double* __restrict__ out
   const int atA = b.shell_atom[b.bf_shell[mu]], atB = b.shell_atom[b.bf_shell[nu]];
   const int pa[3] = {fa.x, fa.y, fa.z}, pb[3] = {fb.x, fb.y, fb.z};
   const int64_t nn = (int64_t)n * n;
-  double dA[3] = {0.0, 0.0, 0.0}, dB[3] = {0.0, 0.0, 0.0};
+  const int ncomp = (kind == AGB_OEI_DIPOLE) ? 3 : 1;
+  double dA[3][3] = {}, dB[3][3] = {};     // [direction][component]
   double S[3][EM][EM];
   double E0[3][EM], Ep[EM], Em[EM];
   double R[rsize(LT)], W[rsize(LT)];
@@ -66,25 +80,27 @@ __global__ void oei_deriv_kernel(agb_basis b, int kind, double* __restrict__ out
     for (int j = 0; j < fb.np; ++j) {
       const double bb = b.exps[fb.p0 + j], cc = ca * b.coefs[fb.p0 + j];
       if (kind != AGB_OEI_POTENTIAL) {
-        for (int k = 0; k < 3; ++k) os_table<EM>(pa[k] + 1, pb[k] + 3, a, bb, fa.A[k], fb.A[k], S[k]);
+        for (int k = 0; k < 3; ++k) os_table<EM>(pa[k] + 2, pb[k] + 3, a, bb, fa.A[k], fb.A[k], S[k]);
         for (int c = 0; c < 3; ++c) {
+          double vp[3], vm[3] = {0.0, 0.0, 0.0};
           int q[3] = {pa[0], pa[1], pa[2]};
           q[c] += 1;
-          double v = 2.0 * a * oei_value<EM>(kind, q, pb, bb, S);
+          oei_value<EM>(kind, q, pb, bb, fa.A, S, vp);
           if (pa[c] > 0) {
             q[c] -= 2;
-            v -= pa[c] * oei_value<EM>(kind, q, pb, bb, S);
+            oei_value<EM>(kind, q, pb, bb, fa.A, S, vm);
           }
-          dA[c] += cc * v;
+          for (int m = 0; m < ncomp; ++m) dA[c][m] += cc * (2.0 * a * vp[m] - pa[c] * vm[m]);
           if (kind == AGB_OEI_OVERLAP_HALF) continue;
           int r[3] = {pb[0], pb[1], pb[2]};
           r[c] += 1;
-          v = 2.0 * bb * oei_value<EM>(kind, pa, r, bb, S);
+          oei_value<EM>(kind, pa, r, bb, fa.A, S, vp);
+          vm[0] = vm[1] = vm[2] = 0.0;
           if (pb[c] > 0) {
             r[c] -= 2;
-            v -= pb[c] * oei_value<EM>(kind, pa, r, bb, S);
+            oei_value<EM>(kind, pa, r, bb, fa.A, S, vm);
           }
-          dB[c] += cc * v;
+          for (int m = 0; m < ncomp; ++m) dB[c][m] += cc * (2.0 * bb * vp[m] - pb[c] * vm[m]);
         }
         continue;
       }
@@ -131,17 +147,18 @@ __global__ void oei_deriv_kernel(agb_basis b, int kind, double* __restrict__ out
           vB[c] = v;
         }
         for (int c = 0; c < 3; ++c) {
-          dA[c] += pref * vA[c];
-          dB[c] += pref * vB[c];
+          dA[c][0] += pref * vA[c];
+          dB[c][0] += pref * vB[c];
           out[((int64_t)at * 3 + c) * nn + idx] -= pref * (vA[c] + vB[c]);
         }
       }
     }
   }
-  for (int c = 0; c < 3; ++c) {
-    out[((int64_t)atA * 3 + c) * nn + idx] += dA[c];
-    if (kind != AGB_OEI_OVERLAP_HALF) out[((int64_t)atB * 3 + c) * nn + idx] += dB[c];
-  }
+  for (int c = 0; c < 3; ++c)
+    for (int m = 0; m < ncomp; ++m) {
+      out[(((int64_t)atA * 3 + c) * ncomp + m) * nn + idx] += dA[c][m];
+      if (kind != AGB_OEI_OVERLAP_HALF) out[(((int64_t)atB * 3 + c) * ncomp + m) * nn + idx] += dB[c][m];
+    }
 }
 
 __device__ __forceinline__ int64_t tri(int64_t k) {
@@ -282,11 +299,12 @@ extern "C" agb_status agb_ao_one_electron_deriv(const agb_basis* basis, int kind
   AGB_ARG_CHECK(basis != nullptr && out != nullptr, "NULL argument");
   AGB_ARG_CHECK(basis->lmax >= 0 && basis->lmax <= kLMax, "shell angular momentum above f (l = 3) is not supported");
   AGB_ARG_CHECK(kind == AGB_OEI_OVERLAP || kind == AGB_OEI_KINETIC || kind == AGB_OEI_POTENTIAL ||
-                    kind == AGB_OEI_OVERLAP_HALF,
-                "derivatives exist for overlap, kinetic, potential and the half-derivative overlap");
+                    kind == AGB_OEI_OVERLAP_HALF || kind == AGB_OEI_DIPOLE,
+                "derivatives exist for overlap, kinetic, potential, dipole and the half-derivative overlap");
   const int64_t n2 = (int64_t)basis->ncart * basis->ncart;
+  const int ncomp = (kind == AGB_OEI_DIPOLE) ? 3 : 1;
   cudaStream_t st = (cudaStream_t)stream;
-  AGB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * n2 * 3 * basis->natom, st));
+  AGB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * n2 * 3 * ncomp * basis->natom, st));
   const int threads = 128;
   const unsigned grid = (unsigned)((n2 + threads - 1) / threads);
   if (basis->lmax <= 1)

@@ -1,4 +1,5 @@
-"""Analytic nuclear gradients of the RHF, CID_SO and CISD_SO energies at zero field.
+"""Analytic nuclear gradients of the RHF, CID_SO and CISD_SO energies (zero magnetic
+field; a uniform electric field allowed), and atomic polar tensors from them.
 
 The finite-difference route (fin_diff.compute_Nuclear_Gradient) needs 2 x 3N
 complete calculations; this one needs one: the SCF, the CI solve, its
@@ -61,7 +62,8 @@ def nuclear_repulsion_deriv1(mol):
 
 def nuclear_gradient(parameters, precision="fp64", return_parts=False):
     """Analytic dE/dR (natom, 3) of parameters['method'] in RHF, CID_SO, CISD_SO (or the
-    spatial CID / CISD, the same energies) at zero electric and magnetic field."""
+    spatial CID / CISD, the same energies) at zero magnetic field, in the electric
+    field parameters['F_el'] (real orbitals)."""
     from .adjoint import mo_coefficient_gradient
     from .hamiltonian import Hamiltonian
     from .hf_wfn import hf_wfn
@@ -69,8 +71,9 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
     method = parameters["method"]
     if method not in ("RHF", "CID", "CISD", "CID_SO", "CISD_SO"):
         raise ValueError(f"analytic gradients exist for RHF, CID and CISD, not {method}")
-    if any(f != 0.0 for f in parameters["F_el"]) or any(f != 0.0 for f in parameters["F_mag"]):
-        raise ValueError("analytic gradients are implemented at zero field")
+    if any(f != 0.0 for f in parameters["F_mag"]):
+        raise ValueError("analytic gradients are implemented at zero magnetic field (real orbitals)")
+    F_el = [float(f) for f in parameters["F_el"]]
     if method != "RHF" and parameters.get("freeze_core"):
         raise ValueError("analytic correlated gradients are implemented without frozen core")
     H = Hamiltonian(parameters)
@@ -84,6 +87,10 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
     m = MintsHelper(H.basis_set)
     Sd = m.oei_deriv_all(_lib.OEI_OVERLAP)                       # [natom, 3, n, n]
     hd = m.oei_deriv_all(_lib.OEI_KINETIC) + m.oei_deriv_all(_lib.OEI_POTENTIAL)
+    if any(F_el):                                                # h = T + V - F.mu_el (hamiltonian.py:65-68)
+        dmu = m.oei_deriv_all(_lib.OEI_DIPOLE)                   # [natom, 3, 3, n, n]
+        for beta in range(3):
+            hd = hd - F_el[beta] * dmu[:, :, beta]
     Gd = m.eri_deriv_all()                                       # [natom, 3, n, n, n, n]
     Cd = to_dev(C, torch.float64)
     Co = Cd[:, :no].contiguous()
@@ -99,6 +106,8 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
             two_e = jk_fock(GR[K, c], Dc, zero, 0.25).real
             g_hf[K, c] = float(torch.sum(2.0 * Dh * hd[K, c]) + torch.sum(2.0 * Dh * two_e) - torch.sum(Wd * Sd[K, c]))
     g_hf += nuclear_repulsion_deriv1(H.molecule)
+    # E_nuc(F) = E_nuc + (-F) . sum_A Z_A R_A (apyib/hamiltonian.py:58-61)
+    g_hf -= np.outer(H.molecule.Z.astype(float), np.asarray(F_el))
     if method == "RHF":
         return (g_hf, {"E": complex(E_scf) + H.E_nuc}) if return_parts else g_hf
 
@@ -148,3 +157,20 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
         return g, {"hf": g_hf, "skeleton": skel, "orbital": orb, "E_corr": E_corr,
                    "E": complex(E_scf) + H.E_nuc + E_corr}
     return g
+
+
+def apt(parameters, field_step=1e-3, precision="fp64"):
+    """Atomic polar tensor P[3N, 3] = d mu_beta / d R = -d^2 E / (dR dF_beta) as central
+    differences over the electric field of analytic nuclear gradients: six
+    gradient evaluations (one SCF + one CI solve each) where the reference's
+    finite-difference APT (apyib/fin_diff.py:151-265) needs 4 x 3N x 3 energies."""
+    P = None
+    for beta in range(3):
+        g = []
+        for s in (1, -1):
+            F = list(parameters["F_el"])
+            F[beta] += s * field_step
+            g.append(nuclear_gradient(dict(parameters, F_el=F), precision=precision).reshape(-1))
+        col = -(g[0] - g[1]) / (2 * field_step)
+        P = col[:, None] if P is None else np.concatenate([P, col[:, None]], axis=1)
+    return P

@@ -128,9 +128,10 @@ class MintsHelper(object):
     # ------------------------------------------------------------------ nuclear derivatives
     def oei_deriv_all(self, kind):
         """[natom, 3, nbf, nbf] device tensor of d(integral)/dR for OVERLAP, KINETIC,
-        POTENTIAL or OVERLAP_HALF (bra derivative only)."""
+        POTENTIAL or OVERLAP_HALF (bra derivative only); [natom, 3, 3, nbf, nbf] for DIPOLE."""
         nc, na = self.basis.ncart(), self.basis.molecule.natom()
-        out = torch.empty((na, 3, nc, nc), dtype=torch.float64, device=device())
+        shape = (na, 3, 3, nc, nc) if kind == _lib.OEI_DIPOLE else (na, 3, nc, nc)
+        out = torch.empty(shape, dtype=torch.float64, device=device())
         _lib.call("agb_ao_one_electron_deriv", ctypes.byref(self._c), kind, ptr(out), stream_ptr())
         return self._to_ao(out, 2)
 

@@ -313,7 +313,8 @@ agb_status agb_ao_eri(const agb_basis* basis, double* out, void* stream);
 /* Nuclear first derivatives over the Cartesian functions, out[atom][x,y,z][ncart][ncart]
  * (zeroed by the call) for kind AGB_OEI_OVERLAP, AGB_OEI_KINETIC, AGB_OEI_POTENTIAL
  * (basis-function centres and the attracting nucleus both move) or
- * AGB_OEI_OVERLAP_HALF.  psi4's MintsHelper ao_oei_deriv1 / ao_overlap_half_deriv1
+ * AGB_OEI_OVERLAP_HALF; out[atom][x,y,z][component][ncart][ncart] for AGB_OEI_DIPOLE
+ * (origin 0).  psi4's MintsHelper ao_oei_deriv1 / ao_overlap_half_deriv1
  * (apyib/analytic_aats.py:96-104). */
 agb_status agb_ao_one_electron_deriv(const agb_basis* basis, int kind, double* out, void* stream);
 

@@ -33,3 +33,36 @@ def test_analytic_gradient_matches_finite_differences(basis, method):
     err = np.abs(g - gfd).max()
     assert err <= 1e-6 * np.abs(gfd).max() + 1e-9, (basis, method, err, g, gfd)
     assert np.abs(g.sum(axis=0)).max() < 1e-9                      # translational invariance
+
+
+def _apt_cases():
+    import json
+    import os
+    gold = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fd_goldens.json")))
+    cases = [c for c in gold["apt"] if c["parameters"]["method"] in ("RHF", "CID", "CID_SO")]
+    return gold, cases
+
+
+APT_GOLD, APT_CASES = _apt_cases()
+
+
+@pytest.mark.parametrize("case", APT_CASES, ids=[c["name"] for c in APT_CASES])
+def test_semianalytic_apt_matches_reference_golden(case):
+    """APTs from six analytic gradients (+-1e-3 a.u. field) against the reference's
+    finite-difference golden (apyib/tests/test_010_APT.py) to its tolerance."""
+    from apyib_gb300.gradient import apt
+    p = dict(case["parameters"])
+    p["geom"] = APT_GOLD["molecules"][p["geom"]["moldict"]]
+    P = apt(p)
+    err = np.abs(P - np.array(case["ref"])).max()
+    assert err < case["tol"], (case["name"], err)
+
+
+def test_gradient_in_electric_field():
+    p = dict(PARAMS, geom=H2O, basis="STO-3G", method="CISD_SO", freeze_core=False, F_el=[0.0, 0.003, -0.002])
+    g = nuclear_gradient(p)
+    E_list, _, C, bs = energy(p)
+    fd = finite_difference(p, bs, C)
+    g1, g2 = fd.compute_Nuclear_Gradient(1e-3)[0], fd.compute_Nuclear_Gradient(5e-4)[0]
+    gfd = (4 * g2 - g1) / 3
+    assert np.abs(g - gfd).max() <= 1e-6 * np.abs(gfd).max() + 1e-9

@@ -24,7 +24,8 @@ def _ints_at(mol0, name, k, c, d):
     x[k, c] += d
     mol.set_geometry(x)
     m = MintsHelper(B.BasisSet.build(mol, name))
-    return {"OVERLAP": m.ao_overlap(), "KINETIC": m.ao_kinetic(), "POTENTIAL": m.ao_potential(), "ERI": m.ao_eri()}
+    return {"OVERLAP": m.ao_overlap(), "KINETIC": m.ao_kinetic(), "POTENTIAL": m.ao_potential(), "ERI": m.ao_eri(),
+            "DIPOLE": np.stack(m.ao_dipole())}
 
 
 @pytest.mark.parametrize("name", ["STO-3G", "6-31G(d)", "cc-pVDZ"])
@@ -33,7 +34,15 @@ def test_derivatives_match_central_differences(name):
     m = MintsHelper(B.BasisSet.build(mol, name))
     got = {kk: m.oei_deriv_all(v).cpu().numpy() for kk, v in KINDS.items()}
     got["ERI"] = m.eri_deriv_all().cpu().numpy()
+    dip = m.oei_deriv_all(_lib.OEI_DIPOLE).cpu().numpy()                # [atom, c, beta, n, n]
+    S = m.ao_overlap()
+    for c in range(3):                                   # rigid translation: d(-<r>)/dR summed = -S
+        for beta in range(3):
+            np.testing.assert_allclose(dip[:, c, beta].sum(axis=0), -S * (c == beta), atol=1e-11, rtol=0)
+    got["DIPOLE"] = dip
     for kk, g in got.items():
+        if kk == "DIPOLE":
+            continue
         tot = g.sum(axis=0)                                       # translational invariance
         assert np.abs(tot).max() < 1e-11 * max(1.0, np.abs(g).max()), (name, kk, np.abs(tot).max())
     h = 2e-3
