@@ -1,0 +1,247 @@
+"""Analytic atomic axial tensors of RHF, CID and CISD wavefunctions at zero field
+(the quantity of apyib/analytic_aats.py:30-214, 553-1390), from one solve plus
+first-order responses.
+
+The AAT is I[R, B] = Im d^2 <Psi(R) | Psi(B)> / dR dB, the mixed second
+derivative of the overlap between the wavefunction displaced along a nuclear
+coordinate R and the one in a magnetic field B.  To first order in each
+perturbation,
+
+  * orbitals: phi(R) = chi(R) C (1 + R U^R), phi(B) = chi C (1 + B U^B), so the
+    spin-orbital MO overlap is S(R, B) = 1 + R X + B Y + R B X Y with
+    X = U^R^H + C^H <d chi/dR | chi> C (the half-derivative overlap) and Y = U^B;
+  * amplitudes: t(R) = t + R t^R, t(B) = t + B t^B (normalised as the state is).
+
+U^R (real) and U^B (imaginary) come from the closed-shell CPHF equations
+(nuclear: gradient.py; magnetic: (e_a - e_i) X_ai + sum_bk [(ak|ib) - (ab|ik)] X_bk
+= -Y_ai for U^B = i X, h^B = i Y = (i/2) L in the MO basis, U^B zero within the
+occupied and within the virtual space), t^R and t^B from the amplitude response
+(response.solve_response) with the derivative Hamiltonians in the MO basis
+(skeleton integrals + U^H F + F U + G[dD], and the U terms of the ERIs).  The
+overlap sums over reference, singly and doubly excited determinants are then the
+Schur-complement contractions of aats.AAT applied to this exactly linearised
+model; its mixed derivative is taken by central differences over the model's
+small parameter (1e-3 and 5e-4, Richardson-combined), which needs no further
+solves and is exact up to O(1e-12).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .aats import AAT
+from .device import device, ptr, stream_ptr, to_dev, workspace
+from .linalg import jk_fock
+
+
+def _ao2mo(ERI_AO, C):
+    """(pq|rs) = sum conj(C_mp) C_nq conj(C_lr) C_ss (mn|ls) for a real AO tensor (GPU)."""
+    nbf = C.shape[0]
+    out = torch.empty((nbf, nbf, nbf, nbf), dtype=torch.complex128, device=device())
+    nb = _lib.load().agb_ao2mo_scratch_bytes(nbf, nbf, _lib.PREC_FP64)
+    buf, sp, n = workspace(nb)
+    _lib.call("agb_ao2mo", ptr(ERI_AO.contiguous()), nbf, ptr(C), nbf, ptr(out), sp, n, _lib.PREC_FP64,
+              stream_ptr())
+    return out
+
+
+def _u_terms(G, U):
+    """First-order change of (pq|rs) when C -> C (1 + U)."""
+    Uc = U.conj()
+    return (torch.einsum("tp,tqrs->pqrs", Uc, G) + torch.einsum("tq,ptrs->pqrs", U, G)
+            + torch.einsum("tr,pqts->pqrs", Uc, G) + torch.einsum("ts,pqrt->pqrs", U, G))
+
+
+class analytic_derivative(object):
+    """apyib/analytic_aats.py:14-29 interface: analytic_derivative(parameters)."""
+
+    def __init__(self, parameters):
+        from .gradient import _real_orbitals
+        from .hamiltonian import Hamiltonian
+        from .hf_wfn import hf_wfn
+        if any(f != 0.0 for f in parameters["F_el"]) or any(f != 0.0 for f in parameters["F_mag"]):
+            raise ValueError("analytic AATs are defined at zero field")
+        if parameters.get("freeze_core"):
+            raise ValueError("analytic AATs are implemented without frozen core")
+        self.parameters = parameters
+        self.H = Hamiltonian(parameters)
+        self.wfn = hf_wfn(self.H)
+        E_scf, C = self.wfn.solve_SCF(parameters)
+        self.C = _real_orbitals(C)
+        self.wfn.C = self.C
+
+    # ------------------------------------------------------------------ orbital responses
+    def _setup(self):
+        from .integrals import MintsHelper
+        wfn, H = self.wfn, self.H
+        nbf, no = wfn.nbf, wfn.ndocc
+        nv = nbf - no
+        self.nbf, self.no = nbf, no
+        natom = H.molecule.natom()
+        self.natom = natom
+        eps = np.asarray(wfn.eps).real
+        self.eps = eps
+        C = to_dev(self.C, torch.float64)
+        Cc = C.to(torch.complex128)
+        self.Cc = Cc
+        m = MintsHelper(H.basis_set)
+        ERI_AO = to_dev(H.ERI, torch.float64)
+        self.ERI_AO = ERI_AO
+        G = _ao2mo(ERI_AO, Cc)                                    # all-MO (pq|rs)
+        self.G = G
+        Gr = G.real.cpu().numpy()
+        o, v = slice(0, no), slice(no, nbf)
+        Co = Cc[:, :no].contiguous()
+        zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=C.device)
+        h_AO = to_dev(np.asarray(H.T) + np.asarray(H.V))
+        F_AO = jk_fock(ERI_AO, Co @ Co.conj().T, h_AO, 1.0)
+        self.F_MO = Cc.conj().T @ F_AO @ Cc
+        # nuclear CPHF (real), U_oo = -S_oo / 2, U_vv = -S_vv / 2
+        Sd = m.oei_deriv_all(_lib.OEI_OVERLAP)
+        hd = m.oei_deriv_all(_lib.OEI_KINETIC) + m.oei_deriv_all(_lib.OEI_POTENTIAL)
+        Hd = m.oei_deriv_all(_lib.OEI_OVERLAP_HALF)
+        Gd = m.eri_deriv_all()
+        A = (4.0 * Gr[v, o, v, o] - Gr[v, v, o, o].transpose(0, 2, 1, 3) - Gr[v, o, o, v].transpose(0, 2, 3, 1))
+        A = A.reshape(nv * no, nv * no)
+        A[np.diag_indices_from(A)] += (eps[no:][:, None] - eps[:no][None, :]).reshape(-1)
+        Cn = self.C
+        rhs, self.SR, self.skelF, self.skelG, self.HR = [], [], [], [], []
+        for K in range(natom):
+            for c in range(3):
+                GR = Gd[K, c].contiguous()
+                dF_AO = hd[K, c].to(torch.complex128) + jk_fock(GR, (Co @ Co.conj().T), zero, 1.0)
+                Fm = (Cc.conj().T @ dF_AO @ Cc)
+                S = Cn.T @ Sd[K, c].cpu().numpy() @ Cn
+                B = Fm.real.cpu().numpy()[v, o] - S[v, o] * eps[None, :no] \
+                    - np.einsum("kl,aikl->ai", S[o, o], 2.0 * Gr[v, o, o, o] - Gr[v, o, o, o].transpose(0, 2, 1, 3))
+                rhs.append(-B.reshape(-1))
+                self.SR.append(S)
+                self.skelF.append(Fm)
+                self.skelG.append(_ao2mo(GR, Cc))
+                self.HR.append(Cc.conj().T @ Hd[K, c].to(torch.complex128) @ Cc)
+        X = np.linalg.solve(A, np.stack(rhs, axis=1))
+        self.UR = []
+        for n, S in enumerate(self.SR):
+            U = -0.5 * S.copy()
+            U[v, o] = X[:, n].reshape(nv, no)
+            U[o, v] = -S[o, v] - U[v, o].T
+            self.UR.append(torch.as_tensor(U).to(C.device).to(torch.complex128))
+        # magnetic CPHF: U^B = i X with X_ai real, X_ia = X_ai, zero within occ and within vir
+        L = m.ao_angular_momentum(return_torch=True)
+        Am = (Gr[v, o, o, v].transpose(0, 2, 3, 1) - Gr[v, v, o, o].transpose(0, 2, 1, 3)).reshape(nv * no, nv * no)
+        Am[np.diag_indices_from(Am)] += (eps[no:][:, None] - eps[:no][None, :]).reshape(-1)
+        self.hB, rhsB = [], []
+        for b in range(3):
+            Y = Cn.T @ (0.5 * L[b].cpu().numpy()) @ Cn           # h^B = i Y (MO)
+            self.hB.append(torch.as_tensor(1j * Y).to(C.device))
+            rhsB.append(-Y[v, o].reshape(-1))
+        XB = np.linalg.solve(Am, np.stack(rhsB, axis=1))
+        self.UB = []
+        for b in range(3):
+            U = np.zeros((nbf, nbf), dtype=complex)
+            U[v, o] = 1j * XB[:, b].reshape(nv, no)
+            U[o, v] = 1j * XB[:, b].reshape(nv, no).T
+            self.UB.append(torch.as_tensor(U).to(C.device))
+
+    def _dH(self, U, skelF=None, skelG=None, hx=None):
+        """MO derivative Fock matrix and ERIs for orbital response U (+ skeleton parts)."""
+        Cc, no, nbf = self.Cc, self.no, self.nbf
+        zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=Cc.device)
+        dC = Cc @ U
+        Co, dCo = Cc[:, :no], dC[:, :no]
+        dD = dCo @ Co.conj().T + Co @ dCo.conj().T
+        dF = U.conj().T @ self.F_MO + self.F_MO @ U + Cc.conj().T @ jk_fock(self.ERI_AO, dD.contiguous(), zero, 1.0) @ Cc
+        if skelF is not None:
+            dF = dF + skelF
+        if hx is not None:
+            dF = dF + hx
+        dG = _u_terms(self.G, U)
+        if skelG is not None:
+            dG = dG + skelG
+        return dF, dG
+
+    # ------------------------------------------------------------------ amplitudes and responses
+    def _amplitudes(self, singles, precision):
+        from .cisd import CISDPlan, solve
+        from .response import solve_response
+        from .utils import compute_F_SO
+        no, nbf = self.no, self.nbf
+        o, v = 2 * no, 2 * (nbf - no)
+        eps = self.eps
+        eps_so = np.concatenate([np.repeat(eps[:no], 2), np.repeat(eps[no:], 2)])
+        P = dict(self.parameters)
+        plan = CISDPlan(o, v, singles=singles)
+        plan.set_fock(compute_F_SO(None, self.F_MO, return_torch=True), eps_so)
+        plan.blocks_from_mo(self.G)
+        E, t = solve(plan, P, precision=precision)
+
+        def respond(dF, dG):
+            px = CISDPlan(o, v, singles=singles)
+            px.set_fock(compute_F_SO(None, dF, return_torch=True), eps_so)
+            px.blocks_from_mo(dG)
+            return solve_response(plan, px, t, E, P)[1]
+        tR = [respond(*self._dH(self.UR[n], self.skelF[n], self.skelG[n])) for n in range(len(self.UR))]
+        tB = [respond(*self._dH(self.UB[b], hx=self.hB[b])) for b in range(3)]
+        unpack = plan.unpack
+        return unpack(t), [unpack(x) for x in tR], [unpack(x) for x in tB]
+
+    def _so(self, M):
+        n = M.shape[0]
+        S = torch.zeros((2 * n, 2 * n), dtype=torch.complex128, device=M.device)
+        S[0::2, 0::2] = M
+        S[1::2, 1::2] = M
+        return S
+
+    def _aats(self, method, normalization, precision="fp64"):
+        self._setup()
+        nso = 2 * self.nbf
+        eye = torch.eye(nso, dtype=torch.complex128, device=self.Cc.device)
+        Xs = [self._so(U.conj().T + Hr) for U, Hr in zip(self.UR, self.HR)]
+        Ys = [self._so(U) for U in self.UB]
+        singles = method in ("CISD", "CISD_SO")
+        if method == "RHF":
+            T0, TR, TB = (None, None), [(None, None)] * len(Xs), [(None, None)] * 3
+        else:
+            T0, TR, TB = self._amplitudes(singles, precision)
+        n3 = 3 * self.natom
+        out = {}
+        for eps in (1e-3, 5e-4):
+            ov = {"uu": eye}
+            for b in range(3):
+                ov["up", b], ov["un", b] = eye + eps * Ys[b], eye - eps * Ys[b]
+            for a in range(n3):
+                ov["pu", a], ov["nu", a] = eye + eps * Xs[a], eye - eps * Xs[a]
+                for b in range(3):
+                    XY = eps * eps * (Xs[a] @ Ys[b])
+                    ov["pp", a, b] = eye + eps * Xs[a] + eps * Ys[b] + XY
+                    ov["pn", a, b] = eye + eps * Xs[a] - eps * Ys[b] - XY
+                    ov["np", a, b] = eye - eps * Xs[a] + eps * Ys[b] - XY
+                    ov["nn", a, b] = eye - eps * Xs[a] - eps * Ys[b] + XY
+
+            def amp(base, d, s):
+                if base[0] is None and base[1] is None and method == "RHF":
+                    return [1.0, 0, 0]
+                t1 = None if base[0] is None else base[0] + s * eps * d[0]
+                t2 = base[1] + s * eps * d[1]
+                return [1.0, t1, t2]
+            so_method = method if method.endswith("_SO") or method == "RHF" else method + "_SO"
+            A = AAT.from_overlaps({"method": so_method}, ndocc=self.no, nbf=self.nbf, nfzc=0, natom=self.natom,
+                                  overlaps=ov, unperturbed_T=amp(T0, (0, 0), 0),
+                                  nuc_pos_T=[amp(T0, TR[a], 1) for a in range(n3)],
+                                  nuc_neg_T=[amp(T0, TR[a], -1) for a in range(n3)],
+                                  mag_pos_T=[amp(T0, TB[b], 1) for b in range(3)],
+                                  mag_neg_T=[amp(T0, TB[b], -1) for b in range(3)],
+                                  nuc_pert_strength=eps, mag_pert_strength=eps)
+            out[eps] = np.array([[A.compute_SO_aats(a, b, normalization) for b in range(3)] for a in range(n3)])
+        return (4 * out[5e-4] - out[1e-3]) / 3
+
+    # ------------------------------------------------------------------ reference names
+    def compute_RHF_AATs(self, orbitals="non-canonical"):
+        return self._aats("RHF", "intermediate")
+
+    def compute_CID_AATs(self, normalization="full", orbitals="non-canonical", print_level=0):
+        return self._aats("CID", normalization)
+
+    def compute_CISD_AATs(self, normalization="full", orbitals="non-canonical", print_level=0):
+        return self._aats("CISD", normalization)
