@@ -299,12 +299,27 @@ def water_workloads():
     P_fd = fd0.compute_APT(1e-3, 1e-4)
     torch.cuda.synchronize()
     t5 = time.perf_counter()
+    from apyib_gb300.analytic_aats import analytic_derivative
+    analytic_derivative(dict(p0, basis="STO-3G")).compute_CISD_AATs()      # warm-up
+    torch.cuda.synchronize()
+    t6 = time.perf_counter()
+    aat_an = analytic_derivative(p0).compute_CISD_AATs(normalization="full")
+    torch.cuda.synchronize()
+    t7 = time.perf_counter()
+    inputs0 = fd0.compute_AAT(1e-4, 1e-4)
+    aat_fd = AAT(p0, hf_wfn(Hamiltonian(p0)), C, basis, T_list, *inputs0, 1e-4, 1e-4).compute_aat_tensor("full")
+    torch.cuda.synchronize()
+    t8 = time.perf_counter()
     out["derivatives_zero_field"] = {
         "gradient_analytic_s": t1 - t0, "gradient_fd_s": t3 - t2, "gradient_fd_solves": 18,
         "gradient_max_abs_diff": float(np.abs(g_an - g_fd).max()),
         "apt_semianalytic_s": t4 - t3, "apt_analytic_gradients": 6, "apt_fd_s": t5 - t4, "apt_fd_energies": 108,
         "apt_max_abs_diff": float(np.abs(P_an - P_fd.real).max()),
-        "note": "water cc-pVDZ CISD_SO, zero field; FD steps 1e-4 bohr (gradient), 1e-3 bohr / 1e-4 a.u. (APT)"}
+        "aat_analytic_s": t7 - t6, "aat_analytic_responses": 12, "aat_fd_s": t8 - t7, "aat_fd_solves": 24,
+        "aat_max_abs_diff": float(np.abs(aat_an - aat_fd).max()),
+        "note": "water cc-pVDZ CISD_SO, zero field; FD steps 1e-4 bohr (gradient, AAT), 1e-3 bohr / 1e-4 a.u. "
+                "(APT), 1e-4 a.u. (AAT); analytic AAT = one solve, nuclear + magnetic CPHF, 3N+3 amplitude "
+                "responses"}
     return out
 
 
