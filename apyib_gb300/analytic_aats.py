@@ -1,5 +1,5 @@
-"""Analytic atomic axial tensors of RHF, CID and CISD wavefunctions at zero field
-(the quantity of apyib/analytic_aats.py:30-214, 553-1390), from one solve plus
+"""Analytic atomic axial tensors of RHF, MP2, CID and CISD wavefunctions at zero
+field (the quantity of apyib/analytic_aats.py:30-1390), from one solve plus
 first-order responses.
 
 The AAT is I[R, B] = Im d^2 <Psi(R) | Psi(B)> / dR dB, the mixed second
@@ -188,6 +188,33 @@ class analytic_derivative(object):
         unpack = plan.unpack
         return unpack(t), [unpack(x) for x in tR], [unpack(x) for x in tB]
 
+    def _mp2_amplitudes(self):
+        """MP2 first-order amplitudes t = <ab||ij> / (e_i + e_j - e_a - e_b) (apyib/mp2_wfn.py:
+        64-87) and their responses from the first-order non-canonical MP2 equation
+        <ab||ij> + P(F_vv t) - P(F_oo t) = 0 (the Fock terms of apyib/ci_wfn.py:324-327):
+        t^x = [<ab||ij>^x + F^x_bc t_ijac + F^x_ac t_ijcb - F^x_kj t_ikab - F^x_ki t_kjab] / D."""
+        from .utils import compute_ERI_SO, compute_F_SO
+        no, nbf = self.no, self.nbf
+        o = 2 * no
+        e = torch.as_tensor(np.repeat(self.eps, 2)).to(self.Cc.device)
+        D = e[:o, None, None, None] + e[None, :o, None, None] - e[None, None, o:, None] - e[None, None, None, o:]
+
+        def antisym(Gmo):
+            Gs = compute_ERI_SO(None, Gmo, return_torch=True)[o:, :o, o:, :o]      # (a i | b j)
+            return Gs.permute(1, 3, 0, 2) - Gs.permute(3, 1, 0, 2)                # <ab||ij> as [i,j,a,b]
+        t = antisym(self.G) / D
+
+        def respond(dF, dG):
+            Fs = compute_F_SO(None, dF, return_torch=True)
+            Fo, Fv = Fs[:o, :o], Fs[o:, o:]
+            r = antisym(dG)
+            r = r + torch.einsum("bc,ijac->ijab", Fv, t) + torch.einsum("ac,ijcb->ijab", Fv, t)
+            r = r - torch.einsum("kj,ikab->ijab", Fo, t) - torch.einsum("ki,kjab->ijab", Fo, t)
+            return (None, r / D)
+        tR = [respond(*self._dH(self.UR[n], self.skelF[n], self.skelG[n])) for n in range(len(self.UR))]
+        tB = [respond(*self._dH(self.UB[b], hx=self.hB[b])) for b in range(3)]
+        return (None, t), tR, tB
+
     def _so(self, M):
         n = M.shape[0]
         S = torch.zeros((2 * n, 2 * n), dtype=torch.complex128, device=M.device)
@@ -204,6 +231,8 @@ class analytic_derivative(object):
         singles = method in ("CISD", "CISD_SO")
         if method == "RHF":
             T0, TR, TB = (None, None), [(None, None)] * len(Xs), [(None, None)] * 3
+        elif method in ("MP2", "MP2_SO"):
+            T0, TR, TB = self._mp2_amplitudes()
         else:
             T0, TR, TB = self._amplitudes(singles, precision)
         n3 = 3 * self.natom
@@ -243,6 +272,9 @@ class analytic_derivative(object):
     # ------------------------------------------------------------------ reference names
     def compute_RHF_AATs(self, orbitals="non-canonical"):
         return self._aats("RHF", "intermediate")
+
+    def compute_MP2_AATs(self, normalization="full", orbitals="non-canonical"):
+        return self._aats("MP2", normalization)
 
     def compute_CID_AATs(self, normalization="full", orbitals="non-canonical", print_level=0):
         return self._aats("CID", normalization)
