@@ -64,8 +64,6 @@ class analytic_derivative(object):
         from .hf_wfn import hf_wfn
         if any(f != 0.0 for f in parameters["F_el"]) or any(f != 0.0 for f in parameters["F_mag"]):
             raise ValueError("analytic AATs are defined at zero field")
-        if parameters.get("freeze_core"):
-            raise ValueError("analytic AATs are implemented without frozen core")
         self.parameters = parameters
         self.H = Hamiltonian(parameters)
         self.wfn = hf_wfn(self.H)
@@ -123,11 +121,26 @@ class analytic_derivative(object):
                 self.skelG.append(_ao2mo(GR, Cc))
                 self.HR.append(Cc.conj().T @ Hd[K, c].to(torch.complex128) @ Cc)
         X = np.linalg.solve(A, np.stack(rhs, axis=1))
+        nf = H.basis_set.n_frozen_core()
+        self.nfzc = nf
         self.UR = []
         for n, S in enumerate(self.SR):
             U = -0.5 * S.copy()
             U[v, o] = X[:, n].reshape(nv, no)
             U[o, v] = -S[o, v] - U[v, o].T
+            if nf:
+                # frozen-active rotations change a frozen-core energy: the orbitals stay canonical,
+                # U_ij = (F^R_ij - e_j S_ij + G[dD]_ij) / (e_j - e_i) for i, j in different blocks
+                Uvo = U[v, o]
+                Gd = (np.einsum("bk,ijbk->ij", Uvo, 4.0 * Gr[o, o, v, o] - Gr[o, v, o, o].transpose(0, 2, 1, 3)
+                                - Gr[o, o, o, v].transpose(0, 2, 3, 1))
+                      - np.einsum("kl,ijkl->ij", S[o, o], 2.0 * Gr[o, o, o, o] - Gr[o, o, o, o].transpose(0, 2, 1, 3)))
+                Bo = self.skelF[n].real.cpu().numpy()[o, o] - S[o, o] * eps[None, :no] + Gd
+                den = eps[None, :no] - eps[:no, None]
+                for i in range(no):
+                    for j in range(no):
+                        if (i < nf) != (j < nf):
+                            U[i, j] = Bo[i, j] / den[i, j]
             self.UR.append(torch.as_tensor(U).to(C.device).to(torch.complex128))
         # magnetic CPHF: U^B = i X with X_ai real, X_ia = X_ai, zero within occ and within vir
         L = m.ao_angular_momentum(return_torch=True)
@@ -142,8 +155,19 @@ class analytic_derivative(object):
         self.UB = []
         for b in range(3):
             U = np.zeros((nbf, nbf), dtype=complex)
-            U[v, o] = 1j * XB[:, b].reshape(nv, no)
-            U[o, v] = 1j * XB[:, b].reshape(nv, no).T
+            Xvo = XB[:, b].reshape(nv, no)
+            U[v, o] = 1j * Xvo
+            U[o, v] = 1j * Xvo.T
+            if nf:
+                # canonical frozen-active rotations: U_ij = (h^B_ij + G[dD]_ij) / (e_j - e_i),
+                # G[dD]_ij = i sum_bk X_bk [(ik|bj) - (ib|kj)]
+                Yb = self.hB[b].imag.cpu().numpy()
+                Gd = np.einsum("bk,ikbj->ij", Xvo, Gr[o, o, v, o]) - np.einsum("bk,ibkj->ij", Xvo, Gr[o, v, o, o])
+                den = eps[None, :no] - eps[:no, None]
+                for i in range(no):
+                    for j in range(no):
+                        if (i < nf) != (j < nf):
+                            U[i, j] = 1j * (Yb[i, j] + Gd[i, j]) / den[i, j]
             self.UB.append(torch.as_tensor(U).to(C.device))
 
     def _dH(self, U, skelF=None, skelG=None, hx=None):
@@ -168,20 +192,21 @@ class analytic_derivative(object):
         from .cisd import CISDPlan, solve
         from .response import solve_response
         from .utils import compute_F_SO
-        no, nbf = self.no, self.nbf
-        o, v = 2 * no, 2 * (nbf - no)
+        no, nbf, nf = self.no, self.nbf, self.nfzc
+        o, v = 2 * (no - nf), 2 * (nbf - no)
         eps = self.eps
-        eps_so = np.concatenate([np.repeat(eps[:no], 2), np.repeat(eps[no:], 2)])
+        eps_so = np.concatenate([np.repeat(eps[nf:no], 2), np.repeat(eps[no:], 2)])
         P = dict(self.parameters)
+        t_ = slice(nf, nbf)
         plan = CISDPlan(o, v, singles=singles)
-        plan.set_fock(compute_F_SO(None, self.F_MO, return_torch=True), eps_so)
-        plan.blocks_from_mo(self.G)
+        plan.set_fock(compute_F_SO(None, self.F_MO[t_, t_].contiguous(), return_torch=True), eps_so)
+        plan.blocks_from_mo(self.G[t_, t_, t_, t_].contiguous())
         E, t = solve(plan, P, precision=precision)
 
         def respond(dF, dG):
             px = CISDPlan(o, v, singles=singles)
-            px.set_fock(compute_F_SO(None, dF, return_torch=True), eps_so)
-            px.blocks_from_mo(dG)
+            px.set_fock(compute_F_SO(None, dF[t_, t_].contiguous(), return_torch=True), eps_so)
+            px.blocks_from_mo(dG[t_, t_, t_, t_].contiguous())
             return solve_response(plan, px, t, E, P)[1]
         tR = [respond(*self._dH(self.UR[n], self.skelF[n], self.skelG[n])) for n in range(len(self.UR))]
         tB = [respond(*self._dH(self.UB[b], hx=self.hB[b])) for b in range(3)]
@@ -194,18 +219,19 @@ class analytic_derivative(object):
         <ab||ij> + P(F_vv t) - P(F_oo t) = 0 (the Fock terms of apyib/ci_wfn.py:324-327):
         t^x = [<ab||ij>^x + F^x_bc t_ijac + F^x_ac t_ijcb - F^x_kj t_ikab - F^x_ki t_kjab] / D."""
         from .utils import compute_ERI_SO, compute_F_SO
-        no, nbf = self.no, self.nbf
-        o = 2 * no
-        e = torch.as_tensor(np.repeat(self.eps, 2)).to(self.Cc.device)
+        no, nbf, nf = self.no, self.nbf, self.nfzc
+        o = 2 * (no - nf)
+        t_ = slice(nf, nbf)
+        e = torch.as_tensor(np.repeat(self.eps[nf:], 2)).to(self.Cc.device)
         D = e[:o, None, None, None] + e[None, :o, None, None] - e[None, None, o:, None] - e[None, None, None, o:]
 
         def antisym(Gmo):
-            Gs = compute_ERI_SO(None, Gmo, return_torch=True)[o:, :o, o:, :o]      # (a i | b j)
+            Gs = compute_ERI_SO(None, Gmo[t_, t_, t_, t_].contiguous(), return_torch=True)[o:, :o, o:, :o]  # (a i|b j)
             return Gs.permute(1, 3, 0, 2) - Gs.permute(3, 1, 0, 2)                # <ab||ij> as [i,j,a,b]
         t = antisym(self.G) / D
 
         def respond(dF, dG):
-            Fs = compute_F_SO(None, dF, return_torch=True)
+            Fs = compute_F_SO(None, dF[t_, t_].contiguous(), return_torch=True)
             Fo, Fv = Fs[:o, :o], Fs[o:, o:]
             r = antisym(dG)
             r = r + torch.einsum("bc,ijac->ijab", Fv, t) + torch.einsum("ac,ijcb->ijab", Fv, t)
@@ -257,7 +283,8 @@ class analytic_derivative(object):
                 t2 = base[1] + s * eps * d[1]
                 return [1.0, t1, t2]
             so_method = method if method.endswith("_SO") or method == "RHF" else method + "_SO"
-            A = AAT.from_overlaps({"method": so_method}, ndocc=self.no, nbf=self.nbf, nfzc=0, natom=self.natom,
+            A = AAT.from_overlaps({"method": so_method}, ndocc=self.no, nbf=self.nbf, nfzc=self.nfzc,
+                                  natom=self.natom,
                                   overlaps=ov, unperturbed_T=amp(T0, (0, 0), 0),
                                   nuc_pos_T=[amp(T0, TR[a], 1) for a in range(n3)],
                                   nuc_neg_T=[amp(T0, TR[a], -1) for a in range(n3)],
