@@ -9,7 +9,7 @@
    ``object.__new__`` and given the attributes its term methods read (overlaps,
    amplitudes, sizes, strengths), so no psi4 call is made.
 2. tests/golden/aat_goldens.json: the golden AAT arrays of
-   apyib/tests/test_011_AAT.py and test_012_AAT_SO.py (read as text with the
+   apyib/tests/test_011_AAT.py, test_012_AAT_SO.py and test_013_AAT_parallel.py (read as text with the
    Python AST), with the geometry, basis, method, normalisation and steps of
    each test.
 
@@ -126,7 +126,7 @@ def small_fixture(mod):
 
 def golden_arrays():
     out = []
-    for rel in ("apyib/tests/test_011_AAT.py", "apyib/tests/test_012_AAT_SO.py"):
+    for rel in ("apyib/tests/test_011_AAT.py", "apyib/tests/test_012_AAT_SO.py", "apyib/tests/test_013_AAT_parallel.py"):
         tree = ast.parse(open(os.path.join(REF_ROOT, rel)).read())
         for fn in tree.body:
             if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_"):
@@ -153,6 +153,11 @@ def golden_arrays():
                 if isinstance(node, ast.Call) and getattr(node.func, "attr", "") in ("compute_AAT",
                                                                                       "compute_parallel_aats"):
                     case["steps"] = [ast.literal_eval(a) for a in node.args if isinstance(a, ast.Constant)]
+                    if node.func.attr == "compute_parallel_aats":
+                        case["parallel_normalization"] = next((ast.literal_eval(k.value) for k in node.keywords
+                                                               if k.arg == "normalization"), "full")
+                if isinstance(node, ast.Assert):
+                    case["tol"] = ast.literal_eval(node.test.comparators[0])
             out.append(case)
     src = open(os.path.join(REF_ROOT, "apyib/data/molecules.py")).read()
     tree = ast.parse(src)
