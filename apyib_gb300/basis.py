@@ -22,9 +22,9 @@ Conventions (those of psi4's shell objects, as apyib/integrals.py:35-50 reads th
 The built-in data are the published contractions (STO-3G and STO-6G: Hehre,
 Stewart and Pople, J. Chem. Phys. 51, 2657 (1969); 6-31G: Hehre, Ditchfield and Pople,
 J. Chem. Phys. 56, 2257 (1972), Ditchfield, Hehre and Pople, J. Chem. Phys. 54,
-724 (1971); 6-31G(d) polarisation exponent 0.8 on O: Hariharan and Pople,
+724 (1971); 6-31G(d) polarisation exponent 0.8 on N and O: Hariharan and Pople,
 Theor. Chim. Acta 28, 213 (1973); cc-pVDZ: Dunning, J. Chem. Phys. 90, 1007 (1989))
-for the elements apyib's energy tests use.  The last three exponents of the
+for the elements apyib's tests use (H, N, O).  The last three exponents of the
 oxygen STO-6G 2sp shell are from the same least-squares fit of the 2s and 2p
 Slater functions (shared exponents, zeta = 2.25) re-done in high precision; it
 reproduces the published first three exponents to 3e-8 and all twelve
@@ -293,10 +293,26 @@ SP   3   1.00
 SP   1   1.00
       0.2700058              1.0000000              1.0000000
 ****
+N     0
+S   6   1.00
+   4173.5110000              0.0018348
+    627.4579000              0.0139950
+    142.9021000              0.0685870
+     40.2343300              0.2322410
+     12.8202100              0.4690700
+      4.3904370              0.3604550
+SP   3   1.00
+     11.6263580             -0.1149610              0.0675800
+      2.7162800             -0.1691180              0.3239070
+      0.7722180              1.1458520              0.7408950
+SP   1   1.00
+      0.2120313              1.0000000              1.0000000
+****
 """
 register_basis("6-31g", _631G_TEXT, pure=False)
 for _name in ("6-31g(d)", "6-31g*"):
-    register_basis(_name, _with_polarisation(_631G_TEXT, "O", _631G_D_O), pure=False)
+    register_basis(_name, _with_polarisation(_with_polarisation(_631G_TEXT, "O", _631G_D_O), "N", _631G_D_O),
+                   pure=False)
 
 register_basis("cc-pvdz", """
 spherical

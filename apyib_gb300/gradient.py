@@ -159,18 +159,22 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
     return g
 
 
-def apt(parameters, field_step=1e-3, precision="fp64"):
+def apt(parameters, field_step=5e-4, precision="fp64", richardson=True):
     """Atomic polar tensor P[3N, 3] = d mu_beta / d R = -d^2 E / (dR dF_beta) as central
-    differences over the electric field of analytic nuclear gradients: six
-    gradient evaluations (one SCF + one CI solve each) where the reference's
-    finite-difference APT (apyib/fin_diff.py:151-265) needs 4 x 3N x 3 energies."""
-    P = None
-    for beta in range(3):
-        g = []
-        for s in (1, -1):
-            F = list(parameters["F_el"])
-            F[beta] += s * field_step
-            g.append(nuclear_gradient(dict(parameters, F_el=F), precision=precision).reshape(-1))
-        col = -(g[0] - g[1]) / (2 * field_step)
-        P = col[:, None] if P is None else np.concatenate([P, col[:, None]], axis=1)
-    return P
+    differences over the electric field of analytic nuclear gradients (length gauge):
+    six gradient evaluations per field step (one SCF + one CI solve each), twice with
+    Richardson extrapolation (steps 2h and h), where the reference's finite-difference
+    APT (apyib/fin_diff.py:151-265) needs 4 x 3N x 3 energies."""
+    def central(h):
+        cols = []
+        for beta in range(3):
+            g = []
+            for s in (1, -1):
+                F = list(parameters["F_el"])
+                F[beta] += s * h
+                g.append(nuclear_gradient(dict(parameters, F_el=F), precision=precision).reshape(-1))
+            cols.append(-(g[0] - g[1]) / (2 * h))
+        return np.stack(cols, axis=1)
+    if not richardson:
+        return central(field_step)
+    return (4.0 * central(field_step) - central(2.0 * field_step)) / 3.0

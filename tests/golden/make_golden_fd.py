@@ -1,4 +1,5 @@
-"""Extract the reference's finite-difference golden values into tests/golden/fd_goldens.json.
+"""Extract the reference's finite-difference (and length-gauge analytic APT) golden values
+into tests/golden/fd_goldens.json.
 
 apyib/tests/test_009_Hessian.py and apyib/tests/test_010_APT.py each set up a
 ``parameters`` dict, compare ``finite_difference.compute_Hessian(h)`` /
@@ -66,6 +67,33 @@ def cases(kind, rel):
     return out
 
 
+def analytic_apt_cases():
+    """The length-gauge analytic APT goldens of apyib/tests/test_022_RHF_Analytic_APT.py
+    (geometry given inside each test); the velocity-gauge ones are a different quantity."""
+    rel = "apyib/tests/test_022_RHF_Analytic_APT.py"
+    tree = ast.parse(open(os.path.join(REF_ROOT, rel)).read())
+    out = []
+    for fn in tree.body:
+        if not isinstance(fn, ast.FunctionDef) or not fn.name.endswith("_LG"):
+            continue
+        local = {n.targets[0].id: n.value.value for n in ast.walk(fn) if isinstance(n, ast.Assign)
+                 and isinstance(n.targets[0], ast.Name) and isinstance(n.value, ast.Constant)
+                 and isinstance(n.value.value, str)}
+        c = {"name": fn.name, "file": rel, "line": fn.lineno}
+        for node in ast.walk(fn):
+            if isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Name):
+                if node.targets[0].id == "parameters":
+                    c["parameters"] = {ast.literal_eval(k): (local[v.id] if isinstance(v, ast.Name)
+                                                             else ast.literal_eval(v))
+                                       for k, v in zip(node.value.keys, node.value.values)}
+                elif node.targets[0].id == "apt_ref":
+                    c["ref"] = ast.literal_eval(node.value.args[0])
+            if isinstance(node, ast.Assert):
+                c["tol"] = ast.literal_eval(node.test.comparators[0])
+        out.append(c)
+    return out
+
+
 def main():
     mols = molecules()
     data = {"molecules": {}, "hessian": [], "apt": []}
@@ -74,6 +102,7 @@ def main():
             key = c["parameters"]["geom"]["moldict"]
             data["molecules"][key] = mols[key]
             data[kind].append(c)
+    data["apt_analytic"] = analytic_apt_cases()
     path = os.path.join(HERE, "fd_goldens.json")
     with open(path, "w") as f:
         json.dump(data, f, indent=1)

@@ -48,7 +48,7 @@ APT_GOLD, APT_CASES = _apt_cases()
 
 @pytest.mark.parametrize("case", APT_CASES, ids=[c["name"] for c in APT_CASES])
 def test_semianalytic_apt_matches_reference_golden(case):
-    """APTs from six analytic gradients (+-1e-3 a.u. field) against the reference's
+    """APTs from analytic gradients in +-field (Richardson, 5e-4 and 1e-3 a.u.) against the reference's
     finite-difference golden (apyib/tests/test_010_APT.py) to its tolerance."""
     from apyib_gb300.gradient import apt
     p = dict(case["parameters"])
@@ -66,3 +66,13 @@ def test_gradient_in_electric_field():
     g1, g2 = fd.compute_Nuclear_Gradient(1e-3)[0], fd.compute_Nuclear_Gradient(5e-4)[0]
     gfd = (4 * g2 - g1) / 3
     assert np.abs(g - gfd).max() <= 1e-6 * np.abs(gfd).max() + 1e-9
+
+
+@pytest.mark.parametrize("case", APT_GOLD["apt_analytic"], ids=[c["name"] for c in APT_GOLD["apt_analytic"]])
+def test_apt_matches_reference_analytic_golden(case):
+    """Length-gauge RHF APT of NH3 / 6-31G* (apyib/tests/test_022_RHF_Analytic_APT.py) from
+    analytic gradients in +-field (Richardson over two field steps), to the reference's 1e-6."""
+    from apyib_gb300.gradient import apt
+    P = apt(dict(case["parameters"]))
+    err = np.abs(P - np.array(case["ref"])).max()
+    assert err < case["tol"], (case["name"], err)
