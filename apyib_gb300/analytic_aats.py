@@ -151,6 +151,7 @@ class analytic_derivative(object):
             Y = Cn.T @ (0.5 * L[b].cpu().numpy()) @ Cn           # h^B = i Y (MO)
             self.hB.append(torch.as_tensor(1j * Y).to(C.device))
             rhsB.append(-Y[v, o].reshape(-1))
+        self.Am = Am
         XB = np.linalg.solve(Am, np.stack(rhsB, axis=1))
         self.UB = []
         for b in range(3):

@@ -68,13 +68,13 @@ def cases(kind, rel):
 
 
 def analytic_apt_cases():
-    """The length-gauge analytic APT goldens of apyib/tests/test_022_RHF_Analytic_APT.py
-    (geometry given inside each test); the velocity-gauge ones are a different quantity."""
+    """The length- and velocity-gauge analytic APT goldens of
+    apyib/tests/test_022_RHF_Analytic_APT.py (geometry given inside each test)."""
     rel = "apyib/tests/test_022_RHF_Analytic_APT.py"
     tree = ast.parse(open(os.path.join(REF_ROOT, rel)).read())
     out = []
     for fn in tree.body:
-        if not isinstance(fn, ast.FunctionDef) or not fn.name.endswith("_LG"):
+        if not isinstance(fn, ast.FunctionDef) or not (fn.name.endswith("_LG") or fn.name.endswith("_VG")):
             continue
         local = {n.targets[0].id: n.value.value for n in ast.walk(fn) if isinstance(n, ast.Assign)
                  and isinstance(n.targets[0], ast.Name) and isinstance(n.value, ast.Constant)

@@ -70,9 +70,11 @@ def test_gradient_in_electric_field():
 
 @pytest.mark.parametrize("case", APT_GOLD["apt_analytic"], ids=[c["name"] for c in APT_GOLD["apt_analytic"]])
 def test_apt_matches_reference_analytic_golden(case):
-    """Length-gauge RHF APT of NH3 / 6-31G* (apyib/tests/test_022_RHF_Analytic_APT.py) from
-    analytic gradients in +-field (Richardson over two field steps), to the reference's 1e-6."""
-    from apyib_gb300.gradient import apt
-    P = apt(dict(case["parameters"]))
+    """RHF APTs of NH3 / 6-31G* (apyib/tests/test_022_RHF_Analytic_APT.py): length gauge from
+    analytic gradients in +-field (Richardson over two field steps), velocity gauge from the
+    velocity-operator CPHF response and the determinant overlap derivative; to the reference's 1e-6."""
+    from apyib_gb300.analytic_apts import analytic_derivative
+    ad = analytic_derivative(dict(case["parameters"]))
+    P = ad.compute_RHF_APTs_VG() if case["name"].endswith("_VG") else ad.compute_RHF_APTs_LG()
     err = np.abs(P - np.array(case["ref"])).max()
     assert err < case["tol"], (case["name"], err)
