@@ -249,8 +249,11 @@ class analytic_derivative(object):
         S[1::2, 1::2] = M
         return S
 
-    def _aats(self, method, normalization, precision="fp64", steps=(1e-4,)):
-        self._setup()
+    def _aats(self, method, normalization, precision="fp64", steps=(1e-4,), setup=True):
+        """The AAT tensor; ``setup=False`` reuses the orbital responses already in place
+        (the velocity-gauge APT replaces the magnetic ones)."""
+        if setup:
+            self._setup()
         nso = 2 * self.nbf
         eye = torch.eye(nso, dtype=torch.complex128, device=self.Cc.device)
         Xs = [self._so(U.conj().T + Hr) for U, Hr in zip(self.UR, self.HR)]

@@ -42,12 +42,7 @@ class analytic_derivative(_aat_derivative):
             U[o, v] = 1j * X[:, b].reshape(nv, no).T
             UE.append(torch.as_tensor(U).to(self.Cc.device))
         self.UB, self.hB = UE, hE
-        setup = self._setup
-        self._setup = lambda: None                     # keep the velocity responses in place
-        try:
-            I = self._aats("RHF", "intermediate")
-        finally:
-            self._setup = setup
+        I = self._aats("RHF", "intermediate", setup=False)
         Z = self.H.molecule.Z.astype(float)
         N = np.zeros((3 * len(Z), 3))
         for k in range(3 * len(Z)):
