@@ -59,6 +59,9 @@ SIGNATURES = {
     "agb_last_error": (_c.c_char_p, []),
     "agb_zgemm": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp, _i64,
                          _vp]),
+    "agb_zgemm_scratch_bytes": (_sz, [_i64, _i64, _i64]),
+    "agb_zgemm_ex": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
+                            _i64, _vp, _sz, _vp]),
     "agb_zgemm_df64": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
                               _i64, _vp]),
     "agb_zgemm_df64_scratch_bytes": (_sz, [_i64, _i64, _i64]),

@@ -132,7 +132,7 @@ class _Factors:
             yt = _axis(_axis(y, self.AiT, 0), self.AiT, 1)
             yt = _axis(_axis(yt, self.G, 2), self.G, 3)
             val = 0.25 * X2 * Y2 + torch.sum(Xb * self.F(Yc)) + 0.25 * torch.sum(x * yt)
-        return self.det * complex(val.item())
+        return self.det * val                              # a device scalar: no host round trip per term
 
 
 class AAT(object):
@@ -206,6 +206,13 @@ class AAT(object):
 
     # ------------------------------------------------------------------ normalisation
     def _norm(self, T):
+        key = id(T)
+        cache = self.__dict__.setdefault("_norm_cache", {})
+        if key not in cache:
+            cache[key] = (T, self._norm_value(T))         # T kept alive so that its id stays unique
+        return cache[key][1]
+
+    def _norm_value(self, T):
         t0, t1, t2 = T
         s = t0 ** 2
         if t2 is not None:
@@ -263,32 +270,35 @@ class AAT(object):
             I += self._four(alpha, beta, r, tc, s, t, N)
         return self._pref() * I.imag
 
+    def _term_value(self, alpha, beta, r, s, normalization):
+        return float(self._term(alpha, beta, r, s, normalization))
+
     def compute_SO_I_00(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 0, 0, normalization)
+        return self._term_value(alpha, beta, 0, 0, normalization)
 
     def compute_SO_I_0D(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 0, 2, normalization)
+        return self._term_value(alpha, beta, 0, 2, normalization)
 
     def compute_SO_I_D0(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 2, 0, normalization)
+        return self._term_value(alpha, beta, 2, 0, normalization)
 
     def compute_SO_I_DD(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 2, 2, normalization)
+        return self._term_value(alpha, beta, 2, 2, normalization)
 
     def compute_SO_I_0S(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 0, 1, normalization)
+        return self._term_value(alpha, beta, 0, 1, normalization)
 
     def compute_SO_I_S0(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 1, 0, normalization)
+        return self._term_value(alpha, beta, 1, 0, normalization)
 
     def compute_SO_I_SS(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 1, 1, normalization)
+        return self._term_value(alpha, beta, 1, 1, normalization)
 
     def compute_SO_I_SD(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 1, 2, normalization)
+        return self._term_value(alpha, beta, 1, 2, normalization)
 
     def compute_SO_I_DS(self, alpha, beta, normalization):
-        return self._term(alpha, beta, 2, 1, normalization)
+        return self._term_value(alpha, beta, 2, 1, normalization)
 
     def compute_SO_aats(self, alpha, beta, normalization="full"):
         """apyib/aats.py:520-555: the sum of the terms the method has."""
@@ -297,7 +307,7 @@ class AAT(object):
             terms += [(0, 2), (2, 0), (2, 2)]
         if self.singles:
             terms += [(0, 1), (1, 0), (1, 1), (1, 2), (2, 1)]
-        return sum(self._term(alpha, beta, r, s, normalization) for r, s in terms)
+        return float(sum(self._term(alpha, beta, r, s, normalization) for r, s in terms))
 
     def compute_spatial_aats(self, alpha, beta, normalization="full"):
         """apyib/aats.py:646-1067: the same tensor from closed-shell amplitudes."""

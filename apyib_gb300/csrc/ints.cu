@@ -102,13 +102,18 @@ __device__ __forceinline__ int64_t tri(int64_t k) {   // largest i with i(i+1)/2
   return i;
 }
 
+// One warp per unique Cartesian quartet; its lanes split the primitive quartets
+// (contracted s shells of correlation-consistent bases have 9^4 of them, which a
+// single thread would walk alone while the rest of the grid idles) and the partial
+// sums meet in a fixed shuffle order, so the result is deterministic.
 template <int LM>
-__global__ void eri_kernel(agb_basis b, int64_t nquart, double* __restrict__ out) {
+__global__ void __launch_bounds__(128) eri_kernel(agb_basis b, int64_t nquart, double* __restrict__ out) {
   constexpr int EM = emax(LM), LT = 4 * LM;
   const double two_pi52 = 2.0 * kPi * kPi * sqrt(kPi);
   const int64_t n = b.ncart;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nquart;
-       q += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nquart;
+       q += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t ij = tri(q), kl = q - ij * (ij + 1) / 2;
     const int64_t i = tri(ij), j = ij - i * (i + 1) / 2;
     const int64_t k = tri(kl), l = kl - k * (k + 1) / 2;
@@ -124,9 +129,16 @@ __global__ void eri_kernel(agb_basis b, int64_t nquart, double* __restrict__ out
       m2[c] = p3[c] + p4[c];
     }
     double acc = 0.0;
-    for (int i1 = 0; i1 < f1.np; ++i1) {
-      const double a = b.exps[f1.p0 + i1], ca = b.coefs[f1.p0 + i1];
-      for (int i2 = 0; i2 < f2.np; ++i2) {
+    const int nprim = f1.np * f2.np * f3.np * f4.np;
+    for (int pq = lane; pq < nprim; pq += 32) {
+      int r = pq;
+      const int i4 = r % f4.np;
+      r /= f4.np;
+      const int i3 = r % f3.np;
+      r /= f3.np;
+      const int i2 = r % f2.np, i1 = r / f2.np;
+      {
+        const double a = b.exps[f1.p0 + i1], ca = b.coefs[f1.p0 + i1];
         const double bb = b.exps[f2.p0 + i2], cab = ca * b.coefs[f2.p0 + i2];
         const double p = a + bb;
         double P[3];
@@ -134,9 +146,9 @@ __global__ void eri_kernel(agb_basis b, int64_t nquart, double* __restrict__ out
           P[c] = (a * f1.A[c] + bb * f2.A[c]) / p;
           hermite_e(p1[c], p2[c], a, bb, f1.A[c] - f2.A[c], E1[c]);
         }
-        for (int i3 = 0; i3 < f3.np; ++i3) {
+        {
           const double cx = b.exps[f3.p0 + i3], cc = cab * b.coefs[f3.p0 + i3];
-          for (int i4 = 0; i4 < f4.np; ++i4) {
+          {
             const double d = b.exps[f4.p0 + i4], cabcd = cc * b.coefs[f4.p0 + i4];
             const double qq = cx + d;
             double Q[3];
@@ -166,6 +178,9 @@ __global__ void eri_kernel(agb_basis b, int64_t nquart, double* __restrict__ out
         }
       }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane != 0) continue;
     const int64_t n2 = n * n, n3 = n2 * n;
     out[i * n3 + j * n2 + k * n + l] = acc;
     out[j * n3 + i * n2 + k * n + l] = acc;
@@ -239,7 +254,7 @@ extern "C" agb_status agb_ao_eri(const agb_basis* basis, double* out, void* stre
   const int64_t npair = n * (n + 1) / 2;
   const int64_t nquart = npair * (npair + 1) / 2;
   const int threads = 128;
-  const int grid = agb::grid_for(nquart, threads, 152LL * 16);
+  const int grid = agb::grid_for(nquart * 32, threads, 152LL * 16);
   cudaStream_t st = (cudaStream_t)stream;
   if (basis->lmax <= 1)
     eri_kernel<1><<<grid, threads, 0, st>>>(*basis, nquart, out);

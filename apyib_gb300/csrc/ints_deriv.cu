@@ -189,13 +189,16 @@ __device__ __forceinline__ double eri_sum(const double* const E1[3], const int m
   return s;
 }
 
+// One warp per unique Cartesian quartet, its lanes splitting the primitive quartets
+// (as the ERI kernel); the twelve derivative partials meet in a fixed shuffle order.
 template <int LM>
-__global__ void eri_deriv_kernel(agb_basis b, int64_t nquart, double* __restrict__ out) {
+__global__ void __launch_bounds__(128) eri_deriv_kernel(agb_basis b, int64_t nquart, double* __restrict__ out) {
   constexpr int EM = emax(LM), LT = 4 * LM + 1;
   const double two_pi52 = 2.0 * kPi * kPi * sqrt(kPi);
   const int64_t n = b.ncart, n4 = n * n * n * n;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nquart;
-       q += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nquart;
+       q += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t ij = tri(q), kl = q - ij * (ij + 1) / 2;
     const int64_t i = tri(ij), j = ij - i * (i + 1) / 2;
     const int64_t k = tri(kl), l = kl - k * (k + 1) / 2;
@@ -213,9 +216,16 @@ __global__ void eri_deriv_kernel(agb_basis b, int64_t nquart, double* __restrict
     double d[4][3] = {};
     double E1[3][EM], E2[3][EM], Es[EM];
     double R[rsize(LT)], W[rsize(LT)];
-    for (int i1 = 0; i1 < f[0].np; ++i1) {
+    const int nprim = f[0].np * f[1].np * f[2].np * f[3].np;
+    for (int pq = lane; pq < nprim; pq += 32) {
+      int r = pq;
+      const int i4 = r % f[3].np;
+      r /= f[3].np;
+      const int i3 = r % f[2].np;
+      r /= f[2].np;
+      const int i2 = r % f[1].np, i1 = r / f[1].np;
       const double e0 = b.exps[f[0].p0 + i1], c0 = b.coefs[f[0].p0 + i1];
-      for (int i2 = 0; i2 < f[1].np; ++i2) {
+      {
         const double e1 = b.exps[f[1].p0 + i2], c01 = c0 * b.coefs[f[1].p0 + i2];
         const double p = e0 + e1;
         double P[3];
@@ -223,9 +233,9 @@ __global__ void eri_deriv_kernel(agb_basis b, int64_t nquart, double* __restrict
           P[c] = (e0 * f[0].A[c] + e1 * f[1].A[c]) / p;
           hermite_e(pw[0][c], pw[1][c], e0, e1, f[0].A[c] - f[1].A[c], E1[c]);
         }
-        for (int i3 = 0; i3 < f[2].np; ++i3) {
+        {
           const double e2 = b.exps[f[2].p0 + i3], c012 = c01 * b.coefs[f[2].p0 + i3];
-          for (int i4 = 0; i4 < f[3].np; ++i4) {
+          {
             const double e3 = b.exps[f[3].p0 + i4], cc = c012 * b.coefs[f[3].p0 + i4];
             const double qq = e2 + e3;
             double Q[3];
@@ -274,6 +284,13 @@ __global__ void eri_deriv_kernel(agb_basis b, int64_t nquart, double* __restrict
         }
       }
     }
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d[s][c] += __shfl_xor_sync(0xffffffffu, d[s][c], o);
+    if (lane != 0) continue;
     const int64_t n2 = n * n, n3 = n2 * n;
     const int64_t pos[8] = {i * n3 + j * n2 + k * n + l, j * n3 + i * n2 + k * n + l, i * n3 + j * n2 + l * n + k,
                             j * n3 + i * n2 + l * n + k, k * n3 + l * n2 + i * n + j, l * n3 + k * n2 + i * n + j,
@@ -325,7 +342,7 @@ extern "C" agb_status agb_ao_eri_deriv(const agb_basis* basis, double* out, void
   cudaStream_t st = (cudaStream_t)stream;
   AGB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * n * n * n * n * 3 * basis->natom, st));
   const int threads = 128;
-  const int grid = agb::grid_for(nquart, threads, 152LL * 16);
+  const int grid = agb::grid_for(nquart * 32, threads, 152LL * 16);
   if (basis->lmax <= 1)
     eri_deriv_kernel<1><<<grid, threads, 0, st>>>(*basis, nquart, out);
   else if (basis->lmax == 2)

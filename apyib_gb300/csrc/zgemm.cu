@@ -271,3 +271,20 @@ extern "C" agb_status agb_zgemm(int64_t M, int64_t N, int64_t K, double alpha_re
                     (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
                     (cudaStream_t)stream);
 }
+
+extern "C" size_t agb_zgemm_scratch_bytes(int64_t M, int64_t N, int64_t K) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  const int splits = agb::zgemm_splits(M, N, K, (size_t)-1 / 2);
+  return splits > 1 ? sizeof(agb::z64) * (size_t)splits * (size_t)M * (size_t)N : 0;
+}
+
+extern "C" agb_status agb_zgemm_ex(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im, const void* A,
+                                   int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,
+                                   int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* scratch,
+                                   size_t scratch_bytes, void* stream) {
+  AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  AGB_ARG_CHECK(scratch != nullptr || scratch_bytes == 0, "gemm: scratch is NULL with a nonzero size");
+  return agb::zgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
+                       (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
+                       scratch_bytes ? scratch : nullptr, scratch_bytes, (cudaStream_t)stream);
+}

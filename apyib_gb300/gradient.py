@@ -60,12 +60,42 @@ def nuclear_repulsion_deriv1(mol):
     return g
 
 
-def nuclear_gradient(parameters, precision="fp64", return_parts=False):
+def geometry_integrals(parameters):
+    """The field-independent integrals of an analytic gradient at one geometry: the
+    zero-field Hamiltonian, the AO dipole integrals and the derivative integrals
+    (overlap, core Hamiltonian, dipole, ERI).  A caller that needs gradients at several
+    electric fields (the APT) computes them once and passes them to nuclear_gradient."""
+    from .hamiltonian import Hamiltonian
+    H0 = Hamiltonian(dict(parameters, F_el=[0.0, 0.0, 0.0]))
+    m = MintsHelper(H0.basis_set)
+    return {"H0": H0, "mints": m, "mu": [x.np for x in m.ao_dipole()],
+            "Sd": m.oei_deriv_all(_lib.OEI_OVERLAP),                                   # [natom, 3, n, n]
+            "hd": m.oei_deriv_all(_lib.OEI_KINETIC) + m.oei_deriv_all(_lib.OEI_POTENTIAL),
+            "dmu": m.oei_deriv_all(_lib.OEI_DIPOLE),                                   # [natom, 3, 3, n, n]
+            "Gd": m.eri_deriv_all()}                                                   # [natom, 3, n, n, n, n]
+
+
+def _field_hamiltonian(H0, mu, F_el):
+    """H0 in the uniform electric field F_el, as Hamiltonian(parameters) builds it
+    (apyib/hamiltonian.py:58-68): V - sum_a F_a mu_a and E_nuc(-F)."""
+    import copy
+    H = copy.copy(H0)
+    if any(F_el):
+        H.mu_el = mu
+        V = H0.V
+        for a in range(3):
+            V = V - F_el[a] * mu[a]
+        H.V = V
+    H.E_nuc = H0.molecule.nuclear_repulsion_energy([-f for f in F_el])
+    return H
+
+
+def nuclear_gradient(parameters, precision="fp64", return_parts=False, geometry=None):
     """Analytic dE/dR (natom, 3) of parameters['method'] in RHF, CID_SO, CISD_SO (or the
     spatial CID / CISD, the same energies) at zero magnetic field, in the electric
-    field parameters['F_el'] (real orbitals)."""
+    field parameters['F_el'] (real orbitals).  ``geometry``: geometry_integrals() of the
+    same geometry and basis, to reuse across fields."""
     from .adjoint import mo_coefficient_gradient
-    from .hamiltonian import Hamiltonian
     from .hf_wfn import hf_wfn
 
     method = parameters["method"]
@@ -76,7 +106,8 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
     F_el = [float(f) for f in parameters["F_el"]]
     if method != "RHF" and parameters.get("freeze_core"):
         raise ValueError("analytic correlated gradients are implemented without frozen core")
-    H = Hamiltonian(parameters)
+    geo = geometry if geometry is not None else geometry_integrals(parameters)
+    H = _field_hamiltonian(geo["H0"], geo["mu"], F_el)
     wfn = hf_wfn(H)
     E_scf, C = wfn.solve_SCF(parameters)
     C = _real_orbitals(C)
@@ -84,14 +115,10 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False):
     nbf, no = wfn.nbf, wfn.ndocc
     natom = H.molecule.natom()
     eps = np.asarray(wfn.eps).real
-    m = MintsHelper(H.basis_set)
-    Sd = m.oei_deriv_all(_lib.OEI_OVERLAP)                       # [natom, 3, n, n]
-    hd = m.oei_deriv_all(_lib.OEI_KINETIC) + m.oei_deriv_all(_lib.OEI_POTENTIAL)
-    if any(F_el):                                                # h = T + V - F.mu_el (hamiltonian.py:65-68)
-        dmu = m.oei_deriv_all(_lib.OEI_DIPOLE)                   # [natom, 3, 3, n, n]
-        for beta in range(3):
-            hd = hd - F_el[beta] * dmu[:, :, beta]
-    Gd = m.eri_deriv_all()                                       # [natom, 3, n, n, n, n]
+    Sd, hd, Gd = geo["Sd"], geo["hd"], geo["Gd"]
+    for beta in range(3):                                        # h = T + V - F.mu_el (hamiltonian.py:65-68)
+        if F_el[beta]:
+            hd = hd - F_el[beta] * geo["dmu"][:, :, beta]
     Cd = to_dev(C, torch.float64)
     Co = Cd[:, :no].contiguous()
     Dh = (Co @ Co.T).contiguous()                                # C_o C_o^T
@@ -164,7 +191,10 @@ def apt(parameters, field_step=5e-4, precision="fp64", richardson=True):
     differences over the electric field of analytic nuclear gradients (length gauge):
     six gradient evaluations per field step (one SCF + one CI solve each), twice with
     Richardson extrapolation (steps 2h and h), where the reference's finite-difference
-    APT (apyib/fin_diff.py:151-265) needs 4 x 3N x 3 energies."""
+    APT (apyib/fin_diff.py:151-265) needs 4 x 3N x 3 energies.  The integrals and
+    derivative integrals do not depend on the field and are computed once."""
+    geo = geometry_integrals(parameters)
+
     def central(h):
         cols = []
         for beta in range(3):
@@ -172,7 +202,8 @@ def apt(parameters, field_step=5e-4, precision="fp64", richardson=True):
             for s in (1, -1):
                 F = list(parameters["F_el"])
                 F[beta] += s * h
-                g.append(nuclear_gradient(dict(parameters, F_el=F), precision=precision).reshape(-1))
+                g.append(nuclear_gradient(dict(parameters, F_el=F), precision=precision,
+                                          geometry=geo).reshape(-1))
             cols.append(-(g[0] - g[1]) / (2 * h))
         return np.stack(cols, axis=1)
     if not richardson:

@@ -34,6 +34,14 @@ def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, o
         _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
         del buf
         return out
+    nb = _lib.load().agb_zgemm_scratch_bytes(M, N, K) if M > 0 and N > 0 and K > 0 else 0
+    if nb:                                    # few output tiles, long K: split K across the SMs
+        buf, sp, _ = workspace(nb)
+        _lib.call("agb_zgemm_ex", M, N, K, alpha.real, alpha.imag, ptr(A), sAm, sAk, int(conjA), ptr(B), sBk, sBn,
+                  int(conjB), beta.real, beta.imag, ptr(out), out.stride(0), ctypes.c_void_p(sp), ctypes.c_size_t(nb),
+                  stream_ptr())
+        del buf
+        return out
     _lib.call("agb_zgemm", M, N, K, alpha.real, alpha.imag, ptr(A), sAm, sAk, int(conjA), ptr(B), sBk, sBn,
               int(conjB), beta.real, beta.imag, ptr(out), out.stride(0), stream_ptr())
     return out

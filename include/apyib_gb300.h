@@ -71,6 +71,18 @@ agb_status agb_zgemm(int64_t M, int64_t N, int64_t K, double alpha_re, double al
                      const void* B, int64_t sBk, int64_t sBn, int conjB,
                      double beta_re, double beta_im, void* C, int64_t ldc, void* stream);
 
+/* agb_zgemm with scratch for split-K partial sums: an output of fewer tiles than
+ * the GPU has SMs (e.g. 24 x 24 from K = 24^3 in the back-transformed density
+ * contractions) is computed by up to 256 K-slices whose partials are summed in
+ * slice order (deterministic).  agb_zgemm_scratch_bytes(M,N,K) is the size that
+ * allows every split the heuristic would choose; less scratch, fewer splits. */
+size_t agb_zgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
+agb_status agb_zgemm_ex(int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                        const void* A, int64_t sAm, int64_t sAk, int conjA,
+                        const void* B, int64_t sBk, int64_t sBn, int conjB,
+                        double beta_re, double beta_im, void* C, int64_t ldc,
+                        void* scratch, size_t scratch_bytes, void* stream);
+
 /* Same contraction in double-float arithmetic (each FP64 value split into two
  * floats, exact FMA product splitting, two-sum accumulation; ~2^-44 relative)
  * on the FP32 CUDA cores, which GB300 issues far faster than FP64. */
