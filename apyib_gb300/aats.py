@@ -135,6 +135,80 @@ class _Factors:
         return self.det * val                              # a device scalar: no host round trip per term
 
 
+class _Stack:
+    """The factors of _Factors for a list of overlaps, stacked along a leading axis F,
+    so that the terms of many overlaps run as one set of broadcast batched products.
+    Amplitudes passed to q_all carry a leading axis of length F or 1 (shared)."""
+
+    def __init__(self, Ss, o, f):
+        S = torch.stack([to_dev(x) for x in Ss])
+        A = S[:, :o, :o].cpu().numpy()
+        self.det = torch.as_tensor(np.linalg.det(A)).to(device())               # [F]
+        Ai = torch.as_tensor(np.linalg.inv(A)).to(device())
+        SOV, SVO = S[:, :o, o:], S[:, o:, :o]
+        C = Ai @ SOV                                                            # [F, o, v]
+        B = SVO @ Ai                                                            # [F, v, o]
+        self.G = S[:, o:, o:] - SVO @ C                                         # [F, v, v]
+        self.BT = B[:, :, f:].transpose(1, 2)                                   # [F, o_act, v]
+        self.C = C[:, f:, :]                                                    # [F, o_act, v]
+        self.AiT = Ai[:, f:, f:].transpose(1, 2)                                # [F, o_act, o_act]
+
+    def F(self, u):
+        """A^-T u G^T, u [F or 1, o_act, v]."""
+        return self.AiT @ u @ self.G.transpose(1, 2)
+
+    def q_all(self, pairs, x, y):
+        """{(r, s): det * <bra rank r (amplitudes x[r]) | ket rank s (y[s])>} for the
+        requested rank pairs, each a tensor [F]; x, y: {rank: stacked amplitudes}."""
+        need_r = {r for r, _ in pairs}
+        need_s = {s for _, s in pairs}
+        X1 = X2 = Xb = Y1 = Y2 = Yc = None
+        if 1 in need_r:
+            X1 = (x[1] * self.BT).sum((1, 2))
+        if 2 in need_r:
+            x2 = x[2]
+            Fx, no, _, nv, _ = x2.shape
+            xm = x2.permute(0, 1, 3, 2, 4).reshape(Fx, no * nv, no * nv)            # [(i,a),(j,b)]
+            Xb = (self.BT.reshape(-1, 1, no * nv) @ xm).reshape(-1, no, nv)        # Xb[j,b] = sum_ia x_ijab B_ai
+            X2 = (Xb * self.BT).sum((1, 2))
+        if 1 in need_s:
+            Y1 = (y[1] * self.C).sum((1, 2))
+        if 2 in need_s:
+            y2 = y[2]
+            Fy, no, _, nv, _ = y2.shape
+            ym = y2.permute(0, 2, 4, 1, 3).reshape(Fy, no * nv, no * nv)            # [(l,d),(k,c)]
+            Yc = (self.C.reshape(-1, 1, no * nv) @ ym).reshape(-1, no, nv)         # Yc[k,c] = sum_ld y_klcd C_ld
+            Y2 = (Yc * self.C).sum((1, 2))
+        out = {}
+        for r, s in pairs:
+            if r == 0 and s == 0:
+                val = torch.ones_like(self.det)
+            elif r == 0:
+                val = Y1 if s == 1 else 0.5 * Y2
+            elif s == 0:
+                val = X1 if r == 1 else 0.5 * X2
+            elif r == 1 and s == 1:
+                val = X1 * Y1 + (x[1] * self.F(y[1])).sum((1, 2))
+            elif r == 1 and s == 2:
+                val = 0.5 * X1 * Y2 + (x[1] * self.F(Yc)).sum((1, 2))
+            elif r == 2 and s == 1:
+                val = (Xb * self.F(y[1])).sum((1, 2)) + 0.5 * X2 * Y1
+            else:
+                # x.(A^-T A^-T G G) y = sum_klab (A^-1 A^-1 x)_klab (G G y)_klab: occupied
+                # factors on x, virtual factors on y
+                x2, y2 = x[2], y[2]
+                no, nv = x2.shape[1], x2.shape[3]
+                Ai = self.AiT.transpose(1, 2)
+                xa = (Ai @ x2.reshape(x2.shape[0], no, -1)).reshape(-1, no, no, nv, nv)            # k <- i
+                xa = (Ai @ xa.transpose(1, 2).reshape(xa.shape[0], no, -1)).reshape(-1, no, no, nv, nv)
+                xa = xa.transpose(1, 2)                                                          # [k, l, a, b]
+                ya = (y2.reshape(y2.shape[0], -1, nv) @ self.G.transpose(1, 2)).reshape(-1, no, no, nv, nv)
+                ya = (self.G[:, None] @ ya.reshape(ya.shape[0], no * no, nv, nv)).reshape(-1, no, no, nv, nv)
+                val = 0.25 * X2 * Y2 + (Xb * self.F(Yc)).sum((1, 2)) + 0.25 * (xa * ya).sum((1, 2, 3, 4))
+            out[r, s] = self.det * val
+        return out
+
+
 class AAT(object):
     """apyib/aats.py:19-118 with the same arguments; overlaps on the GPU."""
 
@@ -185,8 +259,7 @@ class AAT(object):
         return self
 
     def _init_common(self, ov, uT, npT, nnT, mpT, mnT, h, b):
-        o, f = 2 * self.ndocc, 2 * self.nfzc
-        self._f = {k: _Factors(S, o, f) for k, S in ov.items()}
+        self._ov = ov
         self.nuc_pert_strength, self.mag_pert_strength = h, b
         method = self.parameters["method"]
         self.spatial = method in ("MP2", "CID", "CISD")
@@ -203,6 +276,14 @@ class AAT(object):
         self.nnT = [amps(T) for T in nnT] if self.doubles else None
         self.mpT = [amps(T) for T in mpT] if self.doubles else None
         self.mnT = [amps(T) for T in mnT] if self.doubles else None
+
+    @property
+    def _f(self):
+        """Per-overlap factors for the element-by-element terms (built on first use)."""
+        if "_factors" not in self.__dict__:
+            o, f = 2 * self.ndocc, 2 * self.nfzc
+            self._factors = {k: _Factors(S, o, f) for k, S in self._ov.items()}
+        return self._factors
 
     # ------------------------------------------------------------------ normalisation
     def _norm(self, T):
@@ -314,9 +395,57 @@ class AAT(object):
         return self.compute_SO_aats(alpha, beta, normalization)
 
     def compute_aat_tensor(self, normalization="full"):
-        """All 3N x 3 elements."""
-        out = np.zeros((3 * self.natom, 3))
-        for a in range(3 * self.natom):
-            for b in range(3):
-                out[a, b] = self.compute_SO_aats(a, b, normalization)
-        return out
+        """All 3N x 3 elements (the sum compute_SO_aats gives for each), every overlap
+        term of every element evaluated at once: the overlaps are stacked and the
+        contractions of the class docstring run as broadcast batched products."""
+        n3 = 3 * self.natom
+        o, f = 2 * self.ndocc, 2 * self.nfzc
+        grid = [(a, b) for a in range(n3) for b in range(3)]
+        pairs = [(0, 0)]
+        if self.doubles:
+            pairs += [(0, 2), (2, 0), (2, 2)]
+        if self.singles:
+            pairs += [(0, 1), (1, 0), (1, 1), (1, 2), (2, 1)]
+        ranks = sorted(({r for r, _ in pairs} | {s for _, s in pairs}) - {0})
+
+        def stack(keys):
+            return _Stack([self._ov[k] for k in keys], o, f)
+
+        def amps(get):
+            """{rank: tensor stacked over the (a, b) grid}."""
+            return {k: torch.stack([get(a, b, k) for a, b in grid]) for k in ranks}
+        N = [self.compute_normalization(a, b, normalization) for a, b in grid]
+        Nu = N[0][0]
+        N_np, N_nn, N_mp, N_mn = (torch.as_tensor(np.array([complex(x[i]) for x in N])).to(device())
+                                  for i in (1, 2, 3, 4))
+        t = {k: self.uT[k][None] for k in ranks}
+        tc = {k: self.uT[k].conj()[None] for k in ranks}
+        # the four displaced/field overlaps of each element, unperturbed amplitudes on both sides
+        q4 = [stack([(kind, a, b) for a, b in grid]).q_all(pairs, tc, t) for kind in ("pp", "pn", "np", "nn")]
+        I = {}
+        for r, s in pairs:
+            I[r, s] = (q4[0][r, s] * N_np * N_mp - q4[1][r, s] * N_np * N_mn
+                       - q4[2][r, s] * N_nn * N_mp + q4[3][r, s] * N_nn * N_mn)
+        if self.doubles:
+            tdH = amps(lambda a, b, k: self.mpT[b][k] - self.mnT[b][k])
+            tdR = amps(lambda a, b, k: (self.npT[a][k] - self.nnT[a][k]).conj())
+            pu, nu = stack([("pu", a) for a, b in grid]), stack([("nu", a) for a, b in grid])
+            up, un = stack([("up", b) for a, b in grid]), stack([("un", b) for a, b in grid])
+            ket = [(r, s) for r, s in pairs if r > 0 and s > 0]
+            qpu = pu.q_all([(0, s) for s in ranks] + ket, tc, tdH)
+            qnu = nu.q_all([(0, s) for s in ranks] + ket, tc, tdH)
+            qup = up.q_all([(r, 0) for r in ranks], tdR, None)
+            qun = un.q_all([(r, 0) for r in ranks], tdR, None)
+            qup.update(up.q_all(ket, tdR, t))
+            qun.update(un.q_all(ket, tdR, t))
+            quu = stack(["uu"]).q_all(ket, tdR, tdH)
+            for r, s in pairs:
+                if r == 0 and s > 0:
+                    I[r, s] = I[r, s] + (qpu[0, s] * N_np - qnu[0, s] * N_nn) * Nu
+                elif s == 0 and r > 0:
+                    I[r, s] = I[r, s] + (qup[r, 0] * N_mp - qun[r, 0] * N_mn) * Nu
+                elif r > 0:
+                    I[r, s] = (I[r, s] + quu[r, s] * Nu * Nu + (qup[r, s] * N_mp - qun[r, s] * N_mn) * Nu
+                               + (qpu[r, s] * N_np - qnu[r, s] * N_nn) * Nu)
+        total = sum(I[rs].imag for rs in pairs) / (4 * self.nuc_pert_strength * self.mag_pert_strength)
+        return total.reshape(n3, 3).cpu().numpy()

@@ -295,7 +295,7 @@ class analytic_derivative(object):
                                   mag_pos_T=[amp(T0, TB[b], 1) for b in range(3)],
                                   mag_neg_T=[amp(T0, TB[b], -1) for b in range(3)],
                                   nuc_pert_strength=eps, mag_pert_strength=eps)
-            out[eps] = np.array([[A.compute_SO_aats(a, b, normalization) for b in range(3)] for a in range(n3)])
+            out[eps] = A.compute_aat_tensor(normalization)
         if len(steps) == 1:
             return out[steps[0]]
         return (4 * out[steps[1]] - out[steps[0]]) / 3

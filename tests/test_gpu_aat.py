@@ -70,6 +70,25 @@ def test_terms_match_reference_determinant_sums(norm):
         assert abs(got - ref) <= 1e-9 * max(1.0, abs(ref)), (a, b, got, ref)
 
 
+@pytest.mark.parametrize("method", ["CISD_SO", "CID_SO", "RHF"])
+@pytest.mark.parametrize("norm", ["full", "intermediate"])
+def test_batched_tensor_matches_terms(norm, method):
+    """compute_aat_tensor (every term of every element at once) against the sum of the
+    reference's term methods at the fixture's element pairs, and against the
+    element-by-element path everywhere."""
+    A = small_case("so", method)
+    full = A.compute_aat_tensor(norm)
+    assert full.shape == (3, 3)
+    for a in range(3):
+        for b in range(3):
+            one = A.compute_SO_aats(a, b, norm)
+            assert abs(full[a, b] - one) <= 1e-10 * max(1.0, abs(one)), (a, b, full[a, b], one)
+    if method == "CISD_SO":
+        for a, b in PAIRS:
+            ref = sum(float(SMALL[f"so_{norm}_{a}_{b}_{name}"]) for name in TERMS)
+            assert abs(full[a, b] - ref) <= 1e-9 * max(1.0, abs(ref)), (a, b, full[a, b], ref)
+
+
 CASES = GOLD["cases"]
 
 
