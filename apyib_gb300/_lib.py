@@ -104,6 +104,8 @@ SIGNATURES = {
     "agb_ao2mo": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _sz, _int, _vp]),
     "agb_jk_fock_scratch_bytes": (_sz, [_i64]),
     "agb_jk_fock": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
+    "agb_jk_fock_sym": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
+    "agb_jk_fock_sym64": (_int, [_vp, _i64, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
     "agb_ao_one_electron": (_int, [_c.POINTER(Basis), _int, _c.POINTER(_d), _vp, _vp]),
     "agb_ao_eri": (_int, [_c.POINTER(Basis), _vp, _vp]),
     "agb_ao_one_electron_deriv": (_int, [_c.POINTER(Basis), _int, _vp, _vp]),

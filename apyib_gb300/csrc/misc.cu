@@ -16,6 +16,10 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
                      const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t dfgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
+agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                     const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
+                     void* scratch, size_t scratch_bytes, cudaStream_t stream);
+size_t ozgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
 
 namespace {
 
@@ -294,6 +298,255 @@ __global__ void __launch_bounds__(512) jk_df_kernel(const double* __restrict__ e
     F[(int64_t)m * n + p] = zmk(hv.x + scale * (2.0 * Jr - Kr), hv.y + scale * (2.0 * Ji - Ki));
   }
 }
+
+// ---- J/K for ERIs symmetric in their last pair, e[m][x][y][z] = e[m][x][z][y] (real AO
+// integrals and their nuclear derivatives are): only z >= y is read.  With S = D + D^T off
+// the diagonal and S[y][y] = D[y][y], each integral read adds
+//   J[m][x] += e S[y][z],   K[m][y] += e D[x][z],   K[m][z] += e D[x][y] (z > y only),
+// the full-tensor sums with the (x, z, y) partner folded in: six double-float multiply-adds
+// per pair of integrals instead of eight, half the splits and half the bytes.  Groups of
+// JK_Y rows of one x as in jk_df_kernel; the lanes own z = 32 c + lane from the chunk that
+// holds the group's first row; the K[z] partials of a group's rows are summed in registers
+// and added to the lane's own slot (Kz, never shared between lanes).  Warps take contiguous
+// group ranges of equal work: groups further down the triangle have fewer chunks.
+__global__ void jk_sym_split_kernel(const z64* __restrict__ D, int n, float4* __restrict__ D4,
+                                    float4* __restrict__ S4) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t y = e / n, z = e % n;
+    const z64 d = D[e];
+    D4[e] = split_z(d);
+    S4[e] = split_z(y == z ? d : zadd(d, D[z * n + y]));
+  }
+}
+
+// Smallest group g whose preceding groups hold at least `target` chunk-units of work.
+__device__ int64_t jk_sym_group_at(int64_t target, int n, int nyb, int nch) {
+  int64_t cum = 0;
+  for (int yb = 0; yb < nyb; ++yb) {
+    const int64_t c = nch - (yb * JK_Y) / 32;
+    if (cum + c * n >= target) return (int64_t)yb * n + (target - cum + c - 1) / c;
+    cum += c * n;
+  }
+  return (int64_t)nyb * n;
+}
+
+__global__ void __launch_bounds__(512) jk_sym_kernel(const double* __restrict__ eri, int n,
+                                                     const float4* __restrict__ D4, const float4* __restrict__ S4,
+                                                     const z64* __restrict__ h, double scale, z64* __restrict__ F) {
+  extern __shared__ float4 jk_sh[];       // Jw, Kw (K[y] per warp), Kz (K[z] per warp): [nw][n] each
+  const int nw = blockDim.x >> 5;
+  float4* Jw = jk_sh;
+  float4* Kw = jk_sh + (size_t)nw * n;
+  float4* Kz = jk_sh + (size_t)2 * nw * n;
+  const int m = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 3 * nw * n; i += blockDim.x) jk_sh[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncthreads();
+  const int nyb = (n + JK_Y - 1) / JK_Y, nch = (n + 31) / 32;
+  int64_t total = 0;
+  for (int yb = 0; yb < nyb; ++yb) total += (int64_t)(nch - (yb * JK_Y) / 32) * n;
+  const int64_t g0 = jk_sym_group_at(total * w / nw, n, nyb, nch);
+  const int64_t g1 = jk_sym_group_at(total * (w + 1) / nw, n, nyb, nch);
+  const double* slab = eri + (int64_t)m * n * n * n;
+  float ks[JK_Y][4];
+#pragma unroll
+  for (int i = 0; i < JK_Y; ++i) ks[i][0] = ks[i][1] = ks[i][2] = ks[i][3] = 0.f;
+  int cur_yb = g0 < g1 ? (int)(g0 / n) : -1;
+  auto flush_k = [&](int yb) {
+#pragma unroll
+    for (int i = 0; i < JK_Y; ++i) {
+      df_warp_sum(ks[i][0], ks[i][1]);
+      df_warp_sum(ks[i][2], ks[i][3]);
+      const int y = yb * JK_Y + i;
+      if (lane == 0 && y < n) {
+        float4 k = Kw[(size_t)w * n + y];
+        df_add(k.x, k.y, ks[i][0], ks[i][1]);
+        df_add(k.z, k.w, ks[i][2], ks[i][3]);
+        Kw[(size_t)w * n + y] = k;
+      }
+      ks[i][0] = ks[i][1] = ks[i][2] = ks[i][3] = 0.f;
+    }
+  };
+  for (int64_t g = g0; g < g1; ++g) {
+    const int yb = (int)(g / n), x = (int)(g % n);
+    if (yb != cur_yb) {
+      flush_k(cur_yb);
+      cur_yb = yb;
+    }
+    const int y0 = yb * JK_Y;
+    // rows past n re-read row n-1 (in bounds) and contribute zero, so every load is unconditional
+    int64_t roff[JK_Y];
+    float4 dxy[JK_Y];
+#pragma unroll
+    for (int i = 0; i < JK_Y; ++i) {
+      roff[i] = (int64_t)min(y0 + i, n - 1);
+      dxy[i] = __ldg(D4 + (int64_t)x * n + roff[i]);
+    }
+    const double* xrows = slab + (int64_t)x * n * n;
+    float jr = 0.f, jrc = 0.f, ji = 0.f, jic = 0.f;
+    for (int c = y0 / 32; c < nch; ++c) {
+      const int z = 32 * c + lane;
+      const int zc = min(z, n - 1);
+      const float4 dxz = __ldg(D4 + (int64_t)x * n + zc);
+      double ev[JK_Y];
+      float4 sv[JK_Y];
+#pragma unroll
+      for (int i = 0; i < JK_Y; ++i) {
+        ev[i] = __ldcs(xrows + roff[i] * n + zc);
+        sv[i] = __ldg(S4 + roff[i] * n + zc);
+      }
+      float kzr = 0.f, kzrc = 0.f, kzi = 0.f, kzic = 0.f;
+#pragma unroll
+      for (int i = 0; i < JK_Y; ++i) {
+        const int y = y0 + i;
+        float eh, el;
+        split_f32pair_fast((z < n && y < n && z >= y) ? ev[i] : 0.0, eh, el);
+        df_mac(jr, jrc, eh, el, sv[i].x, sv[i].y);
+        df_mac(ji, jic, eh, el, sv[i].z, sv[i].w);
+        df_mac(ks[i][0], ks[i][1], eh, el, dxz.x, dxz.y);
+        df_mac(ks[i][2], ks[i][3], eh, el, dxz.z, dxz.w);
+        const bool off = z > y;
+        const float zh = off ? eh : 0.f, zl = off ? el : 0.f;
+        df_mac(kzr, kzrc, zh, zl, dxy[i].x, dxy[i].y);
+        df_mac(kzi, kzic, zh, zl, dxy[i].z, dxy[i].w);
+      }
+      if (z < n) {
+        float4 k = Kz[(size_t)w * n + z];
+        df_add(k.x, k.y, kzr, kzrc);
+        df_add(k.z, k.w, kzi, kzic);
+        Kz[(size_t)w * n + z] = k;
+      }
+    }
+    df_warp_sum(jr, jrc);
+    df_warp_sum(ji, jic);
+    if (lane == 0) {
+      float4 j = Jw[(size_t)w * n + x];
+      df_add(j.x, j.y, jr, jrc);
+      df_add(j.z, j.w, ji, jic);
+      Jw[(size_t)w * n + x] = j;
+    }
+  }
+  if (cur_yb >= 0) flush_k(cur_yb);
+  __syncthreads();
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    double Jr = 0, Ji = 0, Kr = 0, Ki = 0;
+    for (int v = 0; v < nw; ++v) {
+      const float4 j = Jw[(size_t)v * n + p], k = Kw[(size_t)v * n + p], kz = Kz[(size_t)v * n + p];
+      Jr += (double)j.x + (double)j.y; Ji += (double)j.z + (double)j.w;
+      Kr += ((double)k.x + (double)k.y) + ((double)kz.x + (double)kz.y);
+      Ki += ((double)k.z + (double)k.w) + ((double)kz.z + (double)kz.w);
+    }
+    const z64 hv = h ? h[(int64_t)m * n + p] : zmk(0, 0);
+    F[(int64_t)m * n + p] = zmk(hv.x + scale * (2.0 * Jr - Kr), hv.y + scale * (2.0 * Ji - Ki));
+  }
+}
+// ---- The same (l, s)-symmetric J/K in FP64 (the reference's arithmetic): six DFMAs per
+// pair of integrals on the FP64 pipe.  Layout and work split as jk_sym_kernel; the density
+// and S = D + D^T (diagonal D) are read as complex FP64.
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void jk_sym_s_kernel(const z64* __restrict__ D, int n, z64* __restrict__ S) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t y = e / n, z = e % n;
+    S[e] = y == z ? D[e] : zadd(D[e], D[z * n + y]);
+  }
+}
+
+__global__ void __launch_bounds__(512) jk_sym64_kernel(const double* __restrict__ eri, int n,
+                                                       const z64* __restrict__ D, const z64* __restrict__ S,
+                                                       const z64* __restrict__ h, double scale,
+                                                       z64* __restrict__ F) {
+  extern __shared__ z64 jk_sh64[];        // Jw, Kw, Kz: [nw][n] each
+  const int nw = blockDim.x >> 5;
+  z64* Jw = jk_sh64;
+  z64* Kw = jk_sh64 + (size_t)nw * n;
+  z64* Kz = jk_sh64 + (size_t)2 * nw * n;
+  const int m = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 3 * nw * n; i += blockDim.x) jk_sh64[i] = zmk(0, 0);
+  __syncthreads();
+  const int nyb = (n + JK_Y - 1) / JK_Y, nch = (n + 31) / 32;
+  int64_t total = 0;
+  for (int yb = 0; yb < nyb; ++yb) total += (int64_t)(nch - (yb * JK_Y) / 32) * n;
+  const int64_t g0 = jk_sym_group_at(total * w / nw, n, nyb, nch);
+  const int64_t g1 = jk_sym_group_at(total * (w + 1) / nw, n, nyb, nch);
+  const double* slab = eri + (int64_t)m * n * n * n;
+  double ks[JK_Y][2];
+#pragma unroll
+  for (int i = 0; i < JK_Y; ++i) ks[i][0] = ks[i][1] = 0.0;
+  int cur_yb = g0 < g1 ? (int)(g0 / n) : -1;
+  auto flush_k = [&](int yb) {
+#pragma unroll
+    for (int i = 0; i < JK_Y; ++i) {
+      const double kr = warp_sum_d(ks[i][0]), ki = warp_sum_d(ks[i][1]);
+      const int y = yb * JK_Y + i;
+      if (lane == 0 && y < n) Kw[(size_t)w * n + y] = zadd(Kw[(size_t)w * n + y], zmk(kr, ki));
+      ks[i][0] = ks[i][1] = 0.0;
+    }
+  };
+  for (int64_t g = g0; g < g1; ++g) {
+    const int yb = (int)(g / n), x = (int)(g % n);
+    if (yb != cur_yb) {
+      flush_k(cur_yb);
+      cur_yb = yb;
+    }
+    const int y0 = yb * JK_Y;
+    int64_t roff[JK_Y];
+    z64 dxy[JK_Y];
+#pragma unroll
+    for (int i = 0; i < JK_Y; ++i) {
+      roff[i] = (int64_t)min(y0 + i, n - 1);
+      dxy[i] = __ldg(D + (int64_t)x * n + roff[i]);
+    }
+    const double* xrows = slab + (int64_t)x * n * n;
+    double jr = 0.0, ji = 0.0;
+    for (int c = y0 / 32; c < nch; ++c) {
+      const int z = 32 * c + lane;
+      const int zc = min(z, n - 1);
+      const z64 dxz = __ldg(D + (int64_t)x * n + zc);
+      double ev[JK_Y];
+      z64 sv[JK_Y];
+#pragma unroll
+      for (int i = 0; i < JK_Y; ++i) {
+        ev[i] = __ldcs(xrows + roff[i] * n + zc);
+        sv[i] = __ldg(S + roff[i] * n + zc);
+      }
+      double kzr = 0.0, kzi = 0.0;
+#pragma unroll
+      for (int i = 0; i < JK_Y; ++i) {
+        const int y = y0 + i;
+        const double e = (z < n && y < n && z >= y) ? ev[i] : 0.0;
+        jr = fma(e, sv[i].x, jr);
+        ji = fma(e, sv[i].y, ji);
+        ks[i][0] = fma(e, dxz.x, ks[i][0]);
+        ks[i][1] = fma(e, dxz.y, ks[i][1]);
+        const double ez = z > y ? e : 0.0;
+        kzr = fma(ez, dxy[i].x, kzr);
+        kzi = fma(ez, dxy[i].y, kzi);
+      }
+      if (z < n) Kz[(size_t)w * n + z] = zadd(Kz[(size_t)w * n + z], zmk(kzr, kzi));
+    }
+    jr = warp_sum_d(jr);
+    ji = warp_sum_d(ji);
+    if (lane == 0) Jw[(size_t)w * n + x] = zadd(Jw[(size_t)w * n + x], zmk(jr, ji));
+  }
+  if (cur_yb >= 0) flush_k(cur_yb);
+  __syncthreads();
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    double Jr = 0, Ji = 0, Kr = 0, Ki = 0;
+    for (int v = 0; v < nw; ++v) {
+      const z64 j = Jw[(size_t)v * n + p], k = Kw[(size_t)v * n + p], kz = Kz[(size_t)v * n + p];
+      Jr += j.x; Ji += j.y;
+      Kr += k.x + kz.x; Ki += k.y + kz.y;
+    }
+    const z64 hv = h ? h[(int64_t)m * n + p] : zmk(0, 0);
+    F[(int64_t)m * n + p] = zmk(hv.x + scale * (2.0 * Jr - Kr), hv.y + scale * (2.0 * Ji - Ki));
+  }
+}
 }  // namespace
 }  // namespace agb
 
@@ -381,6 +634,7 @@ size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision) {
     size_t need = 0;
     if (precision == AGB_PREC_TF32X3) need = cgemm_tf32x3_scratch(rows[i], nmo, nbf);
     else if (precision == AGB_PREC_DF64) need = dfgemm_scratch_bytes(rows[i], nmo, nbf);
+    else if (precision == AGB_PREC_OZAKI) need = ozgemm_scratch_bytes(rows[i], nmo, nbf);
     if (need > gs) gs = need;
   }
   return 2 * s + sizeof(z64) * (size_t)(nbf * nmo) + 256 + gs + 256;
@@ -394,7 +648,8 @@ size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision) {
 agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t nmo, void* ERI_MO, void* scratch,
                      size_t scratch_bytes, int precision, void* stream) {
   AGB_ARG_CHECK(ERI_AO && C && ERI_MO && nbf > 0 && nmo > 0, "ao2mo: bad argument");
-  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_TF32X3 || precision == AGB_PREC_DF64,
+  AGB_ARG_CHECK(precision == AGB_PREC_FP64 || precision == AGB_PREC_TF32X3 || precision == AGB_PREC_DF64 ||
+                    precision == AGB_PREC_OZAKI,
                 "ao2mo: unknown precision");
   if (!scratch || scratch_bytes < agb_ao2mo_scratch_bytes(nbf, nmo, precision)) {
     agb_set_error_message("ao2mo: scratch too small", __FILE__, __LINE__);
@@ -410,7 +665,8 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
   z64* Cc = (z64*)(base + 2 * s);
   char* gs = base + 2 * s + ((sizeof(z64) * nbf * nmo + 255) & ~(size_t)255);
   size_t gs_bytes = scratch_bytes - (size_t)(gs - (char*)scratch);
-  if (precision == AGB_PREC_TF32X3) AGB_CUDA_TRY(cudaMemsetAsync(gs, 0, 256, st));  // GEMM status word
+  if (precision == AGB_PREC_TF32X3 || precision == AGB_PREC_OZAKI)
+    AGB_CUDA_TRY(cudaMemsetAsync(gs, 0, 256, st));  // GEMM status word
   conj_kernel<<<grid_for(nbf * nmo, 256), 256, 0, st>>>((const z64*)C, nbf * nmo, Cc);
   AGB_LAUNCH_CHECK();
   // out[(rest)][q] = sum_k T[k][(rest)] Cop[k][q]
@@ -420,6 +676,9 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
                           gs_bytes, st);
     if (precision == AGB_PREC_DF64)
       return dfgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
+                       gs_bytes, st);
+    if (precision == AGB_PREC_OZAKI)
+      return ozgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
                        gs_bytes, st);
     return zgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, 0, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs, gs_bytes,
                     st);
@@ -443,7 +702,7 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
   return AGB_OK;
 }
 
-size_t agb_jk_fock_scratch_bytes(int64_t nbf) { return sizeof(float4) * (size_t)nbf * (size_t)nbf + 256; }
+size_t agb_jk_fock_scratch_bytes(int64_t nbf) { return 2 * sizeof(float4) * (size_t)nbf * (size_t)nbf + 512; }
 
 agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale, void* F,
                        void* scratch, size_t scratch_bytes, void* stream) {
@@ -464,6 +723,53 @@ agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const v
   AGB_LAUNCH_CHECK();
   if (sh > 48 * 1024) AGB_CUDA_TRY(cudaFuncSetAttribute(jk_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
   jk_df_kernel<<<(unsigned)nbf, 32 * nw, sh, st>>>(ERI_AO, (int)nbf, D4, (const z64*)h, scale, (z64*)F);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status agb_jk_fock_sym64(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale, void* F,
+                             void* scratch, size_t scratch_bytes, void* stream) {
+  AGB_ARG_CHECK(ERI_AO && D && F && nbf > 0 && nbf < 65536, "jk_fock_sym64: bad argument");
+  if (!scratch || scratch_bytes < agb_jk_fock_scratch_bytes(nbf)) {
+    agb_set_error_message("jk_fock_sym64: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int nw = 16;
+  while (nw > 1 && (size_t)3 * nw * nbf * sizeof(z64) > 200 * 1024) nw >>= 1;
+  const size_t sh = (size_t)3 * nw * nbf * sizeof(z64);
+  AGB_ARG_CHECK(sh <= 200 * 1024, "jk_fock_sym64: nbf too large for the shared J/K slots");
+  z64* S = (z64*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  jk_sym_s_kernel<<<grid_for(nbf * nbf, 256), 256, 0, st>>>((const z64*)D, (int)nbf, S);
+  AGB_LAUNCH_CHECK();
+  if (sh > 48 * 1024)
+    AGB_CUDA_TRY(cudaFuncSetAttribute(jk_sym64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  jk_sym64_kernel<<<(unsigned)nbf, 32 * nw, sh, st>>>(ERI_AO, (int)nbf, (const z64*)D, S, (const z64*)h, scale,
+                                                       (z64*)F);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+
+agb_status agb_jk_fock_sym(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale, void* F,
+                           void* scratch, size_t scratch_bytes, void* stream) {
+  AGB_ARG_CHECK(ERI_AO && D && F && nbf > 0 && nbf < 65536, "jk_fock_sym: bad argument");
+  if (!scratch || scratch_bytes < agb_jk_fock_scratch_bytes(nbf)) {
+    agb_set_error_message("jk_fock_sym: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int nw = 16;
+  while (nw > 1 && (size_t)3 * nw * nbf * sizeof(float4) > 200 * 1024) nw >>= 1;
+  const size_t sh = (size_t)3 * nw * nbf * sizeof(float4);
+  AGB_ARG_CHECK(sh <= 200 * 1024, "jk_fock_sym: nbf too large for the shared J/K slots");
+  const size_t plane = ((sizeof(float4) * (size_t)nbf * nbf) + 255) & ~(size_t)255;
+  float4* D4 = (float4*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  float4* S4 = (float4*)((char*)D4 + plane);
+  jk_sym_split_kernel<<<grid_for(nbf * nbf, 256), 256, 0, st>>>((const z64*)D, (int)nbf, D4, S4);
+  AGB_LAUNCH_CHECK();
+  if (sh > 48 * 1024)
+    AGB_CUDA_TRY(cudaFuncSetAttribute(jk_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  jk_sym_kernel<<<(unsigned)nbf, 32 * nw, sh, st>>>(ERI_AO, (int)nbf, D4, S4, (const z64*)h, scale, (z64*)F);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }

@@ -475,6 +475,7 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
   const z64 coef[3] = {zmk(1, -1), zmk(-1, -1), zmk(0, 1)};
   const bool use_beta = beta.x != 0.0 || beta.y != 0.0;
   for (int part = 0; part < 3; ++part) {
+    if (part == 1 && (conjA == kSrcReal || conjB == kSrcReal)) continue;   // Im.Im of a real operand is zero
     AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, part, L.Mp, eA, fA, sA));
     AGB_STATUS_TRY(slice(B, N, sBn, sBk, conjB, part, L.Np, eB, fB, sB));
     p.coef = zmul(alpha, coef[part]);

@@ -1,8 +1,9 @@
 """Restricted Hartree-Fock with a complex Hermitian core Hamiltonian
 (drop-in for apyib/hf_wfn.py:9-170).
 
-The nbf^4 J/K Fock build runs on the GPU in one pass over the real AO ERIs
-(agb_jk_fock); the orthogonaliser X = S^-1/2, the Hermitian diagonalisation,
+The nbf^4 J/K Fock build runs on the GPU in one pass over the l <= s half of the
+real AO ERIs (agb_jk_fock_sym64: FP64, as the reference's einsum; double-float
+agb_jk_fock_sym when parameters['precision'] is 'mixed'); the orthogonaliser X = S^-1/2, the Hermitian diagonalisation,
 the DIIS bordered solve and the energy/density sums stay FP64 (NumPy/SciPy on
 the host, matrices of size nbf x nbf).
 """
@@ -54,12 +55,14 @@ class hf_wfn(object):
             print(" %02d %20.12f %20.12f %20.12f" % (0, E_SCF.real, E_SCF.imag, E_tot))
         ERI = to_dev(H.ERI, torch.float64)
         Hd = to_dev(H_core)
+        # FP64 J/K (the reference's arithmetic) unless the caller asked for the mixed path
+        jk_precision = "df64" if parameters.get("precision") == "mixed" else "fp64"
         e_iter = F_iter = None
         i = 1
         while i <= parameters["max_iterations"]:
             E_old = E_SCF
             D_old = D
-            F = jk_fock(ERI, to_dev(D), Hd, 0.5).cpu().numpy()
+            F = jk_fock(ERI, to_dev(D), Hd, 0.5, precision=jk_precision).cpu().numpy()
             if parameters["DIIS"]:
                 SDF = S @ D @ F
                 res_vec = np.reshape(X @ (SDF - np.conjugate(SDF.T)) @ X, (-1))

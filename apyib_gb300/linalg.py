@@ -47,8 +47,24 @@ def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, o
     return out
 
 
-def jk_fock(ERI_AO, D, h, scale):
-    """F = h + scale * sum_ls D_ls (2 (mn|ls) - (ml|ns)) (apyib/hf_wfn.py:81, apyib/utils.py:249)."""
+def last_pair_symmetric(eri):
+    """Whether eri[m,n,l,s] == eri[m,n,s,l] exactly, checked once per tensor object and
+    version (the verdict rides on the tensor object; one modified in place is checked
+    again)."""
+    hit = getattr(eri, "_agb_pair_symmetric", None)
+    if hit is not None and hit[0] == eri._version:
+        return hit[1]
+    sym = bool(torch.equal(eri, eri.transpose(2, 3)))
+    eri._agb_pair_symmetric = (eri._version, sym)
+    return sym
+
+
+def jk_fock(ERI_AO, D, h, scale, precision="fp64"):
+    """F = h + scale * sum_ls D_ls (2 (mn|ls) - (ml|ns)) (apyib/hf_wfn.py:81, apyib/utils.py:249).
+    ERIs symmetric in (l, s) (every real AO integral tensor) take a kernel that reads the
+    l <= s half: in FP64 (precision 'fp64', the reference's arithmetic) or in double-float
+    on the FP32 pipe ('df64', ~1e-14 relative).  Any other tensor takes the general
+    double-float kernel."""
     n = D.shape[0]
     eri = ERI_AO.to(device=device(), dtype=torch.float64).contiguous()
     D = D.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
@@ -56,6 +72,12 @@ def jk_fock(ERI_AO, D, h, scale):
     F = torch.empty((n, n), dtype=torch.complex128, device=device())
     nb = _lib.load().agb_jk_fock_scratch_bytes(n)
     buf, sp, _ = workspace(nb)
-    _lib.call("agb_jk_fock", ptr(eri), n, ptr(D), ptr(h), float(scale), ptr(F), ctypes.c_void_p(sp),
-              ctypes.c_size_t(nb), stream_ptr())
+    if precision not in ("fp64", "df64"):
+        raise ValueError(f"jk_fock precision must be 'fp64' or 'df64', not {precision!r}")
+    if last_pair_symmetric(eri):
+        fn = "agb_jk_fock_sym64" if precision == "fp64" else "agb_jk_fock_sym"
+    else:
+        fn = "agb_jk_fock"
+    _lib.call(fn, ptr(eri), n, ptr(D), ptr(h), float(scale), ptr(F), ctypes.c_void_p(sp), ctypes.c_size_t(nb),
+              stream_ptr())
     return F

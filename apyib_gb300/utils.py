@@ -60,7 +60,8 @@ def compute_F_MO(parameters, wfn, C_list, return_torch=False):
 def compute_ERI_MO(parameters, wfn, C_list, return_torch=False, precision=_lib.PREC_FP64):
     """apyib/utils.py:258-279: four quarter-step AO->MO transform (complex C, real AO ERIs).
     precision: _lib.PREC_FP64 (default), PREC_DF64 (double-float GEMMs on the FP32
-    pipe, ~1e-13 relative) or PREC_TF32X3 (tensor cores, ~1e-6 relative)."""
+    pipe, ~1e-13 relative), PREC_OZAKI (FP64-accurate bf16-slice GEMMs on the tensor
+    cores, ~1e-12 of sum |a||b|) or PREC_TF32X3 (tensor cores, ~1e-6 relative)."""
     t = C_list[3]
     C = to_dev(np.asarray(wfn.C)[:, t])
     ERI = to_dev(wfn.H.ERI, torch.float64)

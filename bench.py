@@ -158,7 +158,8 @@ def ao_kernels(nbf, seed=0):
     naux = 3 * nbf
     A = torch.randn(naux, nbf, nbf, generator=g, dtype=torch.float64)
     A = (A + A.transpose(1, 2)) / (2 * (naux * nbf) ** 0.5)
-    eri = torch.einsum("Lmn,Lls->mnls", A.cuda(), A.cuda()).contiguous()
+    eri = torch.einsum("Lmn,Lls->mnls", A.cuda(), A.cuda())
+    eri = (0.5 * (eri + eri.transpose(2, 3))).contiguous()      # exactly symmetric in (l, s), as AO ERIs are
     X = torch.randn(nbf, nbf, generator=g, dtype=torch.complex128)
     C = torch.linalg.qr(X)[0].cuda().contiguous()
     D = (C[:, : nbf // 4] @ C[:, : nbf // 4].conj().T).contiguous()
@@ -185,10 +186,25 @@ def ao_kernels(nbf, seed=0):
     gbs = 8.0 * nbf ** 4 / t / 1e9
     res["jk_fock"] = {"ms": t * 1e3, "eri_GB": 8.0 * nbf ** 4 / 1e9, "achieved_GBps": gbs,
                       "hbm_peak_GBps": peaks["hbm_gbs"], "frac": gbs / peaks["hbm_gbs"]}
+    F_gen = F.clone()
+    t = timed(lambda: _lib.call("agb_jk_fock_sym", ptr(eri), nbf, ptr(D), ptr(h), 1.0, ptr(F), ctypes.c_void_p(jsp),
+                                ctypes.c_size_t(njk), stream_ptr()))
+    gbs = 8.0 * nbf ** 4 / t / 1e9
+    res["jk_fock_sym"] = {"ms": t * 1e3, "eri_GB_read": 4.0 * nbf ** 3 * (nbf + 1) / 1e9, "achieved_GBps": gbs,
+                          "frac": gbs / peaks["hbm_gbs"],
+                          "max_abs_diff_vs_general": (F - F_gen).abs().max().item(),
+                          "note": "ERIs symmetric in (l, s): the l <= s half is read; achieved counts the "
+                                  "full tensor the result depends on (8 nbf^4 B)"}
+    F_df = F.clone()
+    t = timed(lambda: _lib.call("agb_jk_fock_sym64", ptr(eri), nbf, ptr(D), ptr(h), 1.0, ptr(F),
+                                ctypes.c_void_p(jsp), ctypes.c_size_t(njk), stream_ptr()))
+    res["jk_fock_sym64"] = {"ms": t * 1e3, "arith": "fp64 (6 DFMA per pair of integrals)",
+                            "max_abs_diff_vs_df": (F - F_df).abs().max().item()}
     out = torch.empty(nbf, nbf, nbf, nbf, dtype=torch.complex128, device="cuda")
     flops = 2.0 * 2 * nbf ** 5 + 3 * 8.0 * nbf ** 5    # real x complex first step, then three complex steps
     ref = None
-    for name, prec in (("fp64", _lib.PREC_FP64), ("df64", _lib.PREC_DF64), ("tf32x3", _lib.PREC_TF32X3)):
+    for name, prec in (("fp64", _lib.PREC_FP64), ("df64", _lib.PREC_DF64), ("ozaki", _lib.PREC_OZAKI),
+                       ("tf32x3", _lib.PREC_TF32X3)):
         nb = _lib.load().agb_ao2mo_scratch_bytes(nbf, nbf, prec)
         buf, sp, _ = workspace(nb)
         t = timed(lambda: _lib.call("agb_ao2mo", ptr(eri), nbf, ptr(C), nbf, ptr(out), ctypes.c_void_p(sp),
@@ -313,13 +329,14 @@ def water_workloads():
     out["derivatives_zero_field"] = {
         "gradient_analytic_s": t1 - t0, "gradient_fd_s": t3 - t2, "gradient_fd_solves": 18,
         "gradient_max_abs_diff": float(np.abs(g_an - g_fd).max()),
-        "apt_semianalytic_s": t4 - t3, "apt_analytic_gradients": 6, "apt_fd_s": t5 - t4, "apt_fd_energies": 108,
+        "apt_semianalytic_s": t4 - t3, "apt_analytic_gradients": 12, "apt_fd_s": t5 - t4, "apt_fd_energies": 108,
         "apt_max_abs_diff": float(np.abs(P_an - P_fd.real).max()),
         "aat_analytic_s": t7 - t6, "aat_analytic_responses": 12, "aat_fd_s": t8 - t7, "aat_fd_solves": 24,
         "aat_max_abs_diff": float(np.abs(aat_an - aat_fd).max()),
         "note": "water cc-pVDZ CISD_SO, zero field; FD steps 1e-4 bohr (gradient, AAT), 1e-3 bohr / 1e-4 a.u. "
-                "(APT), 1e-4 a.u. (AAT); analytic AAT = one solve, nuclear + magnetic CPHF, 3N+3 amplitude "
-                "responses"}
+                "(APT), 1e-4 a.u. (AAT); semianalytic APT = analytic gradients at +-h, +-2h of each field "
+                "component (Richardson, h = 5e-4 a.u.); analytic AAT = one solve, nuclear + magnetic CPHF, 3N+3 "
+                "amplitude responses"}
     return out
 
 

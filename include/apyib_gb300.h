@@ -24,7 +24,7 @@
  *   agb_cisd_combine               apyib/utils.py:138 + ci_wfn.py:355,361-365
  *   agb_mp2_so                     apyib/mp2_wfn.py:82-85 (solve_MP2_SO)
  *   agb_ao2mo                      apyib/utils.py:274-277 (compute_ERI_MO)
- *   agb_jk_fock                    apyib/hf_wfn.py:81 and apyib/utils.py:241,249
+ *   agb_jk_fock[_sym[64]]          apyib/hf_wfn.py:81 and apyib/utils.py:241,249
  *   agb_ao_one_electron / _eri     psi4 MintsHelper integrals of apyib/hamiltonian.py:32-55
  *                                  (one-electron ones restated in apyib/integrals.py:9-146)
  */
@@ -260,9 +260,10 @@ agb_status agb_mp2_spatial(const void* ERI_MO, int64_t nmo, int64_t no, const do
 /* ERI_MO[p,q,r,s] = sum C*[m,p] C[n,q] C*[l,r] C[s',s] (mn|ls') for real AO ERIs
  * (nbf^4 doubles) and complex C (nbf x nmo), four quarter steps
  * (apyib/utils.py:274-277).  precision: AGB_PREC_FP64 (FP64 pipe),
- * AGB_PREC_DF64 (double-float GEMMs, ~1e-13 relative) or AGB_PREC_TF32X3
- * (tensor cores, ~1e-6 relative).  scratch: agb_ao2mo_scratch_bytes for the
- * same precision. */
+ * AGB_PREC_DF64 (double-float GEMMs, ~1e-13 relative), AGB_PREC_OZAKI (FP64-
+ * accurate bf16-slice GEMMs on the tensor cores, ~1e-12 of sum |a||b|) or
+ * AGB_PREC_TF32X3 (tensor cores, ~1e-6 relative).  scratch:
+ * agb_ao2mo_scratch_bytes for the same precision. */
 size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision);
 agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t nmo, void* ERI_MO,
                      void* scratch, size_t scratch_bytes, int precision, void* stream);
@@ -275,6 +276,15 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
 size_t agb_jk_fock_scratch_bytes(int64_t nbf);
 agb_status agb_jk_fock(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale,
                        void* F, void* scratch, size_t scratch_bytes, void* stream);
+/* agb_jk_fock for ERIs symmetric in their last index pair, (mn|ls) = (mn|sl), as real
+ * AO integrals and their nuclear derivatives are (the caller guarantees it): only
+ * l <= s is read, each integral serving J, K[l] and K[s]; same scratch. */
+agb_status agb_jk_fock_sym(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale,
+                           void* F, void* scratch, size_t scratch_bytes, void* stream);
+/* agb_jk_fock_sym in FP64 arithmetic (six DFMAs per pair of integrals; the precision
+ * of the reference's einsum, for finite differences of energies); same scratch. */
+agb_status agb_jk_fock_sym64(const double* ERI_AO, int64_t nbf, const void* D, const void* h, double scale,
+                             void* F, void* scratch, size_t scratch_bytes, void* stream);
 
 /* ------------------------------------------------------ AO integrals -- */
 

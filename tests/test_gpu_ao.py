@@ -95,10 +95,10 @@ def test_mixed_precision_through_ci_wfn(path):
     assert abs(E - g["E_cid"]) < 1e-9
 
 
-@pytest.mark.parametrize("prec,tol", [(_lib.PREC_DF64, 1e-12), (_lib.PREC_TF32X3, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(_lib.PREC_DF64, 1e-12), (_lib.PREC_OZAKI, 1e-11), (_lib.PREC_TF32X3, 2e-6)])
 def test_transform_precision_modes(prec, tol):
-    """The double-float and 3xTF32 transforms (the first quarter step reads the real
-    AO integrals directly) against the reference's ERI_MO fixture."""
+    """The double-float, Ozaki and 3xTF32 transforms (the first quarter step reads the
+    real AO integrals directly) against the reference's ERI_MO fixture."""
     g = dict(np.load(FILES[0]))
     fc = int(g["nfzc"]) > 0
     wfn = hf_wfn(make(g))

@@ -76,26 +76,45 @@ def test_tf32x3_gemm_alpha_beta_and_transposed_b():
     assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5
 
 
-@pytest.mark.parametrize("n,symmetric", [(1, True), (19, True), (45, True), (70, True), (33, False)])
+@pytest.mark.parametrize("n,symmetric", [(1, True), (2, True), (19, True), (33, True), (45, True), (70, True),
+                                         (33, False)])
 def test_jk_fock_matches_oracle(n, symmetric):
     """Double-float J/K against the FP64 NumPy restatement; n = 45, 70 leave a ragged
-    last block of rows, n = 33 a ragged last lane round, and the non-symmetric case
-    checks that no integral symmetry is assumed."""
+    last block of rows, n = 33 a ragged last lane round.  ERIs symmetric in (l, s) take
+    the half-reading kernel (checked against the general one too); the non-symmetric
+    case checks that no integral symmetry is assumed otherwise."""
+    import ctypes
+
+    from apyib_gb300 import _lib
+    from apyib_gb300.device import ptr, stream_ptr, workspace
+    from apyib_gb300.linalg import last_pair_symmetric
     rng = np.random.default_rng(3 + n)
     if symmetric:
         A = rng.standard_normal((40, n, n))
         A = A + A.transpose(0, 2, 1)
         eri = np.einsum("Lmn,Lls->mnls", A, A) / 40
+        eri = 0.5 * (eri + eri.transpose(0, 1, 3, 2))      # exactly symmetric in (l, s)
     else:
         eri = rng.standard_normal((n, n, n, n))
     D = crandn(rng, n, n)
     h = crandn(rng, n, n)
-    F = jk_fock(to_dev(eri, torch.float64), to_dev(D), to_dev(h), 0.5).cpu().numpy()
+    eri_d = to_dev(eri, torch.float64)
+    assert last_pair_symmetric(eri_d) == symmetric
     ref = port.jk_fock(h, eri, D, 0.5)
     scale = np.abs(eri).max() * np.abs(D).max() * n * n
-    np.testing.assert_allclose(F, ref, atol=1e-13 * scale)
-    F2 = jk_fock(to_dev(eri, torch.float64), to_dev(D), to_dev(h), 0.5).cpu().numpy()
-    np.testing.assert_array_equal(F, F2)        # deterministic
+    for prec, tol in (("fp64", 1e-14), ("df64", 1e-13)):
+        F = jk_fock(eri_d, to_dev(D), to_dev(h), 0.5, precision=prec).cpu().numpy()
+        np.testing.assert_allclose(F, ref, atol=(tol if symmetric else 1e-13) * scale)
+        F2 = jk_fock(eri_d, to_dev(D), to_dev(h), 0.5, precision=prec).cpu().numpy()
+        np.testing.assert_array_equal(F, F2)    # deterministic
+    if symmetric:                               # the general kernel on the same input
+        Fg = torch.empty((n, n), dtype=torch.complex128, device="cuda")
+        nb = _lib.load().agb_jk_fock_scratch_bytes(n)
+        buf, sp, _ = workspace(nb)
+        Dd, hd = to_dev(D), to_dev(h)            # held: the pointers must stay valid
+        _lib.call("agb_jk_fock", ptr(eri_d), n, ptr(Dd), ptr(hd), 0.5, ptr(Fg), ctypes.c_void_p(sp),
+                  ctypes.c_size_t(nb), stream_ptr())
+        np.testing.assert_allclose(F, Fg.cpu().numpy(), atol=1e-13 * scale)
 
 
 def test_so_expansion_matches_oracle():
