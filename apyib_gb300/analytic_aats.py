@@ -16,7 +16,7 @@ U^R (real) and U^B (imaginary) come from the closed-shell CPHF equations
 (nuclear: gradient.py; magnetic: (e_a - e_i) X_ai + sum_bk [(ak|ib) - (ab|ik)] X_bk
 = -Y_ai for U^B = i X, h^B = i Y = (i/2) L in the MO basis, U^B zero within the
 occupied and within the virtual space), t^R and t^B from the amplitude response
-(response.solve_response) with the derivative Hamiltonians in the MO basis
+(response.solve_responses, all perturbations in lockstep) with the derivative Hamiltonians in the MO basis
 (skeleton integrals + U^H F + F U + G[dD], and the U terms of the ERIs).  The
 overlap sums over reference, singly and doubly excited determinants are then the
 Schur-complement contractions of aats.AAT applied to this exactly linearised
@@ -191,7 +191,7 @@ class analytic_derivative(object):
     # ------------------------------------------------------------------ amplitudes and responses
     def _amplitudes(self, singles, precision):
         from .cisd import CISDPlan, solve
-        from .response import solve_response
+        from .response import solve_responses
         from .utils import compute_F_SO
         no, nbf, nf = self.no, self.nbf, self.nfzc
         o, v = 2 * (no - nf), 2 * (nbf - no)
@@ -204,15 +204,25 @@ class analytic_derivative(object):
         plan.blocks_from_mo(self.G[t_, t_, t_, t_].contiguous())
         E, t = solve(plan, P, precision=precision)
 
-        def respond(dF, dG):
+        def perturbed_plan(dF, dG):
             px = CISDPlan(o, v, singles=singles)
             px.set_fock(compute_F_SO(None, dF[t_, t_].contiguous(), return_torch=True), eps_so)
             px.blocks_from_mo(dG[t_, t_, t_, t_].contiguous())
-            return solve_response(plan, px, t, E, P)[1]
-        tR = [respond(*self._dH(self.UR[n], self.skelF[n], self.skelG[n])) for n in range(len(self.UR))]
-        tB = [respond(*self._dH(self.UB[b], hx=self.hB[b])) for b in range(3)]
+            return px
+        pert = [(self.UR[n], dict(skelF=self.skelF[n], skelG=self.skelG[n])) for n in range(len(self.UR))]
+        pert += [(self.UB[b], dict(hx=self.hB[b])) for b in range(3)]
+        # the 3N + 3 responses solved in lockstep, in batches whose plans and DIIS histories
+        # (~25 amplitude vectors each) stay within a quarter of the free device memory
+        per = plan._ws_buf.numel() + 25 * 16 * (plan.n1 + plan.n2)
+        batch = int(max(1, min(len(pert), torch.cuda.mem_get_info()[0] // 4 // per)))
+        tx = []
+        for b0 in range(0, len(pert), batch):
+            pxs = [perturbed_plan(*self._dH(U, **kw)) for U, kw in pert[b0:b0 + batch]]
+            tx += [x for _, x in solve_responses(plan, pxs, t, E, P)]
+            del pxs
         unpack = plan.unpack
-        return unpack(t), [unpack(x) for x in tR], [unpack(x) for x in tB]
+        n3 = len(self.UR)
+        return unpack(t), [unpack(x) for x in tx[:n3]], [unpack(x) for x in tx[n3:]]
 
     def _mp2_amplitudes(self):
         """MP2 first-order amplitudes t = <ab||ij> / (e_i + e_j - e_a - e_b) (apyib/mp2_wfn.py:

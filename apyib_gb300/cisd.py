@@ -125,30 +125,41 @@ class CISDPlan:
         _lib.call("agb_cisd_update", self._h, ptr(t), ptr(r), ptr(o), stream_ptr())
         return o
 
-    def dots(self, x, ys):
+    def dots_into(self, x, ys, out):
+        """conj(y_j) . x (weights 1 and 4 on the singles and packed doubles) into the
+        device tensor out[:len(ys)], without a host round trip."""
         n = len(ys)
+        if n > 16 or out.numel() < n:
+            raise ValueError("dots: at most 16 vectors and an output of at least len(ys)")
         arr = (_vp * n)(*[y.data_ptr() for y in ys])
-        out = self._out3[:n] if n <= 16 else None
         _lib.call("agb_vec_dots", ctypes.c_int64(self.n1), ctypes.c_int64(self.n2), 1.0, 4.0, ptr(x), arr, n,
                   ptr(out), ptr(self._partials), ctypes.c_size_t(self._partials.numel() * 16), stream_ptr())
-        return out.cpu().numpy().copy()
+        return out
 
-    def combine(self, ys, coefs, t_old, t_new):
-        """t_new = sum c_j y_j; returns (E, s1, s2) as complex numbers."""
+    def dots(self, x, ys):
+        return self.dots_into(x, ys, self._out3[:len(ys)]).cpu().numpy().copy()
+
+    def combine_into(self, ys, coefs, t_old, t_new, out3):
+        """t_new = sum c_j y_j with (E, s1, s2) left in the device tensor out3[:3]."""
         n = len(ys)
         arr = (_vp * n)(*[y.data_ptr() for y in ys])
         c = np.zeros(2 * n)
         cc = np.asarray(coefs, dtype=np.complex128)
         c[0::2], c[1::2] = cc.real, cc.imag
         carr = (ctypes.c_double * (2 * n))(*c.tolist())
-        _lib.call("agb_cisd_combine", self._h, arr, carr, n, ptr(t_old), ptr(t_new), ptr(self._out3),
+        _lib.call("agb_cisd_combine", self._h, arr, carr, n, ptr(t_old), ptr(t_new), ptr(out3),
                   ptr(self._partials), ctypes.c_size_t(self._partials.numel() * 16), stream_ptr())
-        h = self._out3[:3].cpu().numpy()
+        return out3
+
+    def combine(self, ys, coefs, t_old, t_new):
+        """t_new = sum c_j y_j; returns (E, s1, s2) as complex numbers."""
+        h = self.combine_into(ys, coefs, t_old, t_new, self._out3)[:3].cpu().numpy()
         return complex(h[0]), complex(h[1]), complex(h[2])
 
     def lincomb(self, ys, coefs, out=None):
+        """sum c_j y_j (no host round trip)."""
         o = self.vec() if out is None else out
-        self.combine(ys, coefs, o if out is not None else ys[0], o)
+        self.combine_into(ys, coefs, o if out is not None else ys[0], o, self._out3)
         return o
 
     def unpack(self, t):

@@ -37,55 +37,115 @@ def solve_response(plan, plan_x, t, E, params, precision="fp64", print_level=0, 
     precision -- 'fp64' (FP64 pipe), 'ozaki' or 'df64' (FP64-accurate GEMMs off the FP64 pipe)
 
     Returns (E^x, t^x) with t^x packed like t."""
-    if plan_x.o != plan.o or plan_x.v != plan.v or plan_x.singles != plan.singles:
-        raise ValueError("plan_x must have the shape of plan")
+    return solve_responses(plan, [plan_x], t, E, params, precision=precision, print_level=print_level,
+                           histories=None if history is None else [history])[0]
+
+
+def solve_responses(plan, plan_xs, t, E, params, precision="fp64", print_level=0, histories=None):
+    """solve_response for several perturbations of one converged problem, in lockstep:
+    each iteration issues every unconverged response's residual, update, DIIS Gram row
+    and extrapolation, and two host round trips serve all of them (the Gram rows, then
+    the energies and step norms).  Each response follows exactly the iteration, DIIS
+    history and convergence test it would follow alone.  Returns [(E^x, t^x), ...]."""
+    for px in plan_xs:
+        if px.o != plan.o or px.v != plan.v or px.singles != plan.singles:
+            raise ValueError("plan_x must have the shape of plan")
     prec = _PREC[precision]
     if prec != _lib.PREC_FP64 and not plan.mixed:
         raise ValueError("FP64-accurate tensor-core / double-float residuals need a mixed plan")
     e_conv, d_conv = params["e_convergence"], params["d_convergence"]
     maxit = params["max_iterations"]
+    use_diis = params["DIIS"]
     singles = plan.singles
-    rx = plan_x.residual(t, 0.0, prec, flags=_lib.RES_CONST)     # c^x + L^x t
-    if prec != _lib.PREC_FP64:
-        plan_x.check_status()
-    Ex_t, _, _ = plan_x.combine([t], [1.0], t, t)                 # sum t EW^x
-    # guess: one Jacobi step from t^x = 0 with E^x = sum t EW^x
-    dt = plan.update(torch.zeros_like(t), plan.lincomb([rx, t], [1.0, -Ex_t]))
-    dE_t, _, _ = plan.combine([dt], [1.0], dt, dt)
-    dE = Ex_t + dE_t
-    diis = _DIIS(plan)
-    first = True
-    it = 1
-    while it <= maxit:
-        dE_old = dE
-        rl = plan.residual(dt, E, prec, flags=_lib.RES_ETERM)     # L t^x - E t^x
+    K = len(plan_xs)
+    if K == 0:
+        return []
+    dev = t.device
+    out = torch.empty((K, 16), dtype=torch.complex128, device=dev)     # (E, s1, s2) per response
+    gram = torch.empty((K, 16), dtype=torch.complex128, device=dev)
+    norms = torch.empty((K, 2), dtype=torch.float64, device=dev)
+    rx = []
+    for k, px in enumerate(plan_xs):
+        rx.append(px.residual(t, 0.0, prec, flags=_lib.RES_CONST))     # c^x + L^x t
         if prec != _lib.PREC_FP64:
-            plan.check_status()
-        R = plan.lincomb([rx, rl, t], [1.0, 1.0, -dE])
-        dt_new = plan.update(dt, R)
-        dt_old = dt.clone()
-        if params["DIIS"]:
-            diis.push(R, dt_new, first)
-            first = False
-            c = diis.coefficients()
-            dE_t, _, _ = plan.combine(diis.t, c, dt, dt)
-        else:
-            dE_t, _, _ = plan.combine([dt_new], [1.0], dt, dt)
-        dE = Ex_t + dE_t
-        # |change| with conjugation: a perturbation such as a magnetic field gives purely
-        # imaginary t^x, whose unconjugated sum of squares is negative and would pass the
-        # reference's real-part comparison at once
-        diff = dt - dt_old
-        rms1 = np.sqrt(float(diff[:plan.n1].abs().pow(2).sum().item()))
-        rms2 = np.sqrt(4.0 * float(diff[plan.n1:].abs().pow(2).sum().item()))
-        ddE = dE_old - dE
-        if history is not None:
-            history.append(dict(iteration=it, dE=dE, delta=ddE, rms_t1=complex(rms1), rms_t2=complex(rms2)))
-        if print_level > 0:
-            print(" %02d %20.12f %20.12f %20.12f %20.12f" % (it, dE.real, ddE.real, rms1.real, rms2.real))
-        if it > 1 and abs(ddE) < e_conv and _lt(rms2, d_conv) and (not singles or _lt(rms1, d_conv)):
-            break
-        if it == maxit:
-            print("Not converged.")
+            px.check_status()
+        px.combine_into([t], [1.0], t, t, out[k])                       # sum t EW^x
+    Ex_t = [complex(x) for x in out[:, 0].cpu().numpy()]
+    # guess: one Jacobi step from t^x = 0 with E^x = sum t EW^x
+    dt = []
+    for k in range(K):
+        d = plan.update(torch.zeros_like(t), plan.lincomb([rx[k], t], [1.0, -Ex_t[k]]))
+        plan.combine_into([d], [1.0], d, d, out[k])
+        dt.append(d)
+    dE = [Ex_t[k] + complex(x) for k, x in enumerate(out[:, 0].cpu().numpy())]
+    diis = [_DIIS(plan) for _ in range(K)]
+    first = [True] * K
+    active = list(range(K))
+    it = 1
+    while it <= maxit and active:
+        dE_old = list(dE)
+        R, dt_new = {}, {}
+        for k in active:
+            rl = plan.residual(dt[k], E, prec, flags=_lib.RES_ETERM)   # L t^x - E t^x
+            if prec != _lib.PREC_FP64:
+                plan.check_status()
+            R[k] = plan.lincomb([rx[k], rl, t], [1.0, 1.0, -dE[k]])
+            dt_new[k] = plan.update(dt[k], R[k])
+            if use_diis:                     # _DIIS.push, its Gram row left on the device
+                h = diis[k]
+                if first[k]:
+                    plan.dots_into(R[k], [R[k]], gram[k])
+                else:
+                    while len(h.e) > h.max:
+                        h.e.pop(0)
+                        h.t.pop(0)
+                        h.B = h.B[1:, 1:]
+                    plan.dots_into(R[k], h.e + [R[k]], gram[k])
+        g = gram.cpu().numpy() if use_diis else None
+        for k in active:
+            if use_diis:
+                h = diis[k]
+                if first[k]:
+                    h.e, h.t = [R[k]], [dt_new[k]]
+                    h.B = np.array([[g[k, 0]]], dtype=np.complex128)
+                    first[k] = False
+                else:
+                    n = len(h.e)
+                    Bn = np.zeros((n + 1, n + 1), dtype=np.complex128)
+                    Bn[:n, :n] = h.B
+                    Bn[:n, n] = g[k, :n]
+                    Bn[n, :n] = np.conj(g[k, :n])
+                    Bn[n, n] = g[k, n]
+                    h.B = Bn
+                    h.e.append(R[k])
+                    h.t.append(dt_new[k])
+                ys, c = h.t, h.coefficients()
+            else:
+                ys, c = [dt_new[k]], [1.0]
+            nxt = plan.vec()
+            plan.combine_into(ys, c, dt[k], nxt, out[k])
+            # |change| with conjugation: a perturbation such as a magnetic field gives purely
+            # imaginary t^x, whose unconjugated sum of squares is negative and would pass the
+            # reference's real-part comparison at once
+            diff = nxt - dt[k]
+            norms[k, 0] = diff[:plan.n1].abs().pow(2).sum()
+            norms[k, 1] = diff[plan.n1:].abs().pow(2).sum()
+            dt[k] = nxt
+        ev = out[:, 0].cpu().numpy()
+        nv = norms.cpu().numpy()
+        for k in list(active):
+            dE[k] = Ex_t[k] + complex(ev[k])
+            rms1 = np.sqrt(float(nv[k, 0]))
+            rms2 = np.sqrt(4.0 * float(nv[k, 1]))
+            ddE = dE_old[k] - dE[k]
+            if histories is not None:
+                histories[k].append(dict(iteration=it, dE=dE[k], delta=ddE, rms_t1=complex(rms1),
+                                         rms_t2=complex(rms2)))
+            if print_level > 0:
+                print(" %02d %20.12f %20.12f %20.12f %20.12f" % (it, dE[k].real, ddE.real, rms1.real, rms2.real))
+            if it > 1 and abs(ddE) < e_conv and _lt(rms2, d_conv) and (not singles or _lt(rms1, d_conv)):
+                active.remove(k)
+            elif it == maxit:
+                print("Not converged.")
         it += 1
-    return dE, dt
+    return [(dE[k], dt[k]) for k in range(K)]

@@ -85,3 +85,34 @@ def test_response_ozaki_matches_fp64():
     dEoz, dtoz = solve_response(plan, plan_x, t, E, P, precision="ozaki")
     assert abs(dE64 - dEoz) < 1e-10 * max(1.0, abs(dE64))
     assert (dt64 - dtoz).abs().max().item() < 1e-9 * max(1.0, dt64.abs().max().item())
+
+
+@pytest.mark.parametrize("diis", [True, False])
+def test_lockstep_responses_match_one_at_a_time(diis):
+    """solve_responses (several perturbations in lockstep, converging at different
+    iterations) gives each response exactly what solve_response gives it alone."""
+    from apyib_gb300.response import solve_responses
+    o, v = 4, 8
+    prob = synthetic.so_factors(o, v, seed=41)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    n = o + v
+    mask = np.add.outer(np.arange(n) % 2, np.arange(n) % 2) % 2 == 0
+    rng = np.random.default_rng(42)
+    B = prob.B
+    plan = make_plan(o, v, prob.fock_so(), chem(B, B), eps_so, True)
+    params = dict(P, DIIS=diis, max_iterations=80)
+    E, t = solve(plan, params)
+    pxs = []
+    for k, s in enumerate((0.05, 0.3, 1.0)):
+        Y = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * s
+        Z = rng.standard_normal(B.shape) + 1j * rng.standard_normal(B.shape)
+        dB = (Z + np.conj(Z.transpose(0, 2, 1))) / 2 * (s / np.sqrt(n * B.shape[0]))
+        pxs.append(make_plan(o, v, (Y + Y.conj().T) * mask, chem(dB, B) + chem(B, dB), eps_so, True))
+    hist_all = [[] for _ in pxs]
+    together = solve_responses(plan, pxs, t, E, params, histories=hist_all)
+    for k, px in enumerate(pxs):
+        hist = []
+        dE, dt = solve_response(plan, px, t, E, params, history=hist)
+        assert len(hist) == len(hist_all[k])
+        assert abs(together[k][0] - dE) <= 1e-14 * max(1.0, abs(dE))
+        assert torch.abs(together[k][1] - dt).max().item() <= 1e-14 * max(1.0, torch.abs(dt).max().item())
