@@ -199,13 +199,16 @@ class analytic_derivative(object):
         eps_so = np.concatenate([np.repeat(eps[nf:no], 2), np.repeat(eps[no:], 2)])
         P = dict(self.parameters)
         t_ = slice(nf, nbf)
-        plan = CISDPlan(o, v, singles=singles)
+        # 'mixed': the amplitudes by the mixed solve and the responses with FP64-accurate
+        # tensor-core / double-float residual GEMMs instead of the FP64 pipe
+        mixed = precision == "mixed"
+        plan = CISDPlan(o, v, singles=singles, mixed=mixed)
         plan.set_fock(compute_F_SO(None, self.F_MO[t_, t_].contiguous(), return_torch=True), eps_so)
         plan.blocks_from_mo(self.G[t_, t_, t_, t_].contiguous())
         E, t = solve(plan, P, precision=precision)
 
         def perturbed_plan(dF, dG):
-            px = CISDPlan(o, v, singles=singles)
+            px = CISDPlan(o, v, singles=singles, mixed=mixed)
             px.set_fock(compute_F_SO(None, dF[t_, t_].contiguous(), return_torch=True), eps_so)
             px.blocks_from_mo(dG[t_, t_, t_, t_].contiguous())
             return px
@@ -218,7 +221,7 @@ class analytic_derivative(object):
         tx = []
         for b0 in range(0, len(pert), batch):
             pxs = [perturbed_plan(*self._dH(U, **kw)) for U, kw in pert[b0:b0 + batch]]
-            tx += [x for _, x in solve_responses(plan, pxs, t, E, P)]
+            tx += [x for _, x in solve_responses(plan, pxs, t, E, P, precision="ozaki" if mixed else "fp64")]
             del pxs
         unpack = plan.unpack
         n3 = len(self.UR)
@@ -317,8 +320,11 @@ class analytic_derivative(object):
     def compute_MP2_AATs(self, normalization="full", orbitals="non-canonical"):
         return self._aats("MP2", normalization)
 
-    def compute_CID_AATs(self, normalization="full", orbitals="non-canonical", print_level=0):
-        return self._aats("CID", normalization)
+    def compute_CID_AATs(self, normalization="full", orbitals="non-canonical", print_level=0, precision="fp64"):
+        """precision 'fp64' (the reference's arithmetic) or 'mixed' (FP64-accurate
+        residual GEMMs off the FP64 pipe for the amplitudes and their responses)."""
+        return self._aats("CID", normalization, precision=precision)
 
-    def compute_CISD_AATs(self, normalization="full", orbitals="non-canonical", print_level=0):
-        return self._aats("CISD", normalization)
+    def compute_CISD_AATs(self, normalization="full", orbitals="non-canonical", print_level=0, precision="fp64"):
+        """precision as compute_CID_AATs."""
+        return self._aats("CISD", normalization, precision=precision)

@@ -317,11 +317,15 @@ def water_workloads():
     t5 = time.perf_counter()
     from apyib_gb300.analytic_aats import analytic_derivative
     analytic_derivative(dict(p0, basis="STO-3G")).compute_CISD_AATs()      # warm-up
+    analytic_derivative(dict(p0, basis="STO-3G")).compute_CISD_AATs(precision="mixed")
     torch.cuda.synchronize()
     t6 = time.perf_counter()
     aat_an = analytic_derivative(p0).compute_CISD_AATs(normalization="full")
     torch.cuda.synchronize()
     t7 = time.perf_counter()
+    aat_mx = analytic_derivative(p0).compute_CISD_AATs(normalization="full", precision="mixed")
+    torch.cuda.synchronize()
+    t7m = time.perf_counter()
     inputs0 = fd0.compute_AAT(1e-4, 1e-4)
     aat_fd = AAT(p0, hf_wfn(Hamiltonian(p0)), C, basis, T_list, *inputs0, 1e-4, 1e-4).compute_aat_tensor("full")
     torch.cuda.synchronize()
@@ -331,7 +335,9 @@ def water_workloads():
         "gradient_max_abs_diff": float(np.abs(g_an - g_fd).max()),
         "apt_semianalytic_s": t4 - t3, "apt_analytic_gradients": 12, "apt_fd_s": t5 - t4, "apt_fd_energies": 108,
         "apt_max_abs_diff": float(np.abs(P_an - P_fd.real).max()),
-        "aat_analytic_s": t7 - t6, "aat_analytic_responses": 12, "aat_fd_s": t8 - t7, "aat_fd_solves": 24,
+        "aat_analytic_s": t7 - t6, "aat_analytic_mixed_s": t7m - t7,
+        "aat_analytic_mixed_max_abs_diff": float(np.abs(aat_mx - aat_an).max()),
+        "aat_analytic_responses": 12, "aat_fd_s": t8 - t7m, "aat_fd_solves": 24,
         "aat_max_abs_diff": float(np.abs(aat_an - aat_fd).max()),
         "note": "water cc-pVDZ CISD_SO, zero field; FD steps 1e-4 bohr (gradient, AAT), 1e-3 bohr / 1e-4 a.u. "
                 "(APT), 1e-4 a.u. (AAT); semianalytic APT = analytic gradients at +-h, +-2h of each field "

@@ -30,3 +30,19 @@ def test_analytic_aat_matches_reference_golden(case):
     ref = np.array(case["ref"])
     err = np.abs(aat - ref).max()
     assert err < case["tol"], (case["name"], err, aat, ref)
+
+
+MIXED = [c for c in CASES if c["parameters"]["method"] in ("CID", "CISD")]
+
+
+@pytest.mark.parametrize("case", MIXED, ids=[c["name"] for c in MIXED])
+def test_analytic_aat_mixed_precision_matches_golden(case):
+    """precision='mixed' (mixed amplitude solve, FP64-accurate tensor-core / double-float
+    residuals for the responses) reproduces the same goldens to the same tolerance."""
+    p = dict(case["parameters"])
+    g = p["geom"]
+    p["geom"] = g["text"] if "text" in g else GOLD["molecules"][g["moldict"]]
+    ad = analytic_derivative(p)
+    aat = getattr(ad, case["call"])(precision="mixed", **case["kwargs"])
+    err = np.abs(aat - np.array(case["ref"])).max()
+    assert err < case["tol"], (case["name"], err)
