@@ -5,7 +5,9 @@ returned as NumPy (like the reference) unless ``return_torch=True``.
 """
 from __future__ import annotations
 
+import collections
 import ctypes
+import hashlib
 
 import numpy as np
 import torch
@@ -123,15 +125,45 @@ def solve_general_DIIS(parameters, res_vec, t_vec, e_iter, t_iter, iteration, mi
     return t_new, e_iter, t_iter
 
 
-def compute_mo_overlap(ndocc, nbf, bra_basis, bra_wfn, ket_basis, ket_wfn, return_torch=False):
-    """apyib/utils.py:370-388: <bra MO p | ket MO q> = C_bra^H S(bra, ket) C_ket, with
-    the AO overlap between two bases (two geometries) on the GPU."""
+_AO_OVERLAPS = collections.OrderedDict()
+
+
+def _basis_fingerprint(bs):
+    """A digest of everything the overlap integrals read from a basis (shell arrays,
+    centres, pure/Cartesian), or None for a basis object without them."""
+    if not hasattr(bs, "flat"):
+        return None
+    h = hashlib.sha1(b"pure" if bs.pure else b"cart")
+    for k, a in sorted(bs.flat().items()):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def _ao_overlap(bra_basis, ket_basis):
+    """<bra AO | ket AO> on the device, kept in a small LRU cache keyed by the two bases'
+    contents: the finite-difference AAT asks for the overlaps of 25 geometries' MOs
+    133 times but for only 19 distinct pairs of geometries (a field moves no nucleus)."""
     from .integrals import MintsHelper
+    key = (_basis_fingerprint(bra_basis), _basis_fingerprint(ket_basis))
+    if None not in key and key in _AO_OVERLAPS:
+        _AO_OVERLAPS.move_to_end(key)
+        return _AO_OVERLAPS[key]
     if bra_basis is ket_basis:
         S = MintsHelper(bra_basis).ao_overlap(return_torch=True)
     else:
         S = MintsHelper(bra_basis).ao_overlap(bra_basis, ket_basis, return_torch=True)
-    S = S.to(torch.complex128)
+    if None not in key:
+        _AO_OVERLAPS[key] = S
+        while len(_AO_OVERLAPS) > 64:
+            _AO_OVERLAPS.popitem(last=False)
+    return S
+
+
+def compute_mo_overlap(ndocc, nbf, bra_basis, bra_wfn, ket_basis, ket_wfn, return_torch=False):
+    """apyib/utils.py:370-388: <bra MO p | ket MO q> = C_bra^H S(bra, ket) C_ket, with
+    the AO overlap between two bases (two geometries) on the GPU."""
+    S = _ao_overlap(bra_basis, ket_basis).to(torch.complex128)
     X = zmm(S, to_dev(ket_wfn))
     out = zmm(to_dev(bra_wfn), X, transA=True, conjA=True)
     return _ret(out, return_torch)
