@@ -175,10 +175,14 @@ class CISDPlan:
         _lib.call("agb_cisd_pack", self._h, ptr(t1), ptr(t2), ptr(t), stream_ptr())
         return t
 
-    def mp2(self):
-        t = self.vec()
-        _lib.call("agb_mp2_so", self._h, ptr(t), ptr(self._out3), ptr(self._partials),
+    def mp2_into(self, t, out):
+        """MP2_SO amplitudes into t and the energy into the device tensor out[0]."""
+        _lib.call("agb_mp2_so", self._h, ptr(t), ptr(out), ptr(self._partials),
                   ctypes.c_size_t(self._partials.numel() * 16), stream_ptr())
+        return t
+
+    def mp2(self):
+        t = self.mp2_into(self.vec(), self._out3)
         return complex(self._out3[0].cpu().numpy()), t
 
 

@@ -346,6 +346,50 @@ def water_workloads():
     return out
 
 
+def hbm_kernels(plan, t, diis, hbm_gbs, reps=5):
+    """The HBM-bound kernels of an iteration at the bench's o/v, each timed alone with
+    CUDA events (mean of `reps` launches after one warm-up) against its algorithmic
+    bytes (complex128 = 16 B per element of the packed amplitude vector, n1 + n2
+    elements): the amplitude update (apyib/ci_wfn.py:336-337) reads t, r and writes
+    t_new (48 B); the DIIS Gram row with the full history (apyib/utils.py:121) reads
+    x and the 8 stored vectors (144 B); the DIIS combination fused with the energy and
+    step norms (apyib/utils.py:138 + ci_wfn.py:355,361-365) reads 8 vectors, t_old and
+    the energy weights and writes t_new (176 B); MP2_SO (apyib/mp2_wfn.py:82-85) reads
+    the packed <ab||ij> and energy weights and writes t2 (48 B per packed doubles
+    element)."""
+    import torch
+    n, n2 = plan.n1 + plan.n2, plan.n2
+    r = t.clone()                                  # any vector of the right length
+    ys = list(diis.t)[:8]
+    ys += [t] * (8 - len(ys))
+    out3 = torch.empty(16, dtype=torch.complex128, device=t.device)
+    tn = torch.empty_like(t)
+    c = [1.0 / len(ys)] * len(ys)
+    cases = {
+        "update": (lambda: plan.update(t, r, out=tn), 48 * n),
+        "diis_gram_row_8": (lambda: plan.dots_into(t, ys, out3), 16 * 9 * n),
+        "diis_combine_8": (lambda: plan.combine_into(ys, c, t, tn, out3), 16 * 11 * n),
+        "mp2_so": (lambda: plan.mp2_into(tn, out3), 48 * n2),
+    }
+    res = {}
+    for name, (fn, nbytes) in cases.items():
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        gbs = nbytes / ms / 1e6
+        res[name] = {"ms": ms, "alg_GB": nbytes / 1e9, "achieved_GBps": gbs, "frac": gbs / hbm_gbs}
+    res["peak_GBps"] = hbm_gbs
+    res["note"] = "CUDA events around each call alone (its reduction tail included), mean of 5, inputs > L2"
+    del r, tn
+    return res
+
+
 def max_over_ranks(x, dist=None):
     """Max of a per-rank scalar over all ranks (identity without a process group)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
@@ -516,6 +560,7 @@ def main():
         "setup_s": setup_s,
     }
 
+    out["hbm_kernels"] = hbm_kernels(plan, state["t"], diis, measured_peaks()[0]["hbm_gbs"])
     del diis, state, host_t, host_out
     torch.cuda.empty_cache()
     if not args.no_solve and rank == 0:
