@@ -291,8 +291,8 @@ __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t 
       if (r >= rows_pad || k >= Kp) continue;
       z64 v = tile[i][tx];
       uint32_t rh, rl, ih, il;
-      split_tf32((uint64_t)__double_as_longlong(v.x), rh, rl);
-      split_tf32((uint64_t)__double_as_longlong(v.y), ih, il);
+      split_tf32_fast((uint32_t)__double2hiint(v.x), (uint32_t)__double2loint(v.x), rh, rl);
+      split_tf32_fast((uint32_t)__double2hiint(v.y), (uint32_t)__double2loint(v.y), ih, il);
       int64_t off = r * Kp + k;
       planes[off] = __uint_as_float(rh);
       planes[plane + off] = __uint_as_float(rl);

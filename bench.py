@@ -537,8 +537,8 @@ def main():
         "metric": METRIC, "value": aggregate_throughput(world, W, dev_ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (3xTF32 tensor core) + c128 (update/DIIS/sums)",
-        "data": "synthetic (seeded Hermitian factors, BASELINE config shape o/v=60/240)",
-        "config": {"workload": "CISD_SO mixed-precision iteration, synthetic o/v=60/240 spin orbitals",
+        "data": f"synthetic (seeded Hermitian factors, o/v={o}/{v}; the headline shape is 60/240)",
+        "config": {"workload": f"CISD_SO mixed-precision iteration, synthetic o/v={o}/{v} spin orbitals",
                    "o": o, "v": v, "naux": 4 * (o + v), "l2": "inputs > L2 (ERI blocks ~45 GB in HBM)",
                    "parallelism": f"replicas x{world}", "alg_flops_per_step": W},
         "e2e": {"value": aggregate_throughput(world, W, e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
@@ -612,7 +612,7 @@ def main():
         out["adjoint"] = {"backward_s": bwd_s, "backward_first_call_s": bwd[0], "fd_solves": 24,
                           "fd_estimate_s": 24 * solve_s,
                           "note": "one density backward vs 24 mixed solves (central differences, 3N+3 = 12 "
-                                  "parameters for H2O), both at o/v=60/240"}
+                                  f"parameters for H2O), both at o/v={o}/{v}"}
         del Dm, Gm, tm, plan
         torch.cuda.empty_cache()
         # Measured FP64-vs-mixed solve comparison where the FP64 solve fits the run: o/v = 40/160.
