@@ -382,6 +382,7 @@ struct VecDims {
   const int2* opairs;
   const int2* vpairs;
   const double* eps;
+  const double* invD;    // 1 / denom_at, stored by agb_cisd_set_fock
 };
 
 __device__ __forceinline__ double denom_at(const VecDims& d, int64_t k) {
@@ -394,11 +395,19 @@ __device__ __forceinline__ double denom_at(const VecDims& d, int64_t k) {
   return d.eps[ij.x] + d.eps[ij.y] - d.eps[d.o + ab.x] - d.eps[d.o + ab.y];
 }
 
+// invD[k] = 1 / D_k, once per set of orbital energies: the pair lookups and the FP64
+// reciprocal (several operations on GB300's narrow FP64 pipe per element) leave the
+// per-iteration update, which then streams t, r and invD at HBM rate.
+__global__ void inv_denom_kernel(VecDims d, int64_t n, double* __restrict__ invD) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    invD[k] = 1.0 / denom_at(d, k);
+}
+
 // t_out = t + r * (1/D), the exact operation numpy performs for complex / real.
 __global__ void update_kernel(VecDims d, int64_t n, const z64* __restrict__ t, const z64* __restrict__ r,
                               z64* __restrict__ t_out) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    double inv = 1.0 / denom_at(d, k);
+    const double inv = d.invD[k];
     z64 rr = r[k], tt = t[k];
     t_out[k] = zmk(tt.x + rr.x * inv, tt.y + rr.y * inv);
   }
@@ -408,7 +417,7 @@ __global__ void update_kernel(VecDims d, int64_t n, const z64* __restrict__ t, c
 __global__ void guess_kernel(VecDims d, int64_t n, const z64* __restrict__ FvoT, const z64* __restrict__ R0p,
                              z64* __restrict__ t) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    double inv = 1.0 / denom_at(d, k);
+    const double inv = d.invD[k];
     z64 num = k < d.n1 ? FvoT[k] : R0p[k - d.n1];
     t[k] = zmk(num.x * inv, num.y * inv);
   }
@@ -596,6 +605,7 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   P->Fvv = (z64*)take(Z * v * v);
   P->EW = (z64*)take(Z * (P->n1 + P->n2));
   P->eps = (double*)take(sizeof(double) * P->nso);
+  P->invD = (double*)take(sizeof(double) * (P->n1 + P->n2));
   P->opairs = (int2*)take(sizeof(int2) * (po > 0 ? po : 1));
   P->vpairs = (int2*)take(sizeof(int2) * (pv > 0 ? pv : 1));
   P->R0p = (z64*)take(Z * po * pv);
@@ -743,7 +753,9 @@ agb_status prepare_static_planes(agb_cisd_plan* P, cudaStream_t st) {
 }
 
 Dims dims_of(const agb_cisd_plan* P) { return Dims{P->o, P->v, P->ov, P->po, P->pv, P->opairs, P->vpairs}; }
-VecDims vdims_of(const agb_cisd_plan* P) { return VecDims{P->o, P->v, P->n1, P->pv, P->opairs, P->vpairs, P->eps}; }
+VecDims vdims_of(const agb_cisd_plan* P) {
+  return VecDims{P->o, P->v, P->n1, P->pv, P->opairs, P->vpairs, P->eps, P->invD};
+}
 
 z64* block_ptr(agb_cisd_plan* P, int id) {
   switch (id) {
@@ -851,6 +863,9 @@ agb_status agb_cisd_set_fock(agb_cisd_plan* P, const void* F_SO, const double* e
   fock_extract_kernel<<<grid_for(nn, 256), 256, 0, st>>>((const z64*)F_SO, eps_so, P->o, P->v,
                                                           P->singles ? P->FvoT : nullptr, P->Foo, P->Fvv,
                                                           P->singles ? P->EW : nullptr, P->eps, flag);
+  AGB_LAUNCH_CHECK();
+  const int64_t n = P->n1 + P->n2;
+  inv_denom_kernel<<<grid_for(n, 256), 256, 0, st>>>(vdims_of(P), n, P->invD);
   AGB_LAUNCH_CHECK();
   int h = 0;
   AGB_CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -12,6 +12,7 @@ struct agb_cisd_plan {
   // ---- static data (complex128 unless noted)
   agb::z64 *FvoT, *Foo, *Fvv, *EW;   // EW = [F_ov (ov) | <ij||ab> packed (n2)]
   double* eps;                        // nso SO orbital energies
+  double* invD;                       // n1 + n2: 1 / D per amplitude (set with the orbital energies)
   int2 *opairs, *vpairs;              // packed pair -> (p,q)
   agb::z64 *R0p;                      // [po][pv] <ab||ij>
   agb::z64 *VT;                       // [(j,b)][(k,c)] <kb||cj>

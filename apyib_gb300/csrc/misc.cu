@@ -89,14 +89,13 @@ __device__ __forceinline__ z64 warp_sum(z64 s) {
 constexpr int kMp2Blocks = 152 * 4;
 
 // t2p = <ab||ij>_p * (1/D), partial[b] = sum t2p * <ij||ab>_p
+// invD2: the plan's 1 / (e_i + e_j - e_a - e_b) of each packed doubles amplitude.
 __global__ void __launch_bounds__(256) mp2_kernel(const z64* __restrict__ R0p, const z64* __restrict__ Wop,
-                                                  const double* __restrict__ eps, const int2* __restrict__ opairs,
-                                                  const int2* __restrict__ vpairs, int o, int64_t pv, int64_t n2,
+                                                  const double* __restrict__ invD2, int64_t n2,
                                                   z64* __restrict__ t2p, z64* __restrict__ partial) {
   z64 acc = zmk(0, 0);
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n2; e += (int64_t)gridDim.x * blockDim.x) {
-    int2 ij = opairs[e / pv], ab = vpairs[e % pv];
-    double inv = 1.0 / (eps[ij.x] + eps[ij.y] - eps[o + ab.x] - eps[o + ab.y]);
+    const double inv = invD2[e];
     z64 num = R0p[e];
     z64 t = zmk(num.x * inv, num.y * inv);
     t2p[e] = t;
@@ -613,7 +612,7 @@ agb_status agb_mp2_so(agb_cisd_plan* P, void* t, void* E_out, void* partials, si
   if (P->n1) {
     AGB_CUDA_TRY(cudaMemsetAsync(t, 0, sizeof(z64) * P->n1, st));
   }
-  mp2_kernel<<<kMp2Blocks, 256, 0, st>>>(P->R0p, P->EW + P->n1, P->eps, P->opairs, P->vpairs, P->o, P->pv, P->n2,
+  mp2_kernel<<<kMp2Blocks, 256, 0, st>>>(P->R0p, P->EW + P->n1, P->invD + P->n1, P->n2,
                                          (z64*)t + P->n1, (z64*)partials);
   AGB_LAUNCH_CHECK();
   sum_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);

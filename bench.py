@@ -505,6 +505,7 @@ def main():
     host_t = torch.empty(plan.n, dtype=torch.complex128, pin_memory=True)
     host_t.copy_(state["t"].cpu())
     host_out = torch.empty(plan.n, dtype=torch.complex128, pin_memory=True)
+    host_out.zero_()                      # both pinned buffers written by the CPU before the timed copies
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
