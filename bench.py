@@ -552,7 +552,7 @@ def main():
                      "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",
                      "frac": (kern_ach / gemm_peak) if kern_ach else None,
                      # DRAM bytes per launch of the same two launches (vvvv ladder, rings) at this size,
-                     # read + written, from one ncu capture of this command (profiles/tf32x3_gemm_traffic_60_240.md)
+                     # read + written, from one ncu capture of this command at this size
                      "traffic": 0.5 * ((46.15 + 0.79) + (53.15 + 3.30)) * 1e9,
                      "traffic_unit": "bytes per launch (mean of the vvvv and ring launches)",
                      "peak_note": f"{peak_kind} bf16 {peaks['bf16_tflops']} TF/s / 2 (tf32 rate) / 3 (3xTF32)",
