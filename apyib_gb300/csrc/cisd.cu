@@ -482,41 +482,55 @@ __device__ __forceinline__ int64_t stride_start(int64_t k0, int64_t stride, int6
 
 // Weighted Gram row: out_j = w(k) sum_k conj(y_j[k]) x[k], w = w1 on the t1 part (k < n1), w2 on t2.
 // Products and running sums in double-float on the FP32 pipe (~2^-44 relative; GB300's FP64
-// pipe would bound this HBM stream), per-thread totals in FP64, fixed reduction order.
+// pipe would bound this HBM stream), fixed reduction order.  Block 0 sums the small t1 part
+// alone and the other blocks the packed doubles, so a thread carries one set of double-float
+// sums (4 floats per vector) and no FP64 totals: fewer registers, more resident warps.
 template <int NY>
 __global__ void __launch_bounds__(256) dots_kernel(DotArgs A, z64* partial) {
-  z64 acc[NY];
+  const bool t1 = blockIdx.x == 0;
+  const int64_t lo = t1 ? 0 : A.n1, hi = t1 ? A.n1 : A.n1 + A.n2;
+  const int64_t stride = (int64_t)(t1 ? 1 : gridDim.x - 1) * blockDim.x;
+  const int64_t k0 = lo + (int64_t)(t1 ? 0 : blockIdx.x - 1) * blockDim.x + threadIdx.x;
+  float s[NY][4];
 #pragma unroll
-  for (int j = 0; j < NY; ++j) acc[j] = zmk(0, 0);
-  const int64_t n = A.n1 + A.n2, stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  for (int part = 0; part < 2; ++part) {
-    float s[NY][4];
-#pragma unroll
-    for (int j = 0; j < NY; ++j) s[j][0] = s[j][1] = s[j][2] = s[j][3] = 0.f;
-    const int64_t hi = part ? n : A.n1;
-    for (int64_t k = stride_start(k0, stride, part ? A.n1 : 0); k < hi; k += stride) {
-      const float4 x = split_z_fast(A.x[k]);
-#pragma unroll
-      for (int j = 0; j < NY; ++j) {
-        if (j < A.ny) {
-          const float4 y = split_z_fast(A.ys[j][k]);
-          // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
-          df_mac(s[j][0], s[j][1], y.x, y.y, x.x, x.y);
-          df_mac(s[j][0], s[j][1], y.z, y.w, x.z, x.w);
-          df_mac(s[j][2], s[j][3], y.x, y.y, x.z, x.w);
-          df_mac(s[j][2], s[j][3], -y.z, -y.w, x.x, x.y);
-        }
-      }
-    }
-    const double w = part ? A.w2 : A.w1;
+  for (int j = 0; j < NY; ++j) s[j][0] = s[j][1] = s[j][2] = s[j][3] = 0.f;
+  for (int64_t k = k0; k < hi; k += stride) {
+    const float4 x = split_z_fast(A.x[k]);
 #pragma unroll
     for (int j = 0; j < NY; ++j) {
-      acc[j].x += w * df_to_double(s[j][0], s[j][1]);
-      acc[j].y += w * df_to_double(s[j][2], s[j][3]);
+      if (j < A.ny) {
+        const float4 y = split_z_fast(A.ys[j][k]);
+        // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
+        df_mac(s[j][0], s[j][1], y.x, y.y, x.x, x.y);
+        df_mac(s[j][0], s[j][1], y.z, y.w, x.z, x.w);
+        df_mac(s[j][2], s[j][3], y.x, y.y, x.z, x.w);
+        df_mac(s[j][2], s[j][3], -y.z, -y.w, x.x, x.y);
+      }
     }
   }
+  const double w = t1 ? A.w1 : A.w2;
+  z64 acc[NY];
+#pragma unroll
+  for (int j = 0; j < NY; ++j) acc[j] = zmk(w * df_to_double(s[j][0], s[j][1]), w * df_to_double(s[j][2], s[j][3]));
   block_reduce_store<NY>(acc, partial);
+}
+
+// The Gram-row kernel for ny vectors (partials [kRedBlocks][nv]); returns nv, the slot stride.
+int launch_dots(const DotArgs& A, int ny, z64* part, cudaStream_t st) {
+  if (ny <= 4) {
+    dots_kernel<4><<<kRedBlocks, 256, 0, st>>>(A, part);
+    return 4;
+  }
+  if (ny <= 8) {
+    dots_kernel<8><<<kRedBlocks, 256, 0, st>>>(A, part);
+    return 8;
+  }
+  if (ny <= 12) {
+    dots_kernel<12><<<kRedBlocks, 256, 0, st>>>(A, part);
+    return 12;
+  }
+  dots_kernel<16><<<kRedBlocks, 256, 0, st>>>(A, part);
+  return 16;
 }
 
 struct CombArgs {
@@ -1070,7 +1084,12 @@ agb_status agb_cisd_guess(agb_cisd_plan* P, void* t, void* stream) {
   return AGB_OK;
 }
 
-size_t agb_vec_partials_bytes(int ny) { return sizeof(z64) * (size_t)kRedBlocks * (ny > 3 ? ny : 3); }
+// Each block stores the full slot width of the kernel instance that serves ny vectors
+// (4, 8, 12 or 16; 3 for the combination's E, s1, s2), not just ny.
+size_t agb_vec_partials_bytes(int ny) {
+  const int nv = ny <= 4 ? 4 : (ny <= 8 ? 8 : (ny <= 12 ? 12 : 16));
+  return sizeof(z64) * (size_t)kRedBlocks * (size_t)(nv > 3 ? nv : 3);
+}
 
 agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x, const void* const* ys, int ny,
                         void* out, void* partials, size_t partials_bytes, void* stream) {
@@ -1084,11 +1103,8 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
   A.n1 = n1; A.n2 = n2; A.w1 = w1; A.w2 = w2; A.x = (const z64*)x; A.ny = ny;
   for (int j = 0; j < kMaxVec; ++j) A.ys[j] = j < ny ? (const z64*)ys[j] : nullptr;
   z64* part = (z64*)partials;
-  if (ny <= 4) dots_kernel<4><<<kRedBlocks, 256, 0, st>>>(A, part);
-  else if (ny <= 8) dots_kernel<8><<<kRedBlocks, 256, 0, st>>>(A, part);
-  else dots_kernel<16><<<kRedBlocks, 256, 0, st>>>(A, part);
+  const int nv = launch_dots(A, ny, part, st);
   AGB_LAUNCH_CHECK();
-  int nv = ny <= 4 ? 4 : (ny <= 8 ? 8 : 16);
   // finish only the first ny of the nv slots (stride nv)
   finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
@@ -1146,11 +1162,8 @@ agb_status agb_vec_dots_noalloc(int64_t n1, int64_t n2, double w1, double w2, co
   // Every partial slot read below is written earlier in this same call, so the
   // array's previous contents never leak into the result.
   z64* part = (z64*)scratch;
-  if (ny <= 4) dots_kernel<4><<<kRedBlocks, 256, 0, st>>>(A, part);
-  else if (ny <= 8) dots_kernel<8><<<kRedBlocks, 256, 0, st>>>(A, part);
-  else dots_kernel<16><<<kRedBlocks, 256, 0, st>>>(A, part);
+  const int nv = launch_dots(A, ny, part, st);
   AGB_LAUNCH_CHECK();
-  int nv = ny <= 4 ? 4 : (ny <= 8 ? 8 : 16);
   finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;

@@ -205,6 +205,9 @@ agb_status agb_cisd_update(agb_cisd_plan* plan, const void* t, const void* r, vo
 agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x,
                         const void* const* ys, int ny, void* out, void* partials, size_t partials_bytes,
                         void* stream);
+/* Bytes of the partials buffer agb_vec_dots needs for ny vectors (each of its
+ * blocks stores the full slot width of the kernel instance serving ny: 4, 8, 12
+ * or 16); agb_cisd_combine needs agb_vec_partials_bytes(3). */
 size_t agb_vec_partials_bytes(int ny);
 
 /* agb_vec_dots without the caller-provided partials buffer.  No counterpart in
