@@ -201,7 +201,9 @@ agb_status agb_cisd_status(agb_cisd_plan* plan, void* stream);
 agb_status agb_cisd_update(agb_cisd_plan* plan, const void* t, const void* r, void* t_out, void* stream);
 
 /* out[j] = w1 * sum_{k<n1} conj(y_j[k]) x[k] + w2 * sum_{k>=n1} conj(y_j[k]) x[k], j < ny <= 16.
- * (DIIS Gram row, apyib/utils.py:121, with w2 = 4 for packed doubles.) */
+ * (DIIS Gram row, apyib/utils.py:121, with w2 = 4 for packed doubles.)  The first part
+ * is summed by a single thread block (it is sized for the singles, n1 = o v): pass a long
+ * vector as the second part. */
 agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x,
                         const void* const* ys, int ny, void* out, void* partials, size_t partials_bytes,
                         void* stream);
