@@ -7,6 +7,8 @@
 // quantity of the reference with full (i,j,a,b) ranges is recovered through
 // the antisymmetry t2[i,j,a,b] = -t2[j,i,a,b] = -t2[i,j,b,a]; the full-vector
 // sums of the reference (energy, DIIS Gram, rms) equal 4x the packed sums.
+#include <cuda.h>
+
 #include <vector>
 #include <string>
 #include <mutex>
@@ -1116,14 +1118,48 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
 // ---------------------------------------------------------------------------
 // agb_vec_dots_noalloc: the DIIS Gram-row reduction for callers that cannot
 // allocate device memory.  Its block partial sums live in the file-scope array
-// below (kRedBlocks x 16 complex doubles = 155,648 bytes), which every device
+// below (kRedBlocks x 16 complex doubles = 155,648 bytes), which every context
 // that loads this library keeps until the process exits.
+//
+// The host-side name of a __device__ array is not a device address: its address
+// is looked up with cudaGetSymbolAddress in the context current at the call and
+// cached under that context's unique id (cuCtxGetId ids are never reused within a
+// process), so a device reset, or a caller that makes its own non-primary context
+// current, gets a fresh lookup instead of a stale pointer.
 namespace {
 constexpr int kNoAllocMaxVec = 16;
 __device__ __align__(256) z64 g_dots_noalloc_scratch[kRedBlocks * kNoAllocMaxVec];
 std::mutex g_noalloc_mu;
-constexpr int kNoAllocMaxDevices = 256;
-void* g_noalloc_scratch_ptr[kNoAllocMaxDevices] = {};
+constexpr size_t kNoAllocMaxContexts = 64;
+std::vector<std::pair<unsigned long long, void*>> g_noalloc_cache;   // (context id, array address)
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current context; false if no context is bound to
+// the thread yet (the runtime binds the device's primary context at its first call that
+// needs one, e.g. cudaGetSymbolAddress) or the driver cannot tell.
+bool current_context_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_cur = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)f;
+    looked_up = true;
+  }
+  if (!get_cur || !get_id) return false;
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
 }  // namespace
 
 extern "C" {
@@ -1136,24 +1172,25 @@ agb_status agb_vec_dots_noalloc(int64_t n1, int64_t n2, double w1, double w2, co
                           "per block)", __FILE__, __LINE__);
     return AGB_ERR_ARG;
   }
-  int dev = 0;
-  AGB_CUDA_TRY(cudaGetDevice(&dev));
-  AGB_ARG_CHECK(dev >= 0 && dev < kNoAllocMaxDevices, "vec_dots_noalloc: device ordinal out of range");
   void* scratch = nullptr;
   {
-    // One-time set-up per device (with that device current): the host-side name of
-    // the array is not a device address, so look the address up and keep it.
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_scratch_ptr[dev]) {
+    unsigned long long ctx_id = 0;
+    if (current_context_id(&ctx_id))
+      for (auto& e : g_noalloc_cache)
+        if (e.first == ctx_id) scratch = e.second;
+    if (!scratch) {
+      // Set-up for this context (its device is current): look the address up once.
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_dots_noalloc_scratch);
       if (e != cudaSuccess || p == nullptr) {
         agb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
         return AGB_ERR_CUDA;
       }
-      g_noalloc_scratch_ptr[dev] = p;
+      scratch = p;
+      if (current_context_id(&ctx_id) && g_noalloc_cache.size() < kNoAllocMaxContexts)
+        g_noalloc_cache.emplace_back(ctx_id, p);
     }
-    scratch = g_noalloc_scratch_ptr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
   DotArgs A;

@@ -72,19 +72,23 @@ __device__ __forceinline__ void split_f32pair(uint64_t u, uint32_t& hi, uint32_t
 
 // Cheap x ~ hi + lo for streamed operands: hi = x truncated to 24 significant bits,
 // lo = the next 23 bits (the last 6 of x's 52 fraction bits dropped), so
-// |x - hi - lo| < 2^-46 |x|.  About 18 integer/FP32 operations and no FP64 instruction.
-// Requires |x| < 2^128; |x| < 2^-126 gives hi = 0 and |x| < 2^-112 gives lo = 0.
+// |x - hi - lo| < 2^-46 |x|.  About 20 integer/FP32 operations and no FP64 instruction.
+// Range: |x| < 2^128 is split as above; |x| >= 2^128 (and inf / NaN) gives hi = +-inf and
+// lo = 0, so a sum fed out-of-range values comes out non-finite instead of plausibly wrong;
+// |x| < 2^-126 gives hi = 0 and |x| < 2^-112 gives lo = 0 (an absolute error below 2^-112).
 __device__ __forceinline__ void split_f32pair_fast(double x, float& hi, float& lo) {
   const uint32_t hw = (uint32_t)__double2hiint(x), lw = (uint32_t)__double2loint(x);
   const uint32_t ex = (hw >> 20) & 0x7ffu;                          // biased FP64 exponent
   const uint32_t sign = hw & 0x80000000u;
   const uint32_t frac23 = __funnelshift_l(lw, hw, 3) & 0x7fffffu;    // top 23 fraction bits
-  hi = __uint_as_float(ex > 896u ? (sign | ((ex - 896u) << 23) | frac23) : sign);
+  const bool big = ex >= 1151u;                                     // |x| >= 2^128: no FP32 exponent
+  hi = __uint_as_float(big ? (sign | 0x7f800000u) : (ex > 896u ? (sign | ((ex - 896u) << 23) | frac23) : sign));
   const uint32_t m = (lw >> 6) & 0x7fffffu;                         // next 23 fraction bits, weight 2^(E-46)
   const float mf = __fsub_rn(__uint_as_float(0x4b000000u | m), 8388608.0f);   // exactly m
   // 2^(E-46) = 2^(E-14) * 2^-32, so the scale factor stays a normal float down to E = -112
-  lo = ex > 910u ? __fmul_rn(__fmul_rn(__uint_as_float(sign | ((ex - 910u) << 23)), mf), 2.3283064365386963e-10f)
-                 : 0.0f;
+  lo = (ex > 910u && !big)
+           ? __fmul_rn(__fmul_rn(__uint_as_float(sign | ((ex - 910u) << 23)), mf), 2.3283064365386963e-10f)
+           : 0.0f;
 }
 
 }  // namespace agb

@@ -84,7 +84,7 @@ def solve_responses(plan, plan_xs, t, E, params, precision="fp64", print_level=0
     it = 1
     while it <= maxit and active:
         dE_old = list(dE)
-        R, dt_new = {}, {}
+        R, dt_new, unconj = {}, {}, {}
         for k in active:
             rl = plan.residual(dt[k], E, prec, flags=_lib.RES_ETERM)   # L t^x - E t^x
             if prec != _lib.PREC_FP64:
@@ -124,15 +124,20 @@ def solve_responses(plan, plan_xs, t, E, params, precision="fp64", print_level=0
                 ys, c = [dt_new[k]], [1.0]
             nxt = plan.vec()
             plan.combine_into(ys, c, dt[k], nxt, out[k])
-            # |change| with conjugation: a perturbation such as a magnetic field gives purely
-            # imaginary t^x, whose unconjugated sum of squares is negative and would pass the
-            # reference's real-part comparison at once
+            # |change| with conjugation, where apyib/analytic_aats.py:868-879 sums the unconjugated
+            # squares: the reference solves its magnetic responses in real arithmetic (the factor i
+            # taken out), while here a magnetic-field perturbation gives purely imaginary t^x, whose
+            # unconjugated sum of squares is negative and would pass the reference's real-part
+            # comparison at every iteration (histories keep both forms)
             diff = nxt - dt[k]
             norms[k, 0] = diff[:plan.n1].abs().pow(2).sum()
             norms[k, 1] = diff[plan.n1:].abs().pow(2).sum()
+            if histories is not None:       # the reference's unconjugated sums, for the record
+                unconj[k] = (diff[:plan.n1].pow(2).sum(), 4.0 * diff[plan.n1:].pow(2).sum())
             dt[k] = nxt
         ev = out[:, 0].cpu().numpy()
         nv = norms.cpu().numpy()
+        uc = {k: (complex(a), complex(b)) for k, (a, b) in unconj.items()}
         for k in list(active):
             dE[k] = Ex_t[k] + complex(ev[k])
             rms1 = np.sqrt(float(nv[k, 0]))
@@ -140,7 +145,9 @@ def solve_responses(plan, plan_xs, t, E, params, precision="fp64", print_level=0
             ddE = dE_old[k] - dE[k]
             if histories is not None:
                 histories[k].append(dict(iteration=it, dE=dE[k], delta=ddE, rms_t1=complex(rms1),
-                                         rms_t2=complex(rms2)))
+                                         rms_t2=complex(rms2),
+                                         rms_t1_unconj=complex(np.sqrt(np.complex128(uc[k][0]))),
+                                         rms_t2_unconj=complex(np.sqrt(np.complex128(uc[k][1])))))
             if print_level > 0:
                 print(" %02d %20.12f %20.12f %20.12f %20.12f" % (it, dE[k].real, ddE.real, rms1.real, rms2.real))
             if it > 1 and abs(ddE) < e_conv and _lt(rms2, d_conv) and (not singles or _lt(rms1, d_conv)):

@@ -13,12 +13,15 @@ W = 8 * (o^2 v^4 / 2 + o^3 v^3 + o^4 v^2 / 2 + 5 o^2 v^3 + 5 o^3 v^2) flops
 
 Also reported (measured once per run, outside the timed steps): the full
 mixed-precision solve (3xTF32 iterations, one FP64-accurate base residual with
-Ozaki-split bf16 tensor-core GEMMs, defect
-correction) to the reference's convergence test, the FP64 residual time, the
-FP64 residual norm at the mixed solution (a-posteriori check), and the
-reference-path CPU time (the NumPy oracle) on a bounded sample.
+Ozaki-split bf16 tensor-core GEMMs, defect correction) to the reference's
+convergence test; the plain FP64 GPU solve of the same problem to the same test
+(wall time, |dE| and the largest amplitude difference between the two); the
+FP64 residual norm at the mixed solution (a-posteriori check); the same
+comparison at o/v = 40/160; and the reference path's CPU rate (the NumPy oracle
+on the host cores) on a bounded sample of this workload (``cpu_residual_sample``).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+       python bench.py --profile gemm|jk|hbm ...   (one kernel on a small case)
 Multi-GPU: replicas only (each rank solves its own copy; no collective on the
 data path); value = sum of per-rank work / max rank time.
 """
@@ -98,48 +101,106 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline_oracle(budget_s=12.0, o=20, v=80):
-    """The NumPy oracle (restatement of apyib/ci_wfn.py:309-334) timed on the host cores."""
-    import importlib
+def host_info():
     ncores = len(os.sched_getaffinity(0))
+    try:
+        ram = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES") / 1e9
+    except (ValueError, OSError):
+        ram = None
+    return ncores, ram
+
+
+# Virtual rows per CPU sample step: about 1/120 (60/240) and 1/40 (40/160) of a residual.
+SAMPLE_ROWS = {(60, 240): 2, (40, 160): 4}
+
+
+def cpu_residual_sample(o, v, steps, warmup=1, rows=None, seed=0):
+    """The reference path's residual (the NumPy oracle's restatement of
+    apyib/ci_wfn.py:309-334, opt_einsum-style full-tensor contractions) timed on the
+    host cores at o/v on a bounded sample: each step evaluates the residual rows of
+    ``rows`` virtual indices a (r1[:, a], r2[:, :, a, :]), every einsum of the
+    reference restricted to those output rows with its full contraction lengths, so
+    a step does rows / v of the residual's work on the workload's own shapes.  The
+    integral blocks are the seeded synthetic problem's (vvvv, vovv, vvvo, vvoo for the
+    sampled rows; ovvo, ooov, ovoo, oooo in full) and the amplitudes those of the first
+    iteration (t1 = 0, t2 = <ab||ij> / D), all built before the timed steps, as are the
+    full-size operands' relayouts (``oracle.port.vslab_layouts``): the reference's
+    einsums copy them once per term and residual, which the sample cannot scale, so the
+    implied full-residual time leaves those copies out and favours the CPU.
+    Returns per-step seconds and a description."""
+    import importlib
+    ncores, ram = host_info()
     for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ.setdefault(k, str(ncores))
     port = importlib.import_module("oracle.port")
     from apyib_gb300 import synthetic
-    prob = synthetic.so_factors(o, v, seed=0)
-    blk = port.blocks_from_factors(prob.B, o)
+    rows = rows or SAMPLE_ROWS.get((o, v), max(1, v // 120))
+    prob = synthetic.so_factors(o, v, seed=seed)
     F = prob.fock_so()
+    t_set = time.perf_counter()
+    blk = port.vslab_blocks_from_factors(prob.B, o, 0, rows)
+    # amplitudes of the first iteration: t1 = 0, t2 = <ab||ij> / D (full o, o, v, v)
     D_ia, D_ijab = port.so_denominators(prob.eps_o, prob.eps_v)
+    step_v = 16
+    vvoo = np.concatenate([port.vslab_blocks_from_factors(prob.B, o, b0, min(v, b0 + step_v), names=("vvoo",))["vvoo"]
+                           for b0 in range(0, v, step_v)])
+    t2 = vvoo.transpose(2, 3, 0, 1) / D_ijab
     t1 = np.zeros((o, v), dtype=complex)
-    t2 = blk["vvoo"].transpose(2, 3, 0, 1) / D_ijab
-    port.cisd_so_residual(F, blk, t1, t2, 0.1, o)       # warm-up
-    n, t0 = 0, time.perf_counter()
-    while True:
-        port.cisd_so_residual(F, blk, t1, t2, 0.1, o)
-        n += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = (time.perf_counter() - t0) / n
-    return {"value": alg_flops(o, v) / dt / 1e12, "unit": "TFLOP/s", "cores": ncores, "kind": "port",
-            "sample": f"{n} CISD_SO residual evaluations of the NumPy oracle at o/v={o}/{v} "
-                      f"({dt:.3f} s each); the o/v=60/240 workload does not fit host RAM in NumPy"}
+    del vvoo, D_ijab, prob
+    lay = port.vslab_layouts(blk, t2)
+    setup_s = time.perf_counter() - t_set
+    times = []
+    for step in range(warmup + steps):
+        c0 = time.perf_counter()
+        port.cisd_so_residual_vslab(F, blk, t1, t2, 0.1, o, 0, rows, lay=lay)
+        dt = time.perf_counter() - c0
+        if step >= warmup:
+            times.append(dt)
+    frac = rows / v
+    return {"step_s": times, "rows": rows, "fraction": frac, "cores": ncores, "host_ram_GB": ram,
+            "setup_s": setup_s,
+            "sample": f"residual rows of {rows} of {v} virtual indices per step (every reference einsum of "
+                      f"apyib/ci_wfn.py:309-334 restricted to them, full contraction lengths, operand relayouts "
+                      f"done once before timing; {frac:.4f} of the residual's work) at o/v={o}/{v}, NumPy oracle "
+                      f"port, {ncores} host cores; value = algorithmic flops / (step time / {frac:.4f})"}
+
+
+def cpu_baseline_oracle(o=60, v=240, steps=3):
+    """CPU baseline of the bench line: ``cpu_residual_sample`` at the bench's o/v."""
+    r = cpu_residual_sample(o, v, steps)
+    dt = float(np.mean(r["step_s"]))
+    full_s = dt / r["fraction"]
+    return {"value": alg_flops(o, v) / full_s / 1e12, "unit": "TFLOP/s", "cores": r["cores"], "kind": "port",
+            "sample": r["sample"] + f"; {dt:.2f} s per step",
+            "full_residual_s_from_sample": full_s, "host_ram_GB": r["host_ram_GB"], "setup_s": r["setup_s"]}
+
+
+def bench_config(o, v, world):
+    return {"workload": f"CISD_SO mixed-precision iteration, synthetic o/v={o}/{v} spin orbitals",
+            "o": o, "v": v, "naux": 4 * (o + v), "l2": "inputs > L2 (ERI blocks ~45 GB in HBM)",
+            "parallelism": f"replicas x{world}", "alg_flops_per_step": alg_flops(o, v)}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference path on the host cores (the NumPy oracle's
+    restatement, as the reference itself is Python that imports psi4 at module
+    level), on this bench's workload and metric; each step is one bounded sample
+    (``cpu_residual_sample``) and its value the residual's algorithmic flops over the
+    time of a full residual implied by the sample.  Rank 0 only."""
     if rank != 0:
         return 0
-    res = []
-    cb = None
-    for i in range(args.warmup + args.steps):
-        cb = cpu_baseline_oracle(budget_s=3.0)
-        if i >= args.warmup:
-            res.append(cb["value"])
-    val = float(np.mean(res))
+    o, v = args.o, args.v
+    r = cpu_residual_sample(o, v, args.steps, warmup=args.warmup)
+    step_s = float(np.mean(r["step_s"]))
+    full_s = step_s / r["fraction"]
+    val = alg_flops(o, v) / full_s / 1e12
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": "CISD_SO residual, NumPy oracle (CPU)", "o": 20, "v": 80},
-            "cpu_baseline": dict(cb, value=val),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": bench_config(o, v, world),
+            "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"], "full_residual_s_from_sample": full_s,
+                             "host_ram_GB": r["host_ram_GB"], "setup_s": r["setup_s"]},
             "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -390,6 +451,42 @@ def hbm_kernels(plan, t, diis, hbm_gbs, reps=5):
     return res
 
 
+def mixed_iteration(plan):
+    """One mixed-precision CISD_SO iteration as the bench times it: 3xTF32 residual,
+    FP64 update, DIIS push (Gram row) and the FP64 extrapolation with energy and norms."""
+    from apyib_gb300 import _lib
+    from apyib_gb300.cisd import _DIIS
+    t = plan.guess()
+    E, _, _ = plan.combine([t], [1.0], t, t)
+    diis = _DIIS(plan)
+    state = {"t": t, "E": E, "first": True}
+
+    def iteration():
+        r = plan.residual(state["t"], state["E"], _lib.PREC_TF32X3)
+        tn = plan.update(state["t"], r)
+        diis.push(r, tn, state["first"])
+        state["first"] = False
+        c = diis.coefficients()
+        E, s1, s2 = plan.combine(diis.t, c, state["t"], state["t"])
+        state["E"] = E
+        return E
+    return iteration, state, diis
+
+
+def timed_iterations(iteration, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        iteration()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        iteration()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def max_over_ranks(x, dist=None):
     """Max of a per-rank scalar over all ranks (identity without a process group)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
@@ -406,6 +503,122 @@ def aggregate_throughput(world, work_per_rank, max_seconds):
     return world * work_per_rank / max_seconds
 
 
+def profile_kernel(spec):
+    """One kernel on a small case, for timing and for an ncu capture (``--profile``):
+
+        gemm M N K [tf32x3|df64|oz|fp64]   complex GEMM, A [M,K], B used transposed [N,K]
+        jk NBF REPS [sym|sym64|general]    J/K Fock build over seeded real AO integrals
+        hbm O V                            the amplitude update, DIIS Gram row (8 vectors),
+                                           DIIS combination (8 vectors) and MP2_SO of a mixed
+                                           plan at o/v spin orbitals
+
+    Each case runs twice untimed, then once (gemm) or REPS / 3 times under CUDA events,
+    and prints one line."""
+    import ctypes
+
+    import torch
+
+    from apyib_gb300 import _lib
+    from apyib_gb300.device import ptr, stream_ptr, workspace
+    torch.cuda.set_device(0)
+    kind, args = spec[0], spec[1:]
+    if kind == "gemm":
+        M, N, K = (int(a) for a in args[:3])
+        prec = args[3] if len(args) > 3 else "tf32x3"
+        g = torch.Generator(device="cuda").manual_seed(0)
+        A = torch.randn(M, K, dtype=torch.complex128, device="cuda", generator=g)
+        B = torch.randn(N, K, dtype=torch.complex128, device="cuda", generator=g)
+        C = torch.zeros(M, N, dtype=torch.complex128, device="cuda")
+        size_fn = {"tf32x3": "agb_cgemm_tf32x3_scratch_bytes", "df64": "agb_zgemm_df64_scratch_bytes",
+                   "oz": "agb_zgemm_oz_scratch_bytes"}.get(prec)
+        nb = getattr(_lib.load(), size_fn)(M, N, K) if size_fn else 256
+        buf, sp, _ = workspace(nb)
+        buf.zero_()
+        entry = {"tf32x3": "agb_cgemm_tf32x3", "df64": "agb_zgemm_df64_ex", "oz": "agb_zgemm_oz"}.get(prec)
+
+        def run():
+            if entry:
+                _lib.call(entry, M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
+                          ctypes.c_void_p(sp), ctypes.c_size_t(nb), stream_ptr())
+            else:
+                _lib.call("agb_zgemm", M, N, K, 1.0, 0.0, ptr(A), K, 1, 0, ptr(B), 1, K, 0, 0.0, 0.0, ptr(C), N,
+                          stream_ptr())
+        reps, work, label = 1, 8.0 * M * N * K, f"gemm {prec} {M}x{N}x{K}"
+    elif kind == "jk":
+        from apyib_gb300.linalg import jk_fock
+        n = int(args[0]) if args else 150
+        reps = int(args[1]) if len(args) > 1 else 5
+        variant = args[2] if len(args) > 2 else "sym"
+        g = torch.Generator(device="cpu").manual_seed(0)
+        A = torch.randn(3 * n, n, n, generator=g, dtype=torch.float64)
+        A = ((A + A.transpose(1, 2)) / (2 * (3 * n * n) ** 0.5)).cuda()
+        eri = torch.einsum("Lmn,Lls->mnls", A, A)
+        del A
+        eri = (0.5 * (eri + eri.transpose(2, 3))).contiguous()
+        if variant == "general":
+            eri[0, 0, 0, 1] = eri[0, 0, 0, 1] * (1 + 2.0 ** -40) + 1e-300   # not (l, s)-symmetric
+        Cm = torch.linalg.qr(torch.randn(n, n, generator=g, dtype=torch.complex128))[0].cuda()
+        D = (Cm[:, : n // 4] @ Cm[:, : n // 4].conj().T).contiguous()
+        h = torch.zeros(n, n, dtype=torch.complex128, device="cuda")
+        prec = "fp64" if variant == "sym64" else "df64"
+
+        def run():
+            jk_fock(eri, D, h, 1.0, precision=prec)
+        work, label = 8.0 * n ** 4, f"jk_fock {variant} nbf={n} (GB/s of the full ERI tensor)"
+    elif kind == "hbm":
+        from apyib_gb300 import synthetic
+        from apyib_gb300.cisd import CISDPlan
+        o, v = int(args[0]), int(args[1])
+        which = args[2] if len(args) > 2 else "all"
+        prob = synthetic.so_factors(o, v, seed=0)
+        eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+        plan = CISDPlan(o, v, mixed=True)
+        plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
+        plan.blocks_from_factors(torch.as_tensor(prob.B), precision=_lib.PREC_OZAKI)
+        t = plan.guess()
+        g = torch.Generator(device="cuda").manual_seed(1)
+        ys = [t + 1e-3 * torch.randn(t.shape, dtype=t.dtype, device=t.device, generator=g) for _ in range(8)]
+        out3 = torch.empty(16, dtype=torch.complex128, device=t.device)
+        tn = torch.empty_like(t)
+        n, n2 = plan.n1 + plan.n2, plan.n2
+        cases = {"update": (lambda: plan.update(t, ys[0], out=tn), 48 * n),
+                 "dots": (lambda: plan.dots_into(t, ys, out3), 16 * 9 * n),
+                 "combine": (lambda: plan.combine_into(ys, [0.125] * 8, t, tn, out3), 16 * 11 * n),
+                 "mp2": (lambda: plan.mp2_into(tn, out3), 48 * n2)}
+        sel = cases if which == "all" else {which: cases[which]}
+        for name, (fn, nbytes) in sel.items():
+            fn()
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            print(f"ok hbm {name} o/v={o}/{v}: {ms:.3f} ms, {nbytes / ms / 1e6:.0f} GB/s of {nbytes / 1e9:.3f} GB")
+        plan.check_status()
+        return 0
+    else:
+        raise SystemExit(f"unknown --profile kind {kind!r}")
+    run()
+    run()
+    if kind == "gemm" and prec in ("tf32x3", "oz"):
+        _lib.call("agb_scratch_status", ctypes.c_void_p(sp), stream_ptr())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    unit = "TFLOP/s (8MNK)" if kind == "gemm" else "GB/s"
+    scale = 1e9 if kind == "gemm" else 1e6
+    print(f"ok {label}: {ms:.3f} ms, {work / ms / scale:.1f} {unit}")
+    return 0
+
+
 METRIC = "CISD_SO iteration TFLOP/s (algorithmic), mixed 3xTF32 + FP64 refinement, synthetic o/v=60/240"
 
 
@@ -419,7 +632,13 @@ def main():
     ap.add_argument("--v", type=int, default=240)
     ap.add_argument("--no-solve", action="store_true", help="skip the once-per-run full solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-fp64-solve", action="store_true",
+                    help="skip the full FP64 GPU solve at the bench shape (several minutes at 60/240)")
+    ap.add_argument("--profile", nargs="+", metavar="ARG",
+                    help="run one kernel on a small case instead of the bench (see profile_kernel)")
     args = ap.parse_args()
+    if args.profile:
+        return profile_kernel(args.profile)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -457,20 +676,7 @@ def main():
     del prob
 
     # ---- iteration state
-    t = plan.guess()
-    E, _, _ = plan.combine([t], [1.0], t, t)
-    diis = _DIIS(plan)
-    state = {"t": t, "E": E, "first": True}
-
-    def iteration():
-        r = plan.residual(state["t"], state["E"], _lib.PREC_TF32X3)
-        tn = plan.update(state["t"], r)
-        diis.push(r, tn, state["first"])
-        state["first"] = False
-        c = diis.coefficients()
-        E, s1, s2 = plan.combine(diis.t, c, state["t"], state["t"])
-        state["E"] = E
-        return E
+    iteration, state, diis = mixed_iteration(plan)
 
     for _ in range(args.warmup):
         iteration()
@@ -539,9 +745,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (3xTF32 tensor core) + c128 (update/DIIS/sums)",
         "data": f"synthetic (seeded Hermitian factors, o/v={o}/{v}; the headline shape is 60/240)",
-        "config": {"workload": f"CISD_SO mixed-precision iteration, synthetic o/v={o}/{v} spin orbitals",
-                   "o": o, "v": v, "naux": 4 * (o + v), "l2": "inputs > L2 (ERI blocks ~45 GB in HBM)",
-                   "parallelism": f"replicas x{world}", "alg_flops_per_step": W},
+        "config": bench_config(o, v, world),
         "e2e": {"value": aggregate_throughput(world, W, e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 # per-step phases on the stream: pinned host -> HBM copy, the iteration, HBM -> pinned host
@@ -584,18 +788,32 @@ def main():
         corr = plan.update(torch.zeros_like(tm), r64)
         max_corr = corr.abs().max().item()
         iters = len(hist) - 1
-        tf32_res_s = dev_ms / 1e3
         out["solve"] = {
             "mixed_solve_s": solve_s, "E_mixed": [Em.real, Em.imag], "iterations": iters,
             "tf32_residuals": stats["tf32_residuals"], "fp64_residuals": stats["fp64_residuals"],
             "base_residual_s": stats.get("base_residual_s"),
             "iteration_s": [round(h["seconds"], 4) for h in hist[:-1]],
             "fp64_residual_s": fp64_res_s,
-            "fp64_solve_estimate_s": iters * fp64_res_s,
-            "fp64_solve_estimate_note": "iterations of the mixed solve x measured FP64 residual time",
             "posterior_max_amplitude_correction": max_corr,
         }
         del r64, corr
+        if not args.no_fp64_solve:
+            # the plain FP64 GPU path (every GEMM on the FP64 pipe) solved to the same convergence
+            # test from the same guess: measured wall time and the mixed solve's energy and
+            # amplitude errors against it
+            h64 = []
+            torch.cuda.synchronize()
+            ts = time.perf_counter()
+            E64, t64 = solve(plan, params, precision="fp64", history=h64)
+            torch.cuda.synchronize()
+            fp64_s = time.perf_counter() - ts
+            out["solve"].update({
+                "fp64_solve_s": fp64_s, "E_fp64": [E64.real, E64.imag], "fp64_iterations": len(h64) - 1,
+                "speedup_mixed_vs_fp64": fp64_s / solve_s,
+                "abs_dE_mixed_vs_fp64": abs(Em - E64),
+                "max_abs_amplitude_diff_mixed_vs_fp64": (tm - t64).abs().max().item(),
+                "target": "|dE| <= 1e-9 Eh with the mixed solve faster than the FP64 solve"})
+            del t64
         # Adjoint: one backward (CISD densities, vvvv block recomputed, 3xTF32 GEMMs) at the solution,
         # against the 2*(3N+3) = 24 full solves a finite-difference AAT/APT set needs for H2O (N = 3).
         from apyib_gb300.adjoint import densities
@@ -623,6 +841,8 @@ def main():
         plan3 = CISDPlan(o3, v3, mixed=True)
         plan3.set_fock(torch.as_tensor(prob3.fock_so()), eps3)
         plan3.blocks_from_factors(torch.as_tensor(prob3.B), precision=_lib.PREC_OZAKI)
+        it3, _, _ = mixed_iteration(plan3)
+        c3_ms = timed_iterations(it3, 5, 3)
         res3 = {}
         for prec in ("fp64", "mixed"):
             h3 = []
@@ -636,13 +856,22 @@ def main():
             "speedup": res3["fp64"][0] / res3["mixed"][0],
             "abs_dE_mixed_vs_fp64": abs(res3["mixed"][1] - res3["fp64"][1]),
             "E_fp64": [res3["fp64"][1].real, res3["fp64"][1].imag],
-            "iterations": {"fp64": res3["fp64"][2], "mixed": res3["mixed"][2]}}
-        del plan3
+            "iterations": {"fp64": res3["fp64"][2], "mixed": res3["mixed"][2]},
+            "mixed_iteration_ms": c3_ms, "mixed_iteration_TFLOPs": alg_flops(o3, v3) / c3_ms / 1e9}
+        del plan3, it3
     if not args.no_solve and rank == 0:
         out["ao_kernels_nbf150"] = ao_kernels(150)
         out["h2o_ccpvdz_bz"] = water_workloads()
     if not args.no_cpu and rank == 0:
-        out["cpu_baseline"] = cpu_baseline_oracle()
+        out["cpu_baseline"] = cpu_baseline_oracle(o, v)
+        if "solve_40_160" in out:
+            # the same comparison at o/v = 40/160: the GPU's mixed iteration against the
+            # reference path's residual on the host cores (sampled the same way)
+            c3 = cpu_baseline_oracle(40, 160, steps=2)
+            g3 = out["solve_40_160"]["mixed_iteration_TFLOPs"]
+            out["c3_40_160"] = {"gpu_mixed_iteration_TFLOPs": g3, "cpu_TFLOPs": c3["value"],
+                                "cpu_full_residual_s_from_sample": c3["full_residual_s_from_sample"],
+                                "cpu_sample": c3["sample"], "gpu_over_cpu": g3 / c3["value"]}
     if rank == 0:
         print(json.dumps(out))
     if dist:

@@ -203,7 +203,9 @@ agb_status agb_cisd_update(agb_cisd_plan* plan, const void* t, const void* r, vo
 /* out[j] = w1 * sum_{k<n1} conj(y_j[k]) x[k] + w2 * sum_{k>=n1} conj(y_j[k]) x[k], j < ny <= 16.
  * (DIIS Gram row, apyib/utils.py:121, with w2 = 4 for packed doubles.)  The first part
  * is summed by a single thread block (it is sized for the singles, n1 = o v): pass a long
- * vector as the second part. */
+ * vector as the second part.  Products and sums run in double-float (~2^-44 relative):
+ * entries must satisfy |re|, |im| < 2^128, and an entry at or above it (or inf / NaN)
+ * makes the affected results non-finite; parts below 2^-112 in magnitude are dropped. */
 agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x,
                         const void* const* ys, int ny, void* out, void* partials, size_t partials_bytes,
                         void* stream);
@@ -221,9 +223,12 @@ size_t agb_vec_partials_bytes(int ny);
  * The block partial sums live in a fixed array inside the library (155,648
  * bytes on every device that loads it, kept until the process exits), so this
  * entry point allocates nothing and accepts at most ny = 16 vectors; larger ny
- * is rejected with AGB_ERR_ARG.  The first call on a device looks up the
- * array's device address (with that device current), so make that first call
- * before any stream capture.  All calls on a device share the one array and
+ * is rejected with AGB_ERR_ARG.  The array's device address belongs to one CUDA
+ * context: the first call in each context (the device's primary context, or a
+ * caller's own context made current) looks it up with that context current and
+ * caches it under the context's unique id, so a context destroyed and recreated
+ * (cudaDeviceReset) gets a fresh lookup; make that first call before any stream
+ * capture.  All calls on a device share the one array and
  * each call leaves its partial sums there; calls that overlap on the GPU (for
  * example on two streams at once) race on it, so the caller must keep them
  * from overlapping. */

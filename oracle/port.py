@@ -188,6 +188,89 @@ def cisd_so_residual(F, blk, t1, t2, E, o: int, singles: bool = True):
     return r1, r2
 
 
+VSLAB_SPEC = {"ovvo": "ovvo", "ooov": "ooov", "ovoo": "ovoo", "oooo": "oooo",
+              "vvvv": "avvv", "vovv": "aovv", "vvvo": "avvo", "vvoo": "avoo"}
+
+
+def vslab_blocks_from_factors(B, o: int, a0: int, a1: int, names=tuple(VSLAB_SPEC)):
+    """The antisymmetrised blocks ``cisd_so_residual_vslab`` reads for the residual rows
+    a0 <= a < a1 (virtual index): ovvo, ooov, ovoo and oooo in full, and vvvv, vovv,
+    vvvo, vvoo with their first (virtual) index restricted to [a0, a1).  Same formula
+    as ``blocks_from_factors``; ``names`` selects blocks."""
+    n = B.shape[1]
+    m = {"o": slice(0, o), "v": slice(o, n), "a": slice(o + a0, o + a1)}
+    out = {}
+    for name in names:
+        ranges = VSLAB_SPEC[name]
+        P, Q, R, S = (m[c] for c in ranges)
+        direct = np.einsum("Lpr,Lqs->pqrs", B[:, P, R], B[:, Q, S], optimize=True)
+        exch = np.einsum("Lps,Lqr->pqrs", B[:, P, S], B[:, Q, R], optimize=True)
+        out[name] = direct - exch
+    return out
+
+
+def vslab_layouts(blk, t2):
+    """Full-size operands of ``cisd_so_residual_vslab`` laid out once in the order its
+    contractions read them (the ring integrals as [b, j, k, c]; t2 as [c, i, j, b],
+    [k, c, i, b] and [k, c, j, b]), so that a timed row sample copies nothing of full
+    size: einsum would otherwise re-lay these out on every call, a cost the full
+    residual pays once per term, not once per sampled row block."""
+    W = blk["ovvo"]
+    return {"W_bjkc": np.ascontiguousarray(W.transpose(1, 3, 0, 2)),
+            "t2_cijb": np.ascontiguousarray(t2.transpose(2, 0, 1, 3)),
+            "t2_kcib": np.ascontiguousarray(t2.transpose(1, 2, 0, 3)),
+            "t2_kcjb": np.ascontiguousarray(t2.transpose(0, 2, 1, 3))}
+
+
+def cisd_so_residual_vslab(F, blk, t1, t2, E, o: int, a0: int, a1: int, lay=None):
+    """Rows a0 <= a < a1 of ``cisd_so_residual`` (apyib/ci_wfn.py:309-334): r1[:, a0:a1]
+    and r2[:, :, a0:a1, :], every einsum of the reference restricted to those output
+    rows with its full contraction lengths, so the work is (a1 - a0) / v of each term.
+    ``blk`` comes from ``vslab_blocks_from_factors`` (or has the same slices); ``lay``
+    (from ``vslab_layouts``) gives the full-size operands pre-laid-out."""
+    O = slice(0, o)
+    V = slice(o, F.shape[0])
+    A = slice(a0, a1)
+    Foo, Fvv, Fov = F[O, O], F[V, V], F[O, V]
+    ein = lambda s, *a: np.einsum(s, *a, optimize=True)
+    t1a, t2a = t1[:, A], t2[:, :, A, :]
+    W = blk["ovvo"]
+    r1 = F.T[O, V][:, A].copy()
+    r1 -= ein("ji,ja->ia", Foo, t1a)
+    r1 += ein("ab,ib->ia", Fvv[A], t1)
+    r1 += ein("jabi,jb->ia", W[:, A], t1)
+    r1 += ein("jb,ijab->ia", Fov, t2a)
+    r1 += 0.5 * ein("ajcb,ijcb->ia", blk["vovv"], t2)
+    r1 -= 0.5 * ein("kjib,kjab->ia", blk["ooov"], t2a)
+    r1 -= E * t1a
+    r2 = blk["vvoo"].transpose(2, 3, 0, 1).copy()
+    r2 -= ein("kbij,ka->ijab", blk["ovoo"], t1a)
+    r2 -= ein("akij,kb->ijab", -blk["ovoo"][:, A].transpose(1, 0, 2, 3), t1)
+    r2 += ein("abcj,ic->ijab", blk["vvvo"], t1)
+    r2 += ein("abic,jc->ijab", -blk["vvvo"].transpose(0, 1, 3, 2), t1)
+    r2 += ein("bc,ijac->ijab", Fvv, t2a)
+    if lay is None:
+        r2 += ein("ac,ijcb->ijab", Fvv[A], t2)
+    else:
+        r2 += ein("ac,cijb->ijab", Fvv[A], lay["t2_cijb"])
+    r2 -= ein("kj,ikab->ijab", Foo, t2a)
+    r2 -= ein("ki,kjab->ijab", Foo, t2a)
+    r2 += 0.5 * ein("klij,klab->ijab", blk["oooo"], t2a)
+    r2 += 0.5 * ein("abcd,ijcd->ijab", blk["vvvv"], t2)
+    if lay is None:
+        r2 += ein("kbcj,ikac->ijab", W, t2a)
+        r2 += ein("kbci,kjac->ijab", W, t2a)
+        r2 += ein("kacj,ikcb->ijab", W[:, A], t2)
+        r2 += ein("kaci,kjcb->ijab", W[:, A], t2)
+    else:
+        r2 += ein("bjkc,ikac->ijab", lay["W_bjkc"], t2a)
+        r2 += ein("bikc,kjac->ijab", lay["W_bjkc"], t2a)
+        r2 += ein("kacj,kcib->ijab", W[:, A], lay["t2_kcib"])
+        r2 += ein("kaci,kcjb->ijab", W[:, A], lay["t2_kcjb"])
+    r2 -= E * t2a
+    return r1, r2
+
+
 def so_denominators(eps_o_spatial, eps_v_spatial):
     """apyib/ci_wfn.py:268-271: SO denominators from np.repeat-ed spatial energies."""
     eo = np.repeat(eps_o_spatial, 2)

@@ -26,7 +26,9 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("APYIB_REF", "/root/reference")
+REF_ROOT = os.environ.get("APYIB_REF")
+if not REF_ROOT:
+    raise SystemExit("set APYIB_REF to an apyib source checkout (the directory holding apyib/)")
 NBF, NDOCC, NATOM = 4, 2, 1         # spatial sizes: SO o = 4, v = 4
 PAIRS = [(0, 0), (1, 2), (2, 1)]
 TERMS = ["I_00", "I_0D", "I_D0", "I_DD", "I_0S", "I_S0", "I_SS", "I_SD", "I_DS"]

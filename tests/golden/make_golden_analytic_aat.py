@@ -11,7 +11,9 @@ import json
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("APYIB_REF", "/root/reference")
+REF_ROOT = os.environ.get("APYIB_REF")
+if not REF_ROOT:
+    raise SystemExit("set APYIB_REF to an apyib source checkout (the directory holding apyib/)")
 FILES = ["apyib/tests/test_018_RHF_Analytic_AAT.py", "apyib/tests/test_019_MP2_Analytic_AAT.py",
          "apyib/tests/test_020_CID_Analytic_AAT.py", "apyib/tests/test_021_CISD_Analytic_AAT.py"]
 

@@ -17,7 +17,9 @@ import json
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("APYIB_REF", "/root/reference")
+REF_ROOT = os.environ.get("APYIB_REF")
+if not REF_ROOT:
+    raise SystemExit("set APYIB_REF to an apyib source checkout (the directory holding apyib/)")
 FILES = {"hessian": "apyib/tests/test_009_Hessian.py", "apt": "apyib/tests/test_010_APT.py"}
 
 

@@ -26,7 +26,9 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from apyib_gb300 import basis as B  # noqa: E402
 from tests.golden.reference_energies import H2O  # noqa: E402
 
-REF_ROOT = os.environ.get("APYIB_REF", "/root/reference")
+REF_ROOT = os.environ.get("APYIB_REF")
+if not REF_ROOT:
+    raise SystemExit("set APYIB_REF to an apyib source checkout (the directory holding apyib/)")
 BASIS = "6-31G(d)"
 KINDS = ("overlap", "kinetic", "dipole", "nabla", "angular momentum")
 

@@ -2,8 +2,8 @@
 mp2_wfn, ci_wfn) from a source checkout with a stub ``psi4`` module.
 
 This is fixture-generation infrastructure only: it runs where the reference
-sources are available (``APYIB_REF`` environment variable, default
-``/root/reference``) and is never imported by the GPU tests, ``smoke()`` or
+sources are available (the ``APYIB_REF`` environment variable names the
+checkout; there is no default) and is never imported by the GPU tests, ``smoke()`` or
 ``bench.py``.  The reference imports ``psi4`` at module level
 (apyib/utils.py:4, apyib/hf_wfn.py:3, apyib/mp2_wfn.py:3, apyib/ci_wfn.py:3,
 apyib/hamiltonian.py:3) but the hot-path functions never call it once a
@@ -14,7 +14,17 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("APYIB_REF", "/root/reference")
+
+
+def reference_root():
+    """The apyib source checkout named by ``APYIB_REF`` (required)."""
+    root = os.environ.get("APYIB_REF")
+    if not root:
+        raise SystemExit("set APYIB_REF to an apyib source checkout (the directory holding apyib/)")
+    return root
+
+
+REF_ROOT = reference_root()
 
 
 def _stub_psi4():

@@ -143,3 +143,25 @@ def test_spatial_cisd_is_the_alpha_beta_block_of_the_so_solution(path):
     assert abs(g["E_cid_spatial"] - g["E_cid"]) < 1e-12
     np.testing.assert_allclose(g["t2_cisd"][0::2, 1::2, 0::2, 1::2], g["t2_cisd_spatial"], atol=1e-13)
     np.testing.assert_allclose(g["t1_cisd"][0::2, 0::2], g["t1_cisd_spatial"], atol=1e-13)
+
+
+@pytest.mark.parametrize("a0,a1", [(0, 2), (3, 7), (9, 10)])
+def test_virtual_row_sample_equals_rows_of_the_full_residual(a0, a1):
+    """The CPU baseline times rows a0 <= a < a1 of the residual (every reference einsum
+    restricted to those output rows); they must be exactly those rows of the full one,
+    on a complex non-diagonal Fock matrix and random amplitudes."""
+    prob = synthetic.so_factors(6, 10, seed=3)
+    o, n = prob.o, prob.nso
+    rng = np.random.default_rng(4)
+    F = prob.fock_so() + 0.05 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    t1 = 0.1 * (rng.standard_normal((o, prob.v)) + 1j * rng.standard_normal((o, prob.v)))
+    t2 = 0.1 * (rng.standard_normal((o, o, prob.v, prob.v)) + 1j * rng.standard_normal((o, o, prob.v, prob.v)))
+    t2 = t2 - t2.transpose(1, 0, 2, 3)
+    t2 = t2 - t2.transpose(0, 1, 3, 2)
+    E = 0.3 - 0.1j
+    r1, r2 = port.cisd_so_residual(F, port.blocks_from_factors(prob.B, o), t1, t2, E, o)
+    blk = port.vslab_blocks_from_factors(prob.B, o, a0, a1)
+    for lay in (None, port.vslab_layouts(blk, t2)):
+        s1, s2 = port.cisd_so_residual_vslab(F, blk, t1, t2, E, o, a0, a1, lay=lay)
+        np.testing.assert_allclose(s1, r1[:, a0:a1], atol=1e-13, rtol=0)
+        np.testing.assert_allclose(s2, r2[:, :, a0:a1, :], atol=1e-13, rtol=0)

@@ -100,3 +100,38 @@ def test_lockstep_equals_one_at_a_time_on_cpu():
             # converged: the response equation holds, r^x = c^x + L^x t + (L - E) t^x - E^x t = 0
             rx = px.residual(t, 0.0, flags=_lib.RES_CONST) + plan.residual(dt, E, flags=_lib.RES_ETERM) - dE * t
             assert torch.abs(rx).max().item() < 1e-9
+
+
+def test_imaginary_response_needs_the_conjugated_step_norm():
+    """A magnetic-field perturbation of a real problem gives purely imaginary t^x.  The
+    reference sums the unconjugated squares of the step (apyib/analytic_aats.py:868-879),
+    in its real formulation of the magnetic responses; applied to imaginary t^x that sum is
+    negative, its square root imaginary, and numpy's complex < real compares the real part,
+    0, so the step test would pass at every iteration.  The driver uses conjugated squares:
+    it stops only once the step is small, and the response it returns solves its equation."""
+    rng = np.random.default_rng(9)
+    n, n1 = 24, 6
+    D = torch.as_tensor(-(1.0 + rng.random(n)) * 2.0)
+    L = torch.diag(-D).to(torch.complex128) + torch.as_tensor(0.05 * rng.standard_normal((n, n)) + 0j)
+    c = torch.as_tensor(rng.standard_normal(n) + 0j)
+    ew = torch.as_tensor(0.1 * rng.standard_normal(n) + 0j)
+    plan = DensePlan(L, c, ew, D, n1)
+    t = torch.as_tensor(0.1 * rng.standard_normal(n) + 0j)
+    E = complex(torch.sum(t * ew))
+    # purely imaginary perturbation (i times real matrices), as the magnetic field's -i L / 2
+    px = DensePlan(torch.as_tensor(1j * rng.standard_normal((n, n))), torch.as_tensor(1j * rng.standard_normal(n)),
+                   torch.as_tensor(1j * rng.standard_normal(n)), D, n1)
+    d_conv = 1e-10
+    params = dict(e_convergence=1e-12, d_convergence=d_conv, max_iterations=200, DIIS=True)
+    hist = []
+    dE, dt = solve_response(plan, px, t, E, params, history=hist)
+    assert torch.abs(dt.real).max().item() < 1e-12 < torch.abs(dt.imag).max().item()
+    # the reference's step test, on the unconjugated sums, is vacuous from the first iteration on
+    for h in hist:
+        assert np.complex128(h["rms_t2_unconj"]) < d_conv and np.complex128(h["rms_t1_unconj"]) < d_conv
+    # at iteration 2 the step is still far from converged
+    assert abs(hist[1]["rms_t2"]) > 1e3 * d_conv
+    # the driver's conjugated step norm is what ends the iteration, and the response solves its equation
+    assert len(hist) > 2 and abs(hist[-1]["rms_t2"]) < d_conv and abs(hist[-1]["rms_t1"]) < d_conv
+    rx = px.residual(t, 0.0, flags=_lib.RES_CONST) + plan.residual(dt, E, flags=_lib.RES_ETERM) - dE * t
+    assert torch.abs(rx).max().item() < 1e-9
