@@ -156,13 +156,15 @@ def unpack_vvvv(Gp, v):
 def gamma_full(G, o, v):
     """Assemble the full Dirac Gamma[p,q,r,s] (nso^4) from the blocks."""
     nso = o + v
-    dev = G["oooo"].device
+    dev = next(x for x in G.values() if isinstance(x, torch.Tensor)).device
     Gm = torch.zeros((nso, nso, nso, nso), dtype=torch.complex128, device=dev)
     O, V = slice(0, o), slice(o, nso)
     m = {"o": O, "v": V}
     for k in ("oooo", "ovvo", "ovov", "voov", "vovo", "oovv", "vvoo", "vovv", "ovoo", "vvvo", "ooov"):
-        Gm[m[k[0]], m[k[1]], m[k[2]], m[k[3]]] += G[k]
-    Gm[V, V, V, V] += unpack_vvvv(G["vvvv_p"], v)
+        if k in G:
+            Gm[m[k[0]], m[k[1]], m[k[2]], m[k[3]]] += G[k]
+    if "vvvv_p" in G:
+        Gm[V, V, V, V] += unpack_vvvv(G["vvvv_p"], v)
     return Gm
 
 
@@ -205,6 +207,128 @@ def cisd_energy(F_SO, ERI_SO, eps_o, eps_v, params, singles=True, precision="fp6
     return CISDEnergy.apply(to_dev(F_SO) if not isinstance(F_SO, torch.Tensor) else F_SO,
                             to_dev(ERI_SO) if not isinstance(ERI_SO, torch.Tensor) else ERI_SO,
                             eps_o, eps_v, params, singles, precision)
+
+
+# ---------------------------------------------------------------------------
+# MP2_SO: the Hylleraas Lagrangian and its densities
+#
+# The MP2_SO energy of apyib/mp2_wfn.py:64-87, E = 1/4 sum <ij||ab> t_ijab with
+# t_ijab = <ab||ij> / D_ijab (no conjugate), is the stationary value of
+#     L(t, lam) = 1/4 <W, t> + 1/4 <lam, V + A t>,    <x, y> = sum_ijab x_ijab y_ijab,
+# W_ijab = <ij||ab>, V_ijab = <ab||ij>, and A the Fock operator on the doubles,
+#     (A t)_ijab = sum_c (F_bc t_ijac + F_ac t_ijcb) - sum_k (F_kj t_ikab + F_ki t_kjab),
+# whose diagonal part is -D t (D_ijab = F_ii + F_jj - F_aa - F_bb; the reference's
+# orbital energies when F is the canonical Fock matrix).  Stationarity gives the
+# amplitude equations V + A t = 0 and the left equations W + A^T lam = 0 (A^T: F
+# transposed), so lam = W / D at a canonical point, lam = conj(t) for Hermitian
+# integrals.  The derivatives of L are densities in the format of ``densities``:
+#     D_oo[x,y] = -1/2 sum_iab t_ixab lam_iyab,   D_vv[x,y] = 1/2 sum_ija lam_ijax t_ijay,
+#     Gamma_oovv = t / 2,   Gamma_vvoo[a,b,i,j] = lam_ijab / 2,
+# and E = sum F D + sum <pq|rs> Gamma holds at the solution.  With a non-canonical F
+# (off-diagonal occupied-occupied or virtual-virtual elements) the amplitudes solve
+# the full equations, the non-canonical MP2 that apyib/analytic_aats.py:215-549
+# differentiates for its MP2 AATs.
+
+def _mp2_fock_offdiag(t, Foo, Fvv, transpose=False):
+    """The off-diagonal part of (A t) (or A^T t) for antisymmetric t[o,o,v,v], on the
+    library's complex GEMM."""
+    o, v = t.shape[0], t.shape[2]
+    Fo = Foo - torch.diag(torch.diagonal(Foo))
+    Fv = Fvv - torch.diag(torch.diagonal(Fvv))
+    if transpose:
+        Fo, Fv = Fo.T.contiguous(), Fv.T.contiguous()
+    X = zmm(t.reshape(o * o * v, v), Fv, transB=True).reshape(o, o, v, v)     # sum_c F_bc t_ijac
+    Tk = t.permute(1, 0, 2, 3).reshape(o, o * v * v).contiguous()
+    Z = zmm(Fo, Tk, transA=True).reshape(o, o, v, v).permute(1, 0, 2, 3)      # sum_k F_kj t_ikab
+    return (X - X.transpose(2, 3)) - (Z - Z.transpose(0, 1))
+
+
+def _mp2_denominators(Foo, Fvv):
+    eo, ev = torch.diagonal(Foo), torch.diagonal(Fvv)
+    return eo.view(-1, 1, 1, 1) + eo.view(1, -1, 1, 1) - ev.view(1, 1, -1, 1) - ev.view(1, 1, 1, -1)
+
+
+def mp2_so_blocks(ERI_SO, o):
+    """W[i,j,a,b] = <ij||ab> and V[i,j,a,b] = <ab||ij> from a chemist spin-orbital tensor
+    (<pq|rs> = (pr|qs)), gathered on the device."""
+    g = ERI_SO
+    O, V = slice(0, o), slice(o, g.shape[0])
+    ovov = g[O, V, O, V]
+    vovo = g[V, O, V, O]
+    W = ovov.permute(0, 2, 1, 3) - ovov.permute(0, 2, 3, 1)
+    Vb = vovo.permute(1, 3, 0, 2) - vovo.permute(3, 1, 0, 2)
+    return W.contiguous(), Vb.contiguous()
+
+
+def mp2_lagrangian_solve(F_SO, W, V, o, tol=1e-14, max_iterations=200):
+    """Amplitudes t and multipliers lam of the MP2_SO Lagrangian for the Fock matrix
+    F_SO (its occupied-occupied and virtual-virtual blocks) and the blocks W, V of
+    ``mp2_so_blocks``: t = (V + A_off t) / D and lam = (W + A_off^T lam) / D by
+    Jacobi iteration (one step when F is diagonal).  Returns (E, t, lam)."""
+    Foo, Fvv = F_SO[:o, :o], F_SO[o:, o:]
+    D = _mp2_denominators(Foo, Fvv)
+    offdiag = bool((Foo - torch.diag(torch.diagonal(Foo))).abs().max() > 0 or
+                   (Fvv - torch.diag(torch.diagonal(Fvv))).abs().max() > 0)
+    out = []
+    for rhs, tr in ((V, False), (W, True)):
+        x = rhs / D
+        if offdiag:
+            for _ in range(max_iterations):
+                xn = (rhs + _mp2_fock_offdiag(x, Foo, Fvv, transpose=tr)) / D
+                step = (xn - x).abs().max().item()
+                x = xn
+                if step < tol * max(1.0, x.abs().max().item()):
+                    break
+            else:
+                raise RuntimeError("non-canonical MP2 amplitudes did not converge")
+        out.append(x)
+    t, lam = out
+    E = 0.25 * torch.sum(W * t)
+    return complex(E), t, lam
+
+
+def mp2_densities(t, lam):
+    """Densities of the MP2_SO Lagrangian (see above) in the format of ``densities``:
+    D (nso x nso; occupied-occupied and virtual-virtual blocks) and G with the oovv and
+    vvoo Dirac blocks."""
+    o, v = t.shape[0], t.shape[2]
+    nso = o + v
+    D = torch.zeros((nso, nso), dtype=torch.complex128, device=t.device)
+    To = t.permute(1, 0, 2, 3).reshape(o, o * v * v).contiguous()
+    Lo = lam.permute(1, 0, 2, 3).reshape(o, o * v * v).contiguous()
+    D[:o, :o] = -0.5 * zmm(To, Lo, transB=True)
+    D[o:, o:] = 0.5 * zmm(lam.reshape(o * o * v, v), t.reshape(o * o * v, v), transA=True)
+    G = {"oovv": 0.5 * t, "vvoo": (0.5 * lam.permute(2, 3, 0, 1)).contiguous()}
+    return D, G
+
+
+class MP2Energy(torch.autograd.Function):
+    """E_MP2_SO(F_SO, ERI_SO) (chemist ERIs) with the Lagrangian backward: dE/dF = D,
+    dE/d<pq|rs> = Gamma (oo, vv and oovv / vvoo blocks).  At a diagonal F the energy is
+    the reference's MP2_SO energy with the diagonal as orbital energies."""
+
+    @staticmethod
+    def forward(ctx, F_SO, ERI_SO, o):
+        F = F_SO.detach().to(torch.complex128)
+        W, V = mp2_so_blocks(ERI_SO.detach().to(torch.complex128), o)
+        E, t, lam = mp2_lagrangian_solve(F, W, V, o)
+        ctx.save_for_backward(t, lam)
+        return torch.tensor(E, dtype=torch.complex128, device=F_SO.device)
+
+    @staticmethod
+    def backward(ctx, gE):
+        t, lam = ctx.saved_tensors
+        o, v = t.shape[0], t.shape[2]
+        D, G = mp2_densities(t, lam)
+        Gfull = gamma_full(G, o, v)
+        g = gE.to(torch.complex128)
+        return g * D.conj(), g * Gfull.permute(0, 2, 1, 3).conj(), None
+
+
+def mp2_energy(F_SO, ERI_SO, o):
+    """Differentiable MP2_SO energy (see MP2Energy)."""
+    return MP2Energy.apply(to_dev(F_SO) if not isinstance(F_SO, torch.Tensor) else F_SO,
+                           to_dev(ERI_SO) if not isinstance(ERI_SO, torch.Tensor) else ERI_SO, int(o))
 
 
 # ---------------------------------------------------------------------------
@@ -297,7 +421,8 @@ def _contract3(T, H, axis):
 
 
 def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64", return_intermediates=False):
-    """Wirtinger derivatives (E, dE/dC, dE/dC*) of the CISD_SO correlation energy with
+    """Wirtinger derivatives (E, dE/dC, dE/dC*) of the CISD_SO (CID_SO, or MP2_SO through
+    its Lagrangian densities, ``mp2_densities``) correlation energy with
     respect to the MO coefficients C (nbf x nbf), at fixed AO integrals and fixed
     orbital energies, with C entering through F_MO = C_t^H (h + G[C_fc C_fc^H] +
     G[C_o C_o^H]) C_t and (PQ|RS) = sum C*_mP C_nQ C*_lR C_sS (mn|ls) (apyib/utils.py:
@@ -317,12 +442,22 @@ def mo_coefficient_gradient(h_AO, wfn, params, precision="fp64", return_intermed
     eps = np.asarray(wfn.eps)
     eps_o, eps_v = eps[C_list[1]], eps[C_list[2]]
     o, v = 2 * len(eps_o), 2 * len(eps_v)
-    plan = CISDPlan(o, v, singles=params["method"] in ("CISD", "CISD_SO"), mixed=(precision == "mixed"))
-    plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True),
-                  np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)]))
-    plan.blocks_from_mo(ERI_MO)
-    E, tamp = solve(plan, params, precision=precision)
-    D, G = densities(plan, tamp)
+    eps_so = np.concatenate([np.repeat(eps_o, 2), np.repeat(eps_v, 2)])
+    if params["method"] in ("MP2", "MP2_SO"):
+        # MP2_SO amplitudes t = <ab||ij> / D (canonical orbitals); the Lagrangian's
+        # multipliers lam = <ij||ab> / D = conj(t) for the Hermitian MO integrals
+        plan = CISDPlan(o, v, mp2_only=True)
+        plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True), eps_so)
+        plan.blocks_from_mo(ERI_MO)
+        E, tamp = plan.mp2()
+        _, t2 = plan.unpack(tamp)
+        D, G = mp2_densities(t2, t2.conj().resolve_conj())
+    else:
+        plan = CISDPlan(o, v, singles=params["method"] in ("CISD", "CISD_SO"), mixed=(precision == "mixed"))
+        plan.set_fock(compute_F_SO(wfn, F_MO, return_torch=True), eps_so)
+        plan.blocks_from_mo(ERI_MO)
+        E, tamp = solve(plan, params, precision=precision)
+        D, G = densities(plan, tamp)
     D_sp, Gc = _spin_summed(D, G, o, v)
     nbf = C.shape[0]
     Ct = C[:, t].contiguous()

@@ -1,5 +1,8 @@
-"""Analytic nuclear gradients of the RHF, CID_SO and CISD_SO energies (zero magnetic
-field; a uniform electric field allowed), and atomic polar tensors from them.
+"""Analytic nuclear gradients of the RHF, MP2_SO, CID_SO and CISD_SO energies (zero
+magnetic field; a uniform electric field allowed), and atomic polar tensors from them.
+MP2 enters through the densities of its Hylleraas Lagrangian (adjoint.mp2_densities),
+which make its energy stationary in the amplitudes as the CI energies are, so the same
+skeleton + orbital-response assembly applies.
 
 The finite-difference route (fin_diff.compute_Nuclear_Gradient) needs 2 x 3N
 complete calculations; this one needs one: the SCF, the CI solve, its
@@ -91,16 +94,16 @@ def _field_hamiltonian(H0, mu, F_el):
 
 
 def nuclear_gradient(parameters, precision="fp64", return_parts=False, geometry=None):
-    """Analytic dE/dR (natom, 3) of parameters['method'] in RHF, CID_SO, CISD_SO (or the
-    spatial CID / CISD, the same energies) at zero magnetic field, in the electric
+    """Analytic dE/dR (natom, 3) of parameters['method'] in RHF, MP2_SO, CID_SO, CISD_SO (or
+    the spatial MP2 / CID / CISD, the same energies) at zero magnetic field, in the electric
     field parameters['F_el'] (real orbitals).  ``geometry``: geometry_integrals() of the
     same geometry and basis, to reuse across fields."""
     from .adjoint import mo_coefficient_gradient
     from .hf_wfn import hf_wfn
 
     method = parameters["method"]
-    if method not in ("RHF", "CID", "CISD", "CID_SO", "CISD_SO"):
-        raise ValueError(f"analytic gradients exist for RHF, CID and CISD, not {method}")
+    if method not in ("RHF", "MP2", "MP2_SO", "CID", "CISD", "CID_SO", "CISD_SO"):
+        raise ValueError(f"analytic gradients exist for RHF, MP2, CID and CISD, not {method}")
     if any(f != 0.0 for f in parameters["F_mag"]):
         raise ValueError("analytic gradients are implemented at zero magnetic field (real orbitals)")
     F_el = [float(f) for f in parameters["F_el"]]

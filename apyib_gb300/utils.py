@@ -59,11 +59,29 @@ def compute_F_MO(parameters, wfn, C_list, return_torch=False):
     return _ret(F_MO, return_torch), E_fc
 
 
-def compute_ERI_MO(parameters, wfn, C_list, return_torch=False, precision=_lib.PREC_FP64):
+_TRANSFORM_PREC = {"fp64": _lib.PREC_FP64, "ozaki": _lib.PREC_OZAKI, "df64": _lib.PREC_DF64,
+                   "tf32x3": _lib.PREC_TF32X3}
+
+
+def transform_precision(parameters):
+    """Precision of the AO->MO transform for a parameters dict: its 'transform_precision'
+    key ('fp64', 'ozaki', 'df64' or 'tf32x3') when present, else Ozaki under
+    precision='mixed' (FP64-accurate, ~1e-12 of sum |a||b|, on the tensor cores) and
+    FP64 otherwise."""
+    key = parameters.get("transform_precision")
+    if key is None:
+        key = "ozaki" if parameters.get("precision") == "mixed" else "fp64"
+    return _TRANSFORM_PREC[key]
+
+
+def compute_ERI_MO(parameters, wfn, C_list, return_torch=False, precision=None):
     """apyib/utils.py:258-279: four quarter-step AO->MO transform (complex C, real AO ERIs).
-    precision: _lib.PREC_FP64 (default), PREC_DF64 (double-float GEMMs on the FP32
-    pipe, ~1e-13 relative), PREC_OZAKI (FP64-accurate bf16-slice GEMMs on the tensor
-    cores, ~1e-12 of sum |a||b|) or PREC_TF32X3 (tensor cores, ~1e-6 relative)."""
+    precision: _lib.PREC_FP64, PREC_DF64 (double-float GEMMs on the FP32 pipe, ~1e-13
+    relative), PREC_OZAKI (FP64-accurate bf16-slice GEMMs on the tensor cores, ~1e-12 of
+    sum |a||b|) or PREC_TF32X3 (tensor cores, ~1e-6 relative); None chooses by
+    ``transform_precision(parameters)``."""
+    if precision is None:
+        precision = transform_precision(parameters)
     t = C_list[3]
     C = to_dev(np.asarray(wfn.C)[:, t])
     ERI = to_dev(wfn.H.ERI, torch.float64)

@@ -487,6 +487,56 @@ def timed_iterations(iteration, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
+def gpu_numa_cpus(dev_index):
+    """(NUMA node of the GPU's PCI function, the usable host cores on that node) from sysfs;
+    (None, []) when the system does not say."""
+    import torch
+    try:
+        bdf = torch.cuda.get_device_properties(dev_index).pci_bus_id.lower()
+    except Exception:
+        bdf = None
+    if not bdf:
+        try:
+            out = subprocess.run(["nvidia-smi", "-i", str(dev_index), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                                 capture_output=True, text=True, timeout=20).stdout.strip().lower()
+            bdf = out[4:] if len(out) > 12 else out       # 00000000:xx:yy.z -> 0000:xx:yy.z
+        except Exception:
+            return None, []
+    try:
+        with open(f"/sys/bus/pci/devices/{bdf}/numa_node") as f:
+            node = int(f.read().strip())
+        if node < 0:
+            return None, []
+        with open(f"/sys/devices/system/node/node{node}/cpulist") as f:
+            cpus = set()
+            for part in f.read().strip().split(","):
+                a, _, b = part.partition("-")
+                cpus.update(range(int(a), int(b or a) + 1))
+    except (OSError, ValueError):
+        return None, []
+    return node, sorted(cpus & os.sched_getaffinity(0))
+
+
+def pinned_local(n, dtype, dev_index):
+    """Pinned host buffers placed on the GPU's NUMA node: allocated and first touched by
+    this thread while it runs on that node's cores (the kernel places pages where they
+    are first touched), so host<->GPU copies do not cross the socket link.  Returns the
+    tensors and the node (None when the node or its cores are not available)."""
+    import torch
+    node, cpus = gpu_numa_cpus(dev_index)
+    old = os.sched_getaffinity(0)
+    try:
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+        bufs = [torch.empty(n, dtype=dtype, pin_memory=True) for _ in range(2)]
+        for b in bufs:
+            b.zero_()
+    finally:
+        if cpus:
+            os.sched_setaffinity(0, old)
+    return bufs, (node if cpus else None)
+
+
 def max_over_ranks(x, dist=None):
     """Max of a per-rank scalar over all ranks (identity without a process group)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
@@ -708,10 +758,8 @@ def main():
     clocks = sampler.stop()
 
     # ---- e2e: the same iteration with amplitudes resident on the host (pinned)
-    host_t = torch.empty(plan.n, dtype=torch.complex128, pin_memory=True)
-    host_t.copy_(state["t"].cpu())
-    host_out = torch.empty(plan.n, dtype=torch.complex128, pin_memory=True)
-    host_out.zero_()                      # both pinned buffers written by the CPU before the timed copies
+    (host_t, host_out), numa_node = pinned_local(plan.n, torch.complex128, local)
+    host_t.copy_(state["t"].cpu())        # both pinned buffers written by the CPU before the timed copies
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -750,7 +798,8 @@ def main():
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 # per-step phases on the stream: pinned host -> HBM copy, the iteration, HBM -> pinned host
                 "h2d_ms": h2d_ms, "iteration_ms": e2e_iter_ms, "d2h_ms": d2h_ms,
-                "h2d_GBps": nbytes / h2d_ms / 1e6, "d2h_GBps": nbytes / d2h_ms / 1e6},
+                "h2d_GBps": nbytes / h2d_ms / 1e6, "d2h_GBps": nbytes / d2h_ms / 1e6,
+                "pinned_numa_node": numa_node},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
                      "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",

@@ -2,8 +2,9 @@
 Hellmann-Feynman densities, derivative integrals and the CPHF orbital response)
 against central finite differences of complete GPU calculations
 (fin_diff.compute_Nuclear_Gradient at 1e-3 and 5e-4 bohr, Richardson-combined),
-for RHF, CID and CISD (spin-orbital and spatial) of water away from its
-equilibrium geometry, to 1e-6 relative."""
+for RHF, MP2 (through its Lagrangian densities), CID and CISD (spin-orbital and
+spatial) of water away from its equilibrium geometry, to 1e-6 relative; atomic polar
+tensors from them against the reference's finite-difference goldens."""
 import numpy as np
 import pytest
 
@@ -16,7 +17,7 @@ from apyib_gb300.gradient import nuclear_gradient  # noqa: E402
 from tests.golden.reference_energies import H2O, PARAMS  # noqa: E402
 
 CASES = [("STO-3G", "RHF"), ("STO-3G", "CISD_SO"), ("STO-3G", "CID"), ("6-31G", "CISD"), ("cc-pVDZ", "RHF"),
-         ("cc-pVDZ", "CID_SO")]
+         ("cc-pVDZ", "CID_SO"), ("STO-3G", "MP2_SO"), ("6-31G", "MP2")]
 
 
 @pytest.mark.parametrize("basis,method", CASES, ids=[f"{b}-{m}" for b, m in CASES])
@@ -39,7 +40,7 @@ def _apt_cases():
     import json
     import os
     gold = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fd_goldens.json")))
-    cases = [c for c in gold["apt"] if c["parameters"]["method"] in ("RHF", "CID", "CID_SO")]
+    cases = [c for c in gold["apt"] if c["parameters"]["method"] in ("RHF", "MP2", "MP2_SO", "CID", "CID_SO")]
     return gold, cases
 
 
