@@ -74,6 +74,9 @@ SIGNATURES = {
     "agb_cgemm_tf32x3": (_int, [_i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _int, _vp, _i64, _i64, _int, _d, _d, _vp,
                                 _i64, _vp, _sz, _vp]),
     "agb_scratch_status": (_int, [_vp, _vp]),
+    "agb_zgemm_batched": (_int, [_i64, _i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _i64, _int, _vp, _i64, _i64, _i64,
+                                 _int, _d, _d, _vp, _i64, _i64, _vp]),
+    "agb_zdet_inv_batched": (_int, [_i64, _int, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _vp]),
     "agb_gemm_timing_enable": (None, [_int]),
     "agb_gemm_timing_collect": (_int, [_d, _c.POINTER(_int), _c.POINTER(_d), _c.POINTER(_d)]),
     "agb_compute_f_so": (_int, [_vp, _i64, _vp, _vp]),

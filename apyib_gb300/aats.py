@@ -27,9 +27,10 @@ all times det(A).  The terms I_00 ... I_DS and their sum are then assembled
 exactly as apyib/aats.py:161-555 does, with the same normalisations
 (apyib/aats.py:134-158) and the same prefactor Im(I) / (4 h_R h_B).  MO
 overlaps between geometries/fields come from the GPU integral source
-(utils.compute_mo_overlap), the contractions run through the library's GEMM
-(``linalg.zmm``); det(A) and A^-1 (occupied x occupied) are formed on the host
-in FP64, as the SCF's small dense algebra is.
+(utils.compute_mo_overlap); det(A) and A^-1 (occupied x occupied) come from the
+library's batched Gauss-Jordan kernel (agb_zdet_inv_batched) and every product and
+sum from its batched complex GEMM (agb_zgemm_batched), all overlaps of a tensor at
+once, in FP64.
 
 Spatial-orbital AATs (apyib/aats.py:646-1067) are the same quantity: the
 closed-shell amplitudes are expanded to spin orbitals (alpha even, beta odd)
@@ -42,7 +43,7 @@ import numpy as np
 import torch
 
 from .device import device, to_dev
-from .linalg import zmm
+from .linalg import bdet_inv, bdot, bmm
 from .utils import compute_mo_overlap, compute_so_overlap
 
 
@@ -71,91 +72,28 @@ def so_amplitudes(t1, t2, spatial):
     return T1, T2
 
 
-def _axis(T, M, ax):
-    """M applied along axis ``ax`` of T: out[.., p, ..] = sum_q M[p, q] T[.., q, ..]."""
-    Tm = T.movedim(ax, 0)
-    shp = Tm.shape
-    out = zmm(M.contiguous(), Tm.reshape(shp[0], -1).contiguous())
-    return out.reshape((M.shape[0],) + tuple(shp[1:])).movedim(0, ax)
-
-
-class _Factors:
-    """det(A), A^-1, B, C, G of one spin-orbital overlap, restricted to the active
-    occupied orbitals [f, o) for the excitation indices."""
-
-    def __init__(self, S, o, f):
-        S = to_dev(S)
-        A = S[:o, :o].cpu().numpy()
-        Ainv = np.linalg.inv(A)
-        self.det = complex(np.linalg.det(A))
-        Ai = torch.as_tensor(Ainv).to(device())
-        SOV = S[:o, o:].contiguous()
-        SVO = S[o:, :o].contiguous()
-        C = zmm(Ai, SOV)                                   # o x v
-        B = zmm(SVO, Ai)                                   # v x o
-        self.G = (S[o:, o:] - zmm(SVO, C)).contiguous()    # v x v
-        self.B = B[:, f:].contiguous()                     # v x o_act
-        self.C = C[f:, :].contiguous()                     # o_act x v
-        self.AiT = Ai[f:, f:].transpose(0, 1).contiguous()  # (A^-1)^T on active indices
-
-    def F(self, u):
-        """A^-T u G^T for u (o_act x v)."""
-        return zmm(zmm(self.AiT, u.contiguous()), self.G, transB=True)
-
-    def q(self, r, x, s, y):
-        """sum over bra excitations (rank r, amplitudes x) and ket excitations
-        (rank s, amplitudes y) of weight * <bra|ket>, weights 1 and 1/4."""
-        if r == 0 and s == 0:
-            return self.det
-        X1 = X2 = Y1 = Y2 = Xb = Yc = None
-        if r == 1:
-            X1 = torch.sum(x * self.B.transpose(0, 1))
-        elif r == 2:
-            Xb = _axis(x, self.B.transpose(0, 1), 2).diagonal(dim1=0, dim2=2).sum(-1)   # Xb[j, b] = sum_ia x_ijab B_ai
-            X2 = torch.sum(Xb * self.B.transpose(0, 1))
-        if s == 1:
-            Y1 = torch.sum(y * self.C)
-        elif s == 2:
-            Yc = _axis(y, self.C.transpose(0, 1), 1).diagonal(dim1=1, dim2=3).sum(-1)  # Yc[k, c] = sum_ld y_klcd C_ld
-            Y2 = torch.sum(Yc * self.C)
-        if r == 0:
-            val = Y1 if s == 1 else 0.5 * Y2
-        elif s == 0:
-            val = X1 if r == 1 else 0.5 * X2
-        elif r == 1 and s == 1:
-            val = X1 * Y1 + torch.sum(x * self.F(y))
-        elif r == 1 and s == 2:
-            val = 0.5 * X1 * Y2 + torch.sum(x * self.F(Yc))
-        elif r == 2 and s == 1:
-            val = torch.sum(Xb * self.F(y)) + 0.5 * X2 * Y1
-        else:
-            yt = _axis(_axis(y, self.AiT, 0), self.AiT, 1)
-            yt = _axis(_axis(yt, self.G, 2), self.G, 3)
-            val = 0.25 * X2 * Y2 + torch.sum(Xb * self.F(Yc)) + 0.25 * torch.sum(x * yt)
-        return self.det * val                              # a device scalar: no host round trip per term
-
-
 class _Stack:
-    """The factors of _Factors for a list of overlaps, stacked along a leading axis F,
-    so that the terms of many overlaps run as one set of broadcast batched products.
-    Amplitudes passed to q_all carry a leading axis of length F or 1 (shared)."""
+    """det(A), A^-1, B, C, G of a list of spin-orbital overlaps, stacked along a leading
+    axis F and restricted to the active occupied orbitals [f, o) for the excitation
+    indices, so that the terms of many overlaps run as one set of batched products on
+    the library (agb_zdet_inv_batched for det(A) and A^-1, agb_zgemm_batched for every
+    product and sum).  Amplitudes passed to q_all carry a leading axis of length F or 1
+    (shared)."""
 
     def __init__(self, Ss, o, f):
         S = torch.stack([to_dev(x) for x in Ss])
-        A = S[:, :o, :o].cpu().numpy()
-        self.det = torch.as_tensor(np.linalg.det(A)).to(device())               # [F]
-        Ai = torch.as_tensor(np.linalg.inv(A)).to(device())
+        self.det, Ai = bdet_inv(S[:, :o, :o])                                  # [F], [F, o, o]
         SOV, SVO = S[:, :o, o:], S[:, o:, :o]
-        C = Ai @ SOV                                                            # [F, o, v]
-        B = SVO @ Ai                                                            # [F, v, o]
-        self.G = S[:, o:, o:] - SVO @ C                                         # [F, v, v]
-        self.BT = B[:, :, f:].transpose(1, 2)                                   # [F, o_act, v]
-        self.C = C[:, f:, :]                                                    # [F, o_act, v]
-        self.AiT = Ai[:, f:, f:].transpose(1, 2)                                # [F, o_act, o_act]
+        C = bmm(Ai, SOV)                                                        # [F, o, v]
+        B = bmm(SVO, Ai)                                                        # [F, v, o]
+        self.G = S[:, o:, o:] - bmm(SVO, C)                                     # [F, v, v]
+        self.BT = B[:, :, f:].transpose(1, 2).contiguous()                      # [F, o_act, v]
+        self.C = C[:, f:, :].contiguous()                                       # [F, o_act, v]
+        self.Ai = Ai[:, f:, f:].contiguous()                                    # A^-1 on the active indices
 
     def F(self, u):
         """A^-T u G^T, u [F or 1, o_act, v]."""
-        return self.AiT @ u @ self.G.transpose(1, 2)
+        return bmm(bmm(self.Ai, u, transA=True), self.G, transB=True)
 
     def q_all(self, pairs, x, y):
         """{(r, s): det * <bra rank r (amplitudes x[r]) | ket rank s (y[s])>} for the
@@ -164,21 +102,21 @@ class _Stack:
         need_s = {s for _, s in pairs}
         X1 = X2 = Xb = Y1 = Y2 = Yc = None
         if 1 in need_r:
-            X1 = (x[1] * self.BT).sum((1, 2))
+            X1 = bdot(x[1], self.BT)
         if 2 in need_r:
             x2 = x[2]
             Fx, no, _, nv, _ = x2.shape
             xm = x2.permute(0, 1, 3, 2, 4).reshape(Fx, no * nv, no * nv)            # [(i,a),(j,b)]
-            Xb = (self.BT.reshape(-1, 1, no * nv) @ xm).reshape(-1, no, nv)        # Xb[j,b] = sum_ia x_ijab B_ai
-            X2 = (Xb * self.BT).sum((1, 2))
+            Xb = bmm(self.BT.reshape(self.BT.shape[0], 1, no * nv), xm).reshape(-1, no, nv)   # sum_ia x_ijab B_ai
+            X2 = bdot(Xb, self.BT)
         if 1 in need_s:
-            Y1 = (y[1] * self.C).sum((1, 2))
+            Y1 = bdot(y[1], self.C)
         if 2 in need_s:
             y2 = y[2]
             Fy, no, _, nv, _ = y2.shape
             ym = y2.permute(0, 2, 4, 1, 3).reshape(Fy, no * nv, no * nv)            # [(l,d),(k,c)]
-            Yc = (self.C.reshape(-1, 1, no * nv) @ ym).reshape(-1, no, nv)         # Yc[k,c] = sum_ld y_klcd C_ld
-            Y2 = (Yc * self.C).sum((1, 2))
+            Yc = bmm(self.C.reshape(self.C.shape[0], 1, no * nv), ym).reshape(-1, no, nv)     # sum_ld y_klcd C_ld
+            Y2 = bdot(Yc, self.C)
         out = {}
         for r, s in pairs:
             if r == 0 and s == 0:
@@ -188,25 +126,39 @@ class _Stack:
             elif s == 0:
                 val = X1 if r == 1 else 0.5 * X2
             elif r == 1 and s == 1:
-                val = X1 * Y1 + (x[1] * self.F(y[1])).sum((1, 2))
+                val = X1 * Y1 + bdot(x[1], self.F(y[1]))
             elif r == 1 and s == 2:
-                val = 0.5 * X1 * Y2 + (x[1] * self.F(Yc)).sum((1, 2))
+                val = 0.5 * X1 * Y2 + bdot(x[1], self.F(Yc))
             elif r == 2 and s == 1:
-                val = (Xb * self.F(y[1])).sum((1, 2)) + 0.5 * X2 * Y1
+                val = bdot(Xb, self.F(y[1])) + 0.5 * X2 * Y1
             else:
                 # x.(A^-T A^-T G G) y = sum_klab (A^-1 A^-1 x)_klab (G G y)_klab: occupied
                 # factors on x, virtual factors on y
                 x2, y2 = x[2], y[2]
                 no, nv = x2.shape[1], x2.shape[3]
-                Ai = self.AiT.transpose(1, 2)
-                xa = (Ai @ x2.reshape(x2.shape[0], no, -1)).reshape(-1, no, no, nv, nv)            # k <- i
-                xa = (Ai @ xa.transpose(1, 2).reshape(xa.shape[0], no, -1)).reshape(-1, no, no, nv, nv)
+                xa = bmm(self.Ai, x2.reshape(x2.shape[0], no, -1)).reshape(-1, no, no, nv, nv)      # k <- i
+                xa = bmm(self.Ai, xa.transpose(1, 2).reshape(xa.shape[0], no, -1)).reshape(-1, no, no, nv, nv)
                 xa = xa.transpose(1, 2)                                                          # [k, l, a, b]
-                ya = (y2.reshape(y2.shape[0], -1, nv) @ self.G.transpose(1, 2)).reshape(-1, no, no, nv, nv)
-                ya = (self.G[:, None] @ ya.reshape(ya.shape[0], no * no, nv, nv)).reshape(-1, no, no, nv, nv)
-                val = 0.25 * X2 * Y2 + (Xb * self.F(Yc)).sum((1, 2)) + 0.25 * (xa * ya).sum((1, 2, 3, 4))
+                ya = bmm(y2.reshape(y2.shape[0], -1, nv), self.G, transB=True)                   # d <- b
+                ya = ya.reshape(ya.shape[0], no * no, nv, nv).permute(0, 2, 1, 3).reshape(ya.shape[0], nv, -1)
+                ya = bmm(self.G, ya)
+                ya = ya.reshape(ya.shape[0], nv, no * no, nv).permute(0, 2, 1, 3)                # c <- a
+                val = 0.25 * X2 * Y2 + bdot(Xb, self.F(Yc)) + 0.25 * bdot(xa, ya)
             out[r, s] = self.det * val
         return out
+
+
+class _Factors:
+    """_Stack of one overlap: q(r, x, s, y) is the single term as a device scalar."""
+
+    def __init__(self, S, o, f):
+        self._st = _Stack([S], o, f)
+        self.det = self._st.det[0]
+
+    def q(self, r, x, s, y):
+        xs = {r: x.unsqueeze(0)} if r else {}
+        ys = {s: y.unsqueeze(0)} if s else {}
+        return self._st.q_all([(r, s)], xs, ys)[r, s][0]      # a device scalar: no host round trip per term
 
 
 class AAT(object):

@@ -47,6 +47,58 @@ def zmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0, o
     return out
 
 
+def bmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0):
+    """Batched complex product op(A_b) @ op(B_b) for 3-D complex128 CUDA tensors
+    [batch, rows, cols] (a batch extent of 1 broadcasts: batch stride 0) through
+    agb_zgemm_batched (FP64).  Returns a new [batch, M, N] tensor."""
+    A = A.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg()
+    B = B.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg()
+    if A.dim() == 2:
+        A = A.unsqueeze(0)
+    if B.dim() == 2:
+        B = B.unsqueeze(0)
+    nb = max(A.shape[0], B.shape[0])
+    if A.shape[0] not in (1, nb) or B.shape[0] not in (1, nb):
+        raise ValueError(f"bmm: batch extents {A.shape[0]} and {B.shape[0]} do not broadcast")
+    M, K = (A.shape[2], A.shape[1]) if transA else (A.shape[1], A.shape[2])
+    K2, N = (B.shape[2], B.shape[1]) if transB else (B.shape[1], B.shape[2])
+    assert K == K2, (A.shape, B.shape, transA, transB)
+    sAm, sAk = (A.stride(2), A.stride(1)) if transA else (A.stride(1), A.stride(2))
+    sBk, sBn = (B.stride(2), B.stride(1)) if transB else (B.stride(1), B.stride(2))
+    sAb = A.stride(0) if A.shape[0] == nb and nb > 1 else 0
+    sBb = B.stride(0) if B.shape[0] == nb and nb > 1 else 0
+    out = torch.empty((nb, M, N), dtype=torch.complex128, device=device())
+    a = complex(alpha)
+    _lib.call("agb_zgemm_batched", nb, M, N, K, a.real, a.imag, ptr(A), sAm, sAk, sAb, int(conjA), ptr(B), sBk, sBn,
+              sBb, int(conjB), 0.0, 0.0, ptr(out), N, M * N, stream_ptr())
+    return out
+
+
+def bdot(X, Y):
+    """sum over all but the leading (batch) axis of X * Y (no conjugation), batches
+    broadcasting, as batched 1 x K by K x 1 products on the library's GEMM."""
+    nb = max(X.shape[0], Y.shape[0])
+    Xm = X.reshape(X.shape[0], 1, -1)
+    Ym = Y.reshape(Y.shape[0], -1, 1)
+    return bmm(Xm, Ym).reshape(nb)
+
+
+def bdet_inv(S):
+    """(det, inverse) of each matrix of a [batch, n, n] complex128 CUDA tensor through
+    agb_zdet_inv_batched (FP64 Gauss-Jordan elimination with partial pivoting, n <= 96);
+    raises if one is exactly singular."""
+    S = S.to(device=device(), dtype=torch.complex128).resolve_conj().resolve_neg().contiguous()
+    nb, n, _ = S.shape
+    inv = torch.empty_like(S)
+    det = torch.empty(nb, dtype=torch.complex128, device=device())
+    info = torch.zeros(nb, dtype=torch.int32, device=device())
+    _lib.call("agb_zdet_inv_batched", nb, n, ptr(S), n, n * n, ptr(inv), n, n * n, ptr(det), ptr(info),
+              stream_ptr())
+    if int(info.max().item()) != 0:
+        raise ZeroDivisionError("agb_zdet_inv_batched: singular matrix in the batch")
+    return det, inv
+
+
 def last_pair_symmetric(eri):
     """Whether eri[m,n,l,s] == eri[m,n,s,l] exactly, checked once per tensor object and
     version (the verdict rides on the tensor object; one modified in place is checked

@@ -123,6 +123,22 @@ agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, do
                             double beta_re, double beta_im, void* C, int64_t ldc,
                             void* scratch, size_t scratch_bytes, void* stream);
 
+/* Batched products for the overlap-based AAT terms (apyib/aats.py:120-555 evaluates
+ * each as a sum of o x o determinants; here they are a few small products per overlap):
+ * C_b = alpha * op(A_b) op(B_b) + beta * C_b for b < batch, with agb_zgemm's strides plus
+ * batch strides sAb, sBb, sCb in complex elements (0 broadcasts an operand).  FP64. */
+agb_status agb_zgemm_batched(int64_t batch, int64_t M, int64_t N, int64_t K, double alpha_re, double alpha_im,
+                             const void* A, int64_t sAm, int64_t sAk, int64_t sAb, int conjA,
+                             const void* B, int64_t sBk, int64_t sBn, int64_t sBb, int conjB,
+                             double beta_re, double beta_im, void* C, int64_t ldc, int64_t sCb, void* stream);
+/* Determinant and inverse of each n x n complex matrix A_b (row-major, leading dimension
+ * lda, batch stride sAb; 1 <= n <= 96) by Gauss-Jordan elimination with partial pivoting
+ * in FP64: Ainv_b (ldi, sIb), det[b] (complex), info[b] = 0, or k + 1 when the pivot of
+ * step k was exactly zero (outputs unspecified).  info may be NULL.  Replaces the
+ * np.linalg.det / inv of the occupied overlap blocks (apyib/aats.py:120-131). */
+agb_status agb_zdet_inv_batched(int64_t batch, int n, const void* A, int64_t lda, int64_t sAb, void* Ainv,
+                                int64_t ldi, int64_t sIb, void* det, int* info, void* stream);
+
 /* Benchmark instrumentation (no reference counterpart): when enabled, every
  * tcgen05 GEMM launch is bracketed by CUDA events on its stream;
  * agb_gemm_timing_collect reports launches, kernel milliseconds and

@@ -23,8 +23,19 @@ def on_cpu(monkeypatch):
     def to_cpu(x, dtype=torch.complex128):
         t = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.ascontiguousarray(x))
         return t.to(dtype=dtype).resolve_conj().contiguous()
+    def bmm(A, B, transA=False, conjA=False, transB=False, conjB=False, alpha=1.0):
+        A = A.mT if transA else A
+        B = B.mT if transB else B
+        return alpha * ((A.conj() if conjA else A) @ (B.conj() if conjB else B))
+
+    def bdet_inv(S):
+        return torch.linalg.det(S), torch.linalg.inv(S)
+
     monkeypatch.setattr(aats, "device", lambda: torch.device("cpu"))
     monkeypatch.setattr(aats, "to_dev", to_cpu)
+    monkeypatch.setattr(aats, "bmm", bmm)
+    monkeypatch.setattr(aats, "bdot", lambda X, Y: (X.reshape(X.shape[0], -1) * Y.reshape(Y.shape[0], -1)).sum(-1))
+    monkeypatch.setattr(aats, "bdet_inv", bdet_inv)
 
 
 def so_overlap(M):
