@@ -229,18 +229,23 @@ def cisd_energy(F_SO, ERI_SO, eps_o, eps_v, params, singles=True, precision="fp6
 # the full equations, the non-canonical MP2 that apyib/analytic_aats.py:215-549
 # differentiates for its MP2 AATs.
 
-def _mp2_fock_offdiag(t, Foo, Fvv, transpose=False):
-    """The off-diagonal part of (A t) (or A^T t) for antisymmetric t[o,o,v,v], on the
-    library's complex GEMM."""
+def mp2_fock_apply(t, Fo, Fv, transpose=False):
+    """(A t)_ijab = sum_c (F_bc t_ijac + F_ac t_ijcb) - sum_k (F_kj t_ikab + F_ki t_kjab) for
+    antisymmetric t[o,o,v,v] and the given occupied / virtual Fock blocks (F^T with
+    transpose=True), on the library's complex GEMM."""
     o, v = t.shape[0], t.shape[2]
-    Fo = Foo - torch.diag(torch.diagonal(Foo))
-    Fv = Fvv - torch.diag(torch.diagonal(Fvv))
     if transpose:
         Fo, Fv = Fo.T.contiguous(), Fv.T.contiguous()
     X = zmm(t.reshape(o * o * v, v), Fv, transB=True).reshape(o, o, v, v)     # sum_c F_bc t_ijac
     Tk = t.permute(1, 0, 2, 3).reshape(o, o * v * v).contiguous()
     Z = zmm(Fo, Tk, transA=True).reshape(o, o, v, v).permute(1, 0, 2, 3)      # sum_k F_kj t_ikab
     return (X - X.transpose(2, 3)) - (Z - Z.transpose(0, 1))
+
+
+def _mp2_fock_offdiag(t, Foo, Fvv, transpose=False):
+    """The off-diagonal part of (A t) (or A^T t)."""
+    return mp2_fock_apply(t, Foo - torch.diag(torch.diagonal(Foo)), Fvv - torch.diag(torch.diagonal(Fvv)),
+                          transpose=transpose)
 
 
 def _mp2_denominators(Foo, Fvv):

@@ -34,7 +34,7 @@ import torch
 from . import _lib
 from .aats import AAT
 from .device import device, ptr, stream_ptr, to_dev, workspace
-from .linalg import jk_fock
+from .linalg import apply_axis, cg_solve, jk_fock, zmm
 
 
 def _ao2mo(ERI_AO, C):
@@ -49,10 +49,15 @@ def _ao2mo(ERI_AO, C):
 
 
 def _u_terms(G, U):
-    """First-order change of (pq|rs) when C -> C (1 + U)."""
-    Uc = U.conj()
-    return (torch.einsum("tp,tqrs->pqrs", Uc, G) + torch.einsum("tq,ptrs->pqrs", U, G)
-            + torch.einsum("tr,pqts->pqrs", Uc, G) + torch.einsum("ts,pqrt->pqrs", U, G))
+    """First-order change of (pq|rs) when C -> C (1 + U): one index at a time, each a
+    library GEMM over the other three."""
+    Uc = U.conj().resolve_conj()
+    return apply_axis(G, Uc, 0) + apply_axis(G, U, 1) + apply_axis(G, Uc, 2) + apply_axis(G, U, 3)
+
+
+def _mo(Cc, M):
+    """C^H M C for an AO matrix M (library GEMMs)."""
+    return zmm(zmm(Cc, M.to(torch.complex128), transA=True, conjA=True), Cc)
 
 
 class analytic_derivative(object):
@@ -90,95 +95,99 @@ class analytic_derivative(object):
         self.ERI_AO = ERI_AO
         G = _ao2mo(ERI_AO, Cc)                                    # all-MO (pq|rs)
         self.G = G
-        Gr = G.real.cpu().numpy()
+        Gr = G.real.to(torch.complex128)                          # real orbitals: real integrals
         o, v = slice(0, no), slice(no, nbf)
+        dev = C.device
+        e = torch.as_tensor(eps).to(dev)
+        de = (e[no:, None] - e[None, :no]).reshape(-1)            # e_a - e_i, (a, i) row-major
         Co = Cc[:, :no].contiguous()
-        zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=C.device)
+        Dh = zmm(Co, Co, transB=True, conjB=True)
+        zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=dev)
         h_AO = to_dev(np.asarray(H.T) + np.asarray(H.V))
-        F_AO = jk_fock(ERI_AO, Co @ Co.conj().T, h_AO, 1.0)
-        self.F_MO = Cc.conj().T @ F_AO @ Cc
+        F_AO = jk_fock(ERI_AO, Dh, h_AO, 1.0)
+        self.F_MO = _mo(Cc, F_AO)
         # nuclear CPHF (real), U_oo = -S_oo / 2, U_vv = -S_vv / 2
         Sd = m.oei_deriv_all(_lib.OEI_OVERLAP)
         hd = m.oei_deriv_all(_lib.OEI_KINETIC) + m.oei_deriv_all(_lib.OEI_POTENTIAL)
         Hd = m.oei_deriv_all(_lib.OEI_OVERLAP_HALF)
         Gd = m.eri_deriv_all()
-        A = (4.0 * Gr[v, o, v, o] - Gr[v, v, o, o].transpose(0, 2, 1, 3) - Gr[v, o, o, v].transpose(0, 2, 3, 1))
-        A = A.reshape(nv * no, nv * no)
-        A[np.diag_indices_from(A)] += (eps[no:][:, None] - eps[:no][None, :]).reshape(-1)
-        Cn = self.C
+        A = (4.0 * Gr[v, o, v, o] - Gr[v, v, o, o].permute(0, 2, 1, 3) - Gr[v, o, o, v].permute(0, 2, 3, 1))
+        A = A.reshape(nv * no, nv * no) + torch.diag(de.to(torch.complex128))
+        Gvooo = (2.0 * Gr[v, o, o, o] - Gr[v, o, o, o].permute(0, 2, 1, 3)).reshape(nv * no, no * no)
         rhs, self.SR, self.skelF, self.skelG, self.HR = [], [], [], [], []
         for K in range(natom):
             for c in range(3):
                 GR = Gd[K, c].contiguous()
-                dF_AO = hd[K, c].to(torch.complex128) + jk_fock(GR, (Co @ Co.conj().T), zero, 1.0)
-                Fm = (Cc.conj().T @ dF_AO @ Cc)
-                S = Cn.T @ Sd[K, c].cpu().numpy() @ Cn
-                B = Fm.real.cpu().numpy()[v, o] - S[v, o] * eps[None, :no] \
-                    - np.einsum("kl,aikl->ai", S[o, o], 2.0 * Gr[v, o, o, o] - Gr[v, o, o, o].transpose(0, 2, 1, 3))
+                dF_AO = hd[K, c].to(torch.complex128) + jk_fock(GR, Dh, zero, 1.0)
+                Fm = _mo(Cc, dF_AO)
+                S = _mo(Cc, Sd[K, c])
+                # B_ai = F^R_ai - S_ai e_i - sum_kl S_kl [2(ai|kl) - (ak|il)]
+                B = Fm[v, o] - S[v, o] * e[None, :no] - zmm(Gvooo, S[o, o].reshape(-1, 1)).reshape(nv, no)
                 rhs.append(-B.reshape(-1))
                 self.SR.append(S)
                 self.skelF.append(Fm)
                 self.skelG.append(_ao2mo(GR, Cc))
-                self.HR.append(Cc.conj().T @ Hd[K, c].to(torch.complex128) @ Cc)
-        X = np.linalg.solve(A, np.stack(rhs, axis=1))
+                self.HR.append(_mo(Cc, Hd[K, c]))
+        X = cg_solve(A, torch.stack(rhs, dim=1))
         nf = H.basis_set.n_frozen_core()
         self.nfzc = nf
+        idx = torch.arange(no, device=dev)
+        cross = (idx[:, None] < nf) != (idx[None, :] < nf)         # frozen-active pairs
+        den = (e[None, :no] - e[:no, None]).to(torch.complex128)
+        den = torch.where(cross, den, torch.ones_like(den))
+        if nf:
+            M1 = (4.0 * Gr[o, o, v, o] - Gr[o, v, o, o].permute(0, 2, 1, 3)
+                  - Gr[o, o, o, v].permute(0, 2, 3, 1)).reshape(no * no, nv * no)
+            M2 = (2.0 * Gr[o, o, o, o] - Gr[o, o, o, o].permute(0, 2, 1, 3)).reshape(no * no, no * no)
         self.UR = []
         for n, S in enumerate(self.SR):
-            U = -0.5 * S.copy()
+            U = -0.5 * S.clone()
             U[v, o] = X[:, n].reshape(nv, no)
             U[o, v] = -S[o, v] - U[v, o].T
             if nf:
                 # frozen-active rotations change a frozen-core energy: the orbitals stay canonical,
                 # U_ij = (F^R_ij - e_j S_ij + G[dD]_ij) / (e_j - e_i) for i, j in different blocks
-                Uvo = U[v, o]
-                Gd = (np.einsum("bk,ijbk->ij", Uvo, 4.0 * Gr[o, o, v, o] - Gr[o, v, o, o].transpose(0, 2, 1, 3)
-                                - Gr[o, o, o, v].transpose(0, 2, 3, 1))
-                      - np.einsum("kl,ijkl->ij", S[o, o], 2.0 * Gr[o, o, o, o] - Gr[o, o, o, o].transpose(0, 2, 1, 3)))
-                Bo = self.skelF[n].real.cpu().numpy()[o, o] - S[o, o] * eps[None, :no] + Gd
-                den = eps[None, :no] - eps[:no, None]
-                for i in range(no):
-                    for j in range(no):
-                        if (i < nf) != (j < nf):
-                            U[i, j] = Bo[i, j] / den[i, j]
-            self.UR.append(torch.as_tensor(U).to(C.device).to(torch.complex128))
+                Gdd = (zmm(M1, U[v, o].reshape(-1, 1)) - zmm(M2, S[o, o].reshape(-1, 1))).reshape(no, no)
+                Bo = self.skelF[n][o, o] - S[o, o] * e[None, :no] + Gdd
+                U[o, o] = torch.where(cross, Bo / den, U[o, o])
+            self.UR.append(U.contiguous())
         # magnetic CPHF: U^B = i X with X_ai real, X_ia = X_ai, zero within occ and within vir
         L = m.ao_angular_momentum(return_torch=True)
-        Am = (Gr[v, o, o, v].transpose(0, 2, 3, 1) - Gr[v, v, o, o].transpose(0, 2, 1, 3)).reshape(nv * no, nv * no)
-        Am[np.diag_indices_from(Am)] += (eps[no:][:, None] - eps[:no][None, :]).reshape(-1)
-        self.hB, rhsB = [], []
+        Am = (Gr[v, o, o, v].permute(0, 2, 3, 1) - Gr[v, v, o, o].permute(0, 2, 1, 3)).reshape(nv * no, nv * no)
+        Am = Am + torch.diag(de.to(torch.complex128))
+        self.hB, rhsB, Ys = [], [], []
         for b in range(3):
-            Y = Cn.T @ (0.5 * L[b].cpu().numpy()) @ Cn           # h^B = i Y (MO)
-            self.hB.append(torch.as_tensor(1j * Y).to(C.device))
+            Y = _mo(Cc, 0.5 * L[b])                              # h^B = i Y (MO), Y real
+            Ys.append(Y)
+            self.hB.append(1j * Y)
             rhsB.append(-Y[v, o].reshape(-1))
         self.Am = Am
-        XB = np.linalg.solve(Am, np.stack(rhsB, axis=1))
+        XB = cg_solve(Am, torch.stack(rhsB, dim=1))
+        if nf:
+            N1 = Gr[o, o, v, o].permute(0, 3, 2, 1).reshape(no * no, nv * no)     # (ik|bj) as [i, j, (b, k)]
+            N2 = Gr[o, v, o, o].permute(0, 3, 1, 2).reshape(no * no, nv * no)     # (ib|kj) as [i, j, (b, k)]
         self.UB = []
         for b in range(3):
-            U = np.zeros((nbf, nbf), dtype=complex)
+            U = torch.zeros((nbf, nbf), dtype=torch.complex128, device=dev)
             Xvo = XB[:, b].reshape(nv, no)
             U[v, o] = 1j * Xvo
             U[o, v] = 1j * Xvo.T
             if nf:
                 # canonical frozen-active rotations: U_ij = (h^B_ij + G[dD]_ij) / (e_j - e_i),
                 # G[dD]_ij = i sum_bk X_bk [(ik|bj) - (ib|kj)]
-                Yb = self.hB[b].imag.cpu().numpy()
-                Gd = np.einsum("bk,ikbj->ij", Xvo, Gr[o, o, v, o]) - np.einsum("bk,ibkj->ij", Xvo, Gr[o, v, o, o])
-                den = eps[None, :no] - eps[:no, None]
-                for i in range(no):
-                    for j in range(no):
-                        if (i < nf) != (j < nf):
-                            U[i, j] = 1j * (Yb[i, j] + Gd[i, j]) / den[i, j]
-            self.UB.append(torch.as_tensor(U).to(C.device))
+                Gdd = zmm(N1 - N2, Xvo.reshape(-1, 1)).reshape(no, no)
+                U[o, o] = torch.where(cross, 1j * (Ys[b][o, o] + Gdd) / den, U[o, o])
+            self.UB.append(U.contiguous())
 
     def _dH(self, U, skelF=None, skelG=None, hx=None):
         """MO derivative Fock matrix and ERIs for orbital response U (+ skeleton parts)."""
         Cc, no, nbf = self.Cc, self.no, self.nbf
         zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=Cc.device)
-        dC = Cc @ U
-        Co, dCo = Cc[:, :no], dC[:, :no]
-        dD = dCo @ Co.conj().T + Co @ dCo.conj().T
-        dF = U.conj().T @ self.F_MO + self.F_MO @ U + Cc.conj().T @ jk_fock(self.ERI_AO, dD.contiguous(), zero, 1.0) @ Cc
+        dC = zmm(Cc, U)
+        Co, dCo = Cc[:, :no].contiguous(), dC[:, :no].contiguous()
+        dD = zmm(dCo, Co, transB=True, conjB=True) + zmm(Co, dCo, transB=True, conjB=True)
+        dF = (zmm(U, self.F_MO, transA=True, conjA=True) + zmm(self.F_MO, U)
+              + _mo(Cc, jk_fock(self.ERI_AO, dD.contiguous(), zero, 1.0)))
         if skelF is not None:
             dF = dF + skelF
         if hx is not None:
@@ -232,6 +241,7 @@ class analytic_derivative(object):
         64-87) and their responses from the first-order non-canonical MP2 equation
         <ab||ij> + P(F_vv t) - P(F_oo t) = 0 (the Fock terms of apyib/ci_wfn.py:324-327):
         t^x = [<ab||ij>^x + F^x_bc t_ijac + F^x_ac t_ijcb - F^x_kj t_ikab - F^x_ki t_kjab] / D."""
+        from .adjoint import mp2_fock_apply
         from .utils import compute_ERI_SO, compute_F_SO
         no, nbf, nf = self.no, self.nbf, self.nfzc
         o = 2 * (no - nf)
@@ -247,9 +257,7 @@ class analytic_derivative(object):
         def respond(dF, dG):
             Fs = compute_F_SO(None, dF[t_, t_].contiguous(), return_torch=True)
             Fo, Fv = Fs[:o, :o], Fs[o:, o:]
-            r = antisym(dG)
-            r = r + torch.einsum("bc,ijac->ijab", Fv, t) + torch.einsum("ac,ijcb->ijab", Fv, t)
-            r = r - torch.einsum("kj,ikab->ijab", Fo, t) - torch.einsum("ki,kjab->ijab", Fo, t)
+            r = antisym(dG) + mp2_fock_apply(t, Fo, Fv)
             return (None, r / D)
         tR = [respond(*self._dH(self.UR[n], self.skelF[n], self.skelG[n])) for n in range(len(self.UR))]
         tB = [respond(*self._dH(self.UB[b], hx=self.hB[b])) for b in range(3)]
@@ -287,7 +295,7 @@ class analytic_derivative(object):
             for a in range(n3):
                 ov["pu", a], ov["nu", a] = eye + eps * Xs[a], eye - eps * Xs[a]
                 for b in range(3):
-                    XY = eps * eps * (Xs[a] @ Ys[b])
+                    XY = eps * eps * zmm(Xs[a], Ys[b])
                     ov["pp", a, b] = eye + eps * Xs[a] + eps * Ys[b] + XY
                     ov["pn", a, b] = eye + eps * Xs[a] - eps * Ys[b] - XY
                     ov["np", a, b] = eye - eps * Xs[a] + eps * Ys[b] - XY

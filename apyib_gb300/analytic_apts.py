@@ -15,8 +15,10 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from .analytic_aats import _mo
 from .analytic_aats import analytic_derivative as _aat_derivative
 from .gradient import apt as _apt
+from .linalg import cg_solve
 
 
 class analytic_derivative(_aat_derivative):
@@ -26,21 +28,21 @@ class analytic_derivative(_aat_derivative):
     def compute_RHF_APTs_VG(self, orbitals="non-canonical"):
         from .integrals import MintsHelper
         self._setup()
-        nbf, no, Cn = self.nbf, self.no, self.C
+        nbf, no, Cc = self.nbf, self.no, self.Cc
         nv = nbf - no
         v, o = slice(no, nbf), slice(0, no)
         nab = MintsHelper(self.H.basis_set).ao_nabla(return_torch=True)
         UE, hE, rhs = [], [], []
         for b in range(3):
-            Y = Cn.T @ nab[b].cpu().numpy() @ Cn                 # h^E = i Y, Y = <p| d/dr_b |q>
-            hE.append(torch.as_tensor(1j * Y).to(self.Cc.device))
+            Y = _mo(Cc, nab[b])                                  # h^E = i Y, Y = <p| d/dr_b |q>
+            hE.append(1j * Y)
             rhs.append(-Y[v, o].reshape(-1))
-        X = np.linalg.solve(self.Am, np.stack(rhs, axis=1))
+        X = cg_solve(self.Am, torch.stack(rhs, dim=1))
         for b in range(3):
-            U = np.zeros((nbf, nbf), dtype=complex)
+            U = torch.zeros((nbf, nbf), dtype=torch.complex128, device=Cc.device)
             U[v, o] = 1j * X[:, b].reshape(nv, no)
             U[o, v] = 1j * X[:, b].reshape(nv, no).T
-            UE.append(torch.as_tensor(U).to(self.Cc.device))
+            UE.append(U)
         self.UB, self.hB = UE, hE
         I = self._aats("RHF", "intermediate", setup=False)
         Z = self.H.molecule.Z.astype(float)

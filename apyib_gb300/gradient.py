@@ -24,9 +24,10 @@ response: U_ai from the closed-shell CPHF equations
       = -(F^R_ai - eps_i S^R_ai - sum_kl S^R_kl [2(ai|kl) - (ak|il)]),
 U_pq = -S^R_pq / 2 within the occupied and within the virtual space (the CI
 energy is invariant to those rotations when no orbital is frozen) and
-U_ia = -S^R_ia - U_ai.  The CPHF matrix (n_vir n_occ square) is solved on the
-host in FP64 for all 3N perturbations at once, like the SCF's small dense
-algebra; the integrals, transforms and contractions run on the GPU.
+U_ia = -S^R_ia - U_ai.  The CPHF equations (n_vir n_occ square, positive definite
+for a stable RHF solution) are solved on the device for all 3N perturbations at
+once by preconditioned conjugate gradients (linalg.cg_solve); the integrals,
+transforms and contractions run on the GPU through the library.
 """
 from __future__ import annotations
 
@@ -124,8 +125,9 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False, geometry=
             hd = hd - F_el[beta] * geo["dmu"][:, :, beta]
     Cd = to_dev(C, torch.float64)
     Co = Cd[:, :no].contiguous()
-    Dh = (Co @ Co.T).contiguous()                                # C_o C_o^T
-    Wd = 2.0 * Co @ torch.diag(torch.as_tensor(eps[:no]).to(Co)) @ Co.T
+    Coz = Co.to(torch.complex128)
+    Dh = zmm(Coz, Coz, transB=True).real.contiguous()            # C_o C_o^T
+    Wd = 2.0 * zmm(Coz * torch.as_tensor(eps[:no]).to(Coz)[None, :], Coz, transB=True).real
     Dc = (2.0 * Dh).to(torch.complex128)
     zero = torch.zeros((nbf, nbf), dtype=torch.complex128, device=Co.device)
     g_hf = np.zeros((natom, 3))
@@ -147,39 +149,41 @@ def nuclear_gradient(parameters, precision="fp64", return_parts=False, geometry=
                                                          return_intermediates=True)
     Y, G_AO = inter["Y"], inter["G_AO"]
     dEdC_r = (dEdC + dEdCc).real                                 # real orbitals, real responses
-    # CPHF with all-MO integrals (real)
+    # CPHF with all-MO integrals (real orbitals: real integrals), on the device
+    from .analytic_aats import _mo
+    from .linalg import cg_solve
     from .utils import compute_ERI_MO
     ERI = compute_ERI_MO(params, wfn, [slice(0, 0), slice(0, no), slice(no, nbf), slice(0, nbf)],
-                         return_torch=True).real.cpu().numpy()
+                         return_torch=True).real.to(torch.complex128)
     o, v = slice(0, no), slice(no, nbf)
     nv = nbf - no
-    # A[a,i,b,j] = 4(ai|bj) - (ab|ij) - (aj|ib)
-    A = (4.0 * ERI[v, o, v, o] - ERI[v, v, o, o].transpose(0, 2, 1, 3) - ERI[v, o, o, v].transpose(0, 2, 3, 1))
-    A = A.reshape(nv * no, nv * no)
-    A[np.diag_indices_from(A)] += (eps[no:][:, None] - eps[:no][None, :]).reshape(-1)
-    Ch = C
+    e = torch.as_tensor(eps).to(Co.device)
+    # A[a,i,b,j] = 4(ai|bj) - (ab|ij) - (aj|ib) + (e_a - e_i) delta
+    A = (4.0 * ERI[v, o, v, o] - ERI[v, v, o, o].permute(0, 2, 1, 3) - ERI[v, o, o, v].permute(0, 2, 3, 1))
+    A = A.reshape(nv * no, nv * no) + torch.diag((e[no:, None] - e[None, :no]).reshape(-1).to(torch.complex128))
+    Gvooo = (2.0 * ERI[v, o, o, o] - ERI[v, o, o, o].permute(0, 2, 1, 3)).reshape(nv * no, no * no)
+    Cz = Cd.to(torch.complex128)
     rhs, S_mo = [], {}
     skel = np.zeros((natom, 3))
     for K in range(natom):
         for c in range(3):
             dF_AO = hd[K, c].to(torch.complex128) + jk_fock(GR[K, c], Dh.to(torch.complex128), zero, 1.0)
             skel[K, c] = float((torch.sum(Y * dF_AO) + torch.sum(G_AO * GR[K, c])).real)
-            F_mo = Ch.T @ dF_AO.real.cpu().numpy() @ Ch
-            S = Ch.T @ Sd[K, c].cpu().numpy() @ Ch
+            F_mo = _mo(Cz, dF_AO.real)
+            S = _mo(Cz, Sd[K, c])
             S_mo[K, c] = S
-            B = F_mo[v, o] - S[v, o] * eps[None, :no] \
-                - np.einsum("kl,aikl->ai", S[o, o], 2.0 * ERI[v, o, o, o] - ERI[v, o, o, o].transpose(0, 2, 1, 3))
+            B = F_mo[v, o] - S[v, o] * e[None, :no] - zmm(Gvooo, S[o, o].reshape(-1, 1)).reshape(nv, no)
             rhs.append(-B.reshape(-1))
-    Uvo = np.linalg.solve(A, np.stack(rhs, axis=1))
+    Uvo = cg_solve(A, torch.stack(rhs, dim=1))
     orb = np.zeros((natom, 3))
     n = 0
     for K in range(natom):
         for c in range(3):
             S = S_mo[K, c]
-            U = -0.5 * S.copy()
+            U = -0.5 * S.clone()
             U[v, o] = Uvo[:, n].reshape(nv, no)
             U[o, v] = -S[o, v] - U[v, o].T
-            dC = zmm(Cd.to(torch.complex128), torch.as_tensor(U).to(Cd.device).to(torch.complex128)).real
+            dC = zmm(Cz, U).real
             orb[K, c] = float(torch.sum(dEdC_r * dC))
             n += 1
     g = g_hf + skel + orb

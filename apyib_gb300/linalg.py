@@ -83,6 +83,49 @@ def bdot(X, Y):
     return bmm(Xm, Ym).reshape(nb)
 
 
+def apply_axis(T, M, axis):
+    """out[.., p, ..] = sum_t M[t, p] T[.., t, ..] along ``axis`` of a complex CUDA tensor:
+    one library GEMM (agb_zgemm) over the other axes flattened."""
+    Tm = T.movedim(axis, -1)
+    shp = tuple(Tm.shape)
+    out = zmm(Tm.reshape(-1, shp[-1]), M)
+    return out.reshape(shp[:-1] + (M.shape[1],)).movedim(-1, axis)
+
+
+def cg_solve(A, B, tol=1e-14, max_iterations=1000):
+    """X with A X = B for a symmetric positive-definite A (n x n) and right-hand sides
+    B (n x k), by the conjugate-gradient method with a diagonal (Jacobi) preconditioner,
+    every column its own recurrence, products on the library's GEMM; FP64 on the device.
+    Stops when every column's residual norm is below tol times its right-hand side's
+    norm and raises if that takes more than max_iterations steps.  Used for the
+    coupled-perturbed Hartree-Fock equations, whose matrices (the real and imaginary
+    orbital Hessians of a stable RHF solution) are positive definite."""
+    A = A.to(device=device(), dtype=torch.complex128).contiguous()
+    B = B.to(device=device(), dtype=torch.complex128).reshape(A.shape[0], -1).contiguous()
+    dinv = (1.0 / torch.diagonal(A).real).to(torch.complex128).reshape(-1, 1)
+    X = (dinv * B).contiguous()
+    R = B - zmm(A, X)
+    Z = dinv * R
+    P = Z.clone()
+    rz = bdot(R.T.unsqueeze(1).conj(), Z.T.unsqueeze(1)).real
+    bn = bdot(B.T.unsqueeze(1).conj(), B.T.unsqueeze(1)).real.sqrt().clamp_min(1e-300)
+    for _ in range(max_iterations):
+        rn = bdot(R.T.unsqueeze(1).conj(), R.T.unsqueeze(1)).real.sqrt()
+        if bool((rn <= tol * bn).all()):
+            return X
+        AP = zmm(A, P.contiguous())
+        pap = bdot(P.T.unsqueeze(1).conj(), AP.T.unsqueeze(1)).real
+        alpha = torch.where(pap > 0, rz / pap.clamp_min(1e-300), torch.zeros_like(rz))
+        X = X + alpha.to(torch.complex128) * P
+        R = R - alpha.to(torch.complex128) * AP
+        Z = dinv * R
+        rz_new = bdot(R.T.unsqueeze(1).conj(), Z.T.unsqueeze(1)).real
+        beta = torch.where(rz > 0, rz_new / rz.clamp_min(1e-300), torch.zeros_like(rz))
+        P = Z + beta.to(torch.complex128) * P
+        rz = rz_new
+    raise RuntimeError("cg_solve: no convergence (is the matrix positive definite?)")
+
+
 def bdet_inv(S):
     """(det, inverse) of each matrix of a [batch, n, n] complex128 CUDA tensor through
     agb_zdet_inv_batched (FP64 Gauss-Jordan elimination with partial pivoting, n <= 96);
