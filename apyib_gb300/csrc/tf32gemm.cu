@@ -17,6 +17,7 @@
 #include <cudaTypedefs.h>
 
 #include <atomic>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -58,13 +59,30 @@ agb_status zgemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64
 namespace {
 using namespace tc05;
 
-constexpr int BM = 128, BN = 256, BK = 16;   // BK in fp32 elements (64 bytes)
-constexpr int STAGES = 2;
-constexpr int A_TILE_BYTES = BM * BK * 4;                    // 8 KB per A plane tile
-constexpr int B_TILE_BYTES = BN * BK * 4;                    // 16 KB per B plane tile
-constexpr int STAGE_BYTES = 4 * (A_TILE_BYTES + B_TILE_BYTES);   // 96 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int BM = 128, BN = 256, BK = 16;   // K padding of the planes, in fp32 elements (64 bytes)
 constexpr int THREADS = 192;
+// Pipeline shapes: a k-block of KB fp32 elements per stage (KB * 4 bytes per row, the TMA /
+// MMA swizzle width), STAGES stages.  KB = 16: 2 stages of 96 KB; KB = 8: 4 stages of 48 KB.
+template <int KB> struct Pipe {
+  static constexpr int STAGES = KB == 16 ? 2 : 4;
+  static constexpr int A_TILE_BYTES = BM * KB * 4;
+  static constexpr int B_TILE_BYTES = BN * KB * 4;
+  static constexpr int STAGE_BYTES = 4 * (A_TILE_BYTES + B_TILE_BYTES);
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+  static constexpr uint32_t SBO = 8 * KB * 4;                 // 8-row group stride of the swizzled layout
+  static constexpr uint64_t LAYOUT = KB == 16 ? 4 : 6;        // tcgen05 descriptor: 64-byte / 32-byte swizzle
+};
+
+// tcgen05 shared-memory descriptor of a K-major swizzled tile for the pipeline shape KB.
+template <int KB> __device__ __forceinline__ uint64_t make_desc_kb(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(Pipe<KB>::SBO >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= Pipe<KB>::LAYOUT << 61;
+  return d;
+}
 constexpr unsigned TMEM_COLS = 2 * BN;                       // Re and Im accumulators
 constexpr int kGroupM = 12;                      // tile rows per raster group
 
@@ -96,9 +114,12 @@ struct GemmParams {
   int64_t rowsA, rowsB;  // padded rows per plane
 };
 
+template <int KB>
 __global__ void __launch_bounds__(THREADS, 1)
 tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    GemmParams p) {
+  constexpr int STAGES = Pipe<KB>::STAGES, STAGE_BYTES = Pipe<KB>::STAGE_BYTES;
+  constexpr int A_TILE_BYTES = Pipe<KB>::A_TILE_BYTES, B_TILE_BYTES = Pipe<KB>::B_TILE_BYTES;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -152,7 +173,7 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
         if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
         uint8_t* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-        int kx = (kb0 + kb) * BK;
+        int kx = (kb0 + kb) * KB;
         for (int pl = 0; pl < 4; ++pl) {
           tma_load_2d(st + pl * A_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
           tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kx,
@@ -184,12 +205,12 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
         uint32_t st = smem_u32(smem + s * STAGE_BYTES);
         // planes: 0 Ar_hi 1 Ar_lo 2 Ai_hi 3 Ai_lo | 4 Br_hi 5 Br_lo 6 Bi_hi 7 Bi_lo
 #pragma unroll
-        for (int ks = 0; ks < BK / 8; ++ks) {
+        for (int ks = 0; ks < KB / 8; ++ks) {
           uint64_t a[4], b[4];
 #pragma unroll
           for (int pl = 0; pl < 4; ++pl) {
-            a[pl] = make_desc(st + pl * A_TILE_BYTES + ks * 32);
-            b[pl] = make_desc(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
+            a[pl] = make_desc_kb<KB>(st + pl * A_TILE_BYTES + ks * 32);
+            b[pl] = make_desc_kb<KB>(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
           }
           uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
           // Re: Ar Br - Ai Bi
@@ -321,17 +342,28 @@ int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() { return tma_encode_fn(); }
 
-bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp, int box_rows) {
+bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp, int box_rows, int kb) {
   auto enc = get_encode();
   if (!enc) return false;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
   cuuint64_t strides[1] = {(cuuint64_t)(Kp * sizeof(float))};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)kb, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1u, 1u};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, kb == 16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
+}
+
+// Pipeline shape of the tensor-core GEMM: AGB_TF32_KB=8 selects 4 stages of 8-wide k-blocks
+// (default: 2 stages of 16-wide ones).
+int pipe_kb() {
+  static int kb = 0;
+  if (!kb) {
+    const char* e = getenv("AGB_TF32_KB");
+    kb = (e && atoi(e) == 8) ? 8 : 16;
+  }
+  return kb;
 }
 
 }  // namespace
@@ -382,19 +414,23 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
-  const int64_t Mp = tf32_rows_pad(M), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K), nkb = Kp / BK;
+  const int kb = pipe_kb();
+  const int64_t Mp = tf32_rows_pad(M), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K), nkb = Kp / kb;
   AGB_ARG_CHECK(Mp / BM <= 65535, "tf32_gemm_planes: grid too large");
-  int splits = partials ? choose_splits(M, N, nkb, partial_bytes) : 1;
+  int splits = partials ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
   CUtensorMap mA, mB;
-  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM) || !encode_planes(&mB, (float*)PB, 4 * Np, Kp, BN)) {
+  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb) || !encode_planes(&mB, (float*)PB, 4 * Np, Kp, BN, kb)) {
     agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
   static bool attr_set = false;
   if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Pipe<16>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Pipe<8>::SMEM_BYTES));
     attr_set = true;
   }
   GemmParams p;
@@ -408,7 +444,10 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     AGB_CUDA_TRY(cudaEventCreate(&ev1));
     AGB_CUDA_TRY(cudaEventRecord(ev0, stream));
   }
-  tf32x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
+  if (kb == 8)
+    tf32x3_gemm_kernel<8><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
+  else
+    tf32x3_gemm_kernel<16><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
   AGB_LAUNCH_CHECK();
   if (ev0) {
     AGB_CUDA_TRY(cudaEventRecord(ev1, stream));
