@@ -93,14 +93,24 @@ constexpr int kMp2Blocks = 152 * 4;
 __global__ void __launch_bounds__(256) mp2_kernel(const z64* __restrict__ R0p, const z64* __restrict__ Wop,
                                                   const double* __restrict__ invD2, int64_t n2,
                                                   z64* __restrict__ t2p, z64* __restrict__ partial) {
-  z64 acc = zmk(0, 0);
+  // t = <ab||ij> / D in FP64 (two multiplies); the energy sum W t in double-float on the
+  // FP32 pipe (~2^-44 relative): complex FP64 multiply-adds per element would make this
+  // stream FP64-pipe bound on GB300
+  float er = 0.f, erc = 0.f, ei = 0.f, eic = 0.f;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n2; e += (int64_t)gridDim.x * blockDim.x) {
     const double inv = invD2[e];
-    z64 num = R0p[e];
-    z64 t = zmk(num.x * inv, num.y * inv);
+    const z64 num = R0p[e];
+    const z64 t = zmk(num.x * inv, num.y * inv);
     t2p[e] = t;
-    acc = zadd(acc, zmul(Wop[e], t));
+    const float4 w = split_z_fast(Wop[e]);
+    const float4 tv = split_z_fast(t);
+    // w t = (wr tr - wi ti) + i (wr ti + wi tr)
+    df_mac(er, erc, w.x, w.y, tv.x, tv.y);
+    df_mac(er, erc, -w.z, -w.w, tv.z, tv.w);
+    df_mac(ei, eic, w.x, w.y, tv.z, tv.w);
+    df_mac(ei, eic, w.z, w.w, tv.x, tv.y);
   }
+  z64 acc = zmk(df_to_double(er, erc), df_to_double(ei, eic));
   __shared__ z64 sh[32];
   acc = warp_sum(acc);
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

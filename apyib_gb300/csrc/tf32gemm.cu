@@ -102,6 +102,30 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
       : "memory");
 }
 
+// The same MMA with the A operand kept in the tensor core's collector buffer: FILL reads A
+// from shared memory and keeps it, USE takes it from the buffer (the descriptor names the
+// same tile), LAST uses it a final time and releases the buffer.
+enum CollA { kFill, kUse, kLast };
+template <CollA C>
+__device__ __forceinline__ void mma_tf32_coll(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+  if constexpr (C == kFill)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32.collector::a::fill [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+  else if constexpr (C == kUse)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32.collector::a::use [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+
 struct GemmParams {
   int64_t M, N;
   int nkb;          // k-blocks per split
@@ -114,7 +138,7 @@ struct GemmParams {
   int64_t rowsA, rowsB;  // padded rows per plane
 };
 
-template <int KB>
+template <int KB, bool COLL>
 __global__ void __launch_bounds__(THREADS, 1)
 tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    GemmParams p) {
@@ -213,20 +237,36 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
             b[pl] = make_desc_kb<KB>(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
           }
           uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-          // Re: Ar Br - Ai Bi
-          mma_tf32(d_re, a[1], b[0], id_pos, acc0);
-          mma_tf32(d_re, a[0], b[1], id_pos, 1u);
-          mma_tf32(d_re, a[0], b[0], id_pos, 1u);
-          mma_tf32(d_re, a[3], b[2], id_neg, 1u);
-          mma_tf32(d_re, a[2], b[3], id_neg, 1u);
-          mma_tf32(d_re, a[2], b[2], id_neg, 1u);
-          // Im: Ar Bi + Ai Br
-          mma_tf32(d_im, a[1], b[2], id_pos, acc0);
-          mma_tf32(d_im, a[0], b[3], id_pos, 1u);
-          mma_tf32(d_im, a[0], b[2], id_pos, 1u);
-          mma_tf32(d_im, a[3], b[0], id_pos, 1u);
-          mma_tf32(d_im, a[2], b[1], id_pos, 1u);
-          mma_tf32(d_im, a[2], b[0], id_pos, 1u);
+          if constexpr (COLL) {
+            // the same 12 products grouped by A plane, each plane read from shared memory once
+            mma_tf32_coll<kFill>(d_re, a[0], b[1], id_pos, acc0);      // Re += Ar_hi Br_lo
+            mma_tf32_coll<kUse>(d_re, a[0], b[0], id_pos, 1u);         // Re += Ar_hi Br_hi
+            mma_tf32_coll<kUse>(d_im, a[0], b[3], id_pos, acc0);       // Im += Ar_hi Bi_lo
+            mma_tf32_coll<kLast>(d_im, a[0], b[2], id_pos, 1u);        // Im += Ar_hi Bi_hi
+            mma_tf32_coll<kFill>(d_re, a[1], b[0], id_pos, 1u);        // Re += Ar_lo Br_hi
+            mma_tf32_coll<kLast>(d_im, a[1], b[2], id_pos, 1u);        // Im += Ar_lo Bi_hi
+            mma_tf32_coll<kFill>(d_re, a[2], b[3], id_neg, 1u);        // Re -= Ai_hi Bi_lo
+            mma_tf32_coll<kUse>(d_re, a[2], b[2], id_neg, 1u);         // Re -= Ai_hi Bi_hi
+            mma_tf32_coll<kUse>(d_im, a[2], b[1], id_pos, 1u);         // Im += Ai_hi Br_lo
+            mma_tf32_coll<kLast>(d_im, a[2], b[0], id_pos, 1u);        // Im += Ai_hi Br_hi
+            mma_tf32_coll<kFill>(d_re, a[3], b[2], id_neg, 1u);        // Re -= Ai_lo Bi_hi
+            mma_tf32_coll<kLast>(d_im, a[3], b[0], id_pos, 1u);        // Im += Ai_lo Br_hi
+          } else {
+            // Re: Ar Br - Ai Bi
+            mma_tf32(d_re, a[1], b[0], id_pos, acc0);
+            mma_tf32(d_re, a[0], b[1], id_pos, 1u);
+            mma_tf32(d_re, a[0], b[0], id_pos, 1u);
+            mma_tf32(d_re, a[3], b[2], id_neg, 1u);
+            mma_tf32(d_re, a[2], b[3], id_neg, 1u);
+            mma_tf32(d_re, a[2], b[2], id_neg, 1u);
+            // Im: Ar Bi + Ai Br
+            mma_tf32(d_im, a[1], b[2], id_pos, acc0);
+            mma_tf32(d_im, a[0], b[3], id_pos, 1u);
+            mma_tf32(d_im, a[0], b[2], id_pos, 1u);
+            mma_tf32(d_im, a[3], b[0], id_pos, 1u);
+            mma_tf32(d_im, a[2], b[1], id_pos, 1u);
+            mma_tf32(d_im, a[2], b[0], id_pos, 1u);
+          }
         }
         mma_commit(&empty_bar[s]);   // frees the stage once these MMAs finish
       }
@@ -365,6 +405,15 @@ int pipe_kb() {
   }
   return kb;
 }
+// AGB_TF32_COLL=1: the A operand through the collector buffer.
+bool use_coll() {
+  static int c = -1;
+  if (c < 0) {
+    const char* e = getenv("AGB_TF32_COLL");
+    c = (e && atoi(e) == 1) ? 1 : 0;
+  }
+  return c == 1;
+}
 
 }  // namespace
 
@@ -427,9 +476,13 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   }
   static bool attr_set = false;
   if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Pipe<16>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Pipe<8>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Pipe<16>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Pipe<8>::SMEM_BYTES));
     attr_set = true;
   }
@@ -444,10 +497,15 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     AGB_CUDA_TRY(cudaEventCreate(&ev1));
     AGB_CUDA_TRY(cudaEventRecord(ev0, stream));
   }
-  if (kb == 8)
-    tf32x3_gemm_kernel<8><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
+  const bool coll = use_coll();
+  if (kb == 8 && coll)
+    tf32x3_gemm_kernel<8, true><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
+  else if (kb == 8)
+    tf32x3_gemm_kernel<8, false><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
+  else if (coll)
+    tf32x3_gemm_kernel<16, true><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
   else
-    tf32x3_gemm_kernel<16><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
+    tf32x3_gemm_kernel<16, false><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
   AGB_LAUNCH_CHECK();
   if (ev0) {
     AGB_CUDA_TRY(cudaEventRecord(ev1, stream));
