@@ -77,25 +77,40 @@ class ci_wfn(object):
             return E, t2
         return E, t2.cpu().numpy()
 
-    # Closed-shell spatial-orbital solvers.  For a closed-shell reference the CISD (CID)
-    # eigenproblem in spatial orbitals is the spin-orbital one restricted to singlets, so
-    # both solve on the GPU spin-orbital engine and return the spatial amplitudes
-    # t1[i,a] = t1_SO[2i,2a] and t2[i,j,a,b] = t2_SO[2i,2j+1,2a,2b+1] (alpha-beta block),
-    # the quantities apyib/ci_wfn.py:51-167 and :420-574 iterate directly.
+    # Closed-shell spatial-orbital solvers: the reference's spin-adapted equations
+    # (apyib/ci_wfn.py:51-167, 420-574) on the library's GEMMs (apyib_gb300.spatial).  With
+    # parameters['precision'] = 'mixed' they run on the spin-orbital engine instead (its
+    # tensor-core residuals and defect correction) and return the spatial amplitudes
+    # t1[i,a] = t1_SO[2i,2a], t2[i,j,a,b] = t2_SO[2i,2j+1,2a,2b+1] (alpha-beta block).
+
+    def _solve_spatial(self, singles, print_level):
+        from .spatial import SpatialCISD
+        no = len(self.eps_o)
+        eng = SpatialCISD(self._F_MO, self._ERI_MO, no, singles=singles)
+        eng.set_denominators(self.eps_o, self.eps_v)
+        self.history = []
+        E, t1, t2 = eng.solve(self.parameters, print_level=print_level, history=self.history)
+        return np.complex128(E), t1, t2
 
     def solve_CISD(self, print_level=0, return_torch=False):
         """apyib/ci_wfn.py:420-574; returns (E_CISD, t1[no,nv], t2[no,no,nv,nv])."""
-        E, t1, t2 = self._solve(True, print_level)
-        t1s = t1[0::2, 0::2].contiguous()
-        t2s = t2[0::2, 1::2, 0::2, 1::2].contiguous()
+        if self.parameters.get("precision", "fp64") == "mixed":
+            E, t1, t2 = self._solve(True, print_level)
+            t1s = t1[0::2, 0::2].contiguous()
+            t2s = t2[0::2, 1::2, 0::2, 1::2].contiguous()
+        else:
+            E, t1s, t2s = self._solve_spatial(True, print_level)
         if return_torch:
             return E, t1s, t2s
         return E, t1s.cpu().numpy(), t2s.cpu().numpy()
 
     def solve_CID(self, print_level=0, return_torch=False):
         """apyib/ci_wfn.py:51-167; returns (E_CID, t2[no,no,nv,nv])."""
-        E, _, t2 = self._solve(False, print_level)
-        t2s = t2[0::2, 1::2, 0::2, 1::2].contiguous()
+        if self.parameters.get("precision", "fp64") == "mixed":
+            E, _, t2 = self._solve(False, print_level)
+            t2s = t2[0::2, 1::2, 0::2, 1::2].contiguous()
+        else:
+            E, _, t2s = self._solve_spatial(False, print_level)
         if return_torch:
             return E, t2s
         return E, t2s.cpu().numpy()

@@ -558,9 +558,10 @@ def profile_kernel(spec):
 
         gemm M N K [tf32x3|df64|oz|fp64]   complex GEMM, A [M,K], B used transposed [N,K]
         jk NBF REPS [sym|sym64|general]    J/K Fock build over seeded real AO integrals
-        hbm O V                            the amplitude update, DIIS Gram row (8 vectors),
-                                           DIIS combination (8 vectors) and MP2_SO of a mixed
-                                           plan at o/v spin orbitals
+        ao2mo NBF [ozaki|tf32x3|df64|fp64] the AO->MO transform, nmo = nbf
+        hbm O V [update|dots|combine|mp2]  the amplitude update, DIIS Gram row (8 vectors),
+                                           DIIS combination (8 vectors) and MP2_SO at o/v
+                                           spin orbitals (each once timed, after two runs)
 
     Each case runs twice untimed, then once (gemm) or REPS / 3 times under CUDA events,
     and prints one line."""
@@ -615,6 +616,25 @@ def profile_kernel(spec):
         def run():
             jk_fock(eri, D, h, 1.0, precision=prec)
         work, label = 8.0 * n ** 4, f"jk_fock {variant} nbf={n} (GB/s of the full ERI tensor)"
+    elif kind == "ao2mo":
+        n = int(args[0]) if args else 96
+        prec_name = args[1] if len(args) > 1 else "ozaki"
+        prec = {"fp64": _lib.PREC_FP64, "df64": _lib.PREC_DF64, "ozaki": _lib.PREC_OZAKI,
+                "tf32x3": _lib.PREC_TF32X3}[prec_name]
+        g = torch.Generator(device="cpu").manual_seed(0)
+        A = torch.randn(3 * n, n, n, generator=g, dtype=torch.float64)
+        A = ((A + A.transpose(1, 2)) / (2 * (3 * n * n) ** 0.5)).cuda()
+        eri = torch.einsum("Lmn,Lls->mnls", A, A).contiguous()
+        del A
+        Cm = torch.linalg.qr(torch.randn(n, n, generator=g, dtype=torch.complex128))[0].cuda().contiguous()
+        out = torch.empty(n, n, n, n, dtype=torch.complex128, device="cuda")
+        nb = _lib.load().agb_ao2mo_scratch_bytes(n, n, prec)
+        buf, sp, _ = workspace(nb)
+
+        def run():
+            _lib.call("agb_ao2mo", ptr(eri), n, ptr(Cm), n, ptr(out), ctypes.c_void_p(sp), ctypes.c_size_t(nb), prec,
+                      stream_ptr())
+        reps, work, label = 1, 28.0 * n ** 5, f"ao2mo {prec_name} nbf={n} (TFLOP/s of 28 nbf^5)"
     elif kind == "hbm":
         from apyib_gb300 import synthetic
         from apyib_gb300.cisd import CISDPlan
@@ -622,10 +642,13 @@ def profile_kernel(spec):
         which = args[2] if len(args) > 2 else "all"
         prob = synthetic.so_factors(o, v, seed=0)
         eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
-        plan = CISDPlan(o, v, mixed=True)
+        # these kernels read only the vectors, 1/D and the energy weights: an MP2 plan
+        # (two packed integral blocks) keeps the device footprint small
+        plan = CISDPlan(o, v, mp2_only=True)
         plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
-        plan.blocks_from_factors(torch.as_tensor(prob.B), precision=_lib.PREC_OZAKI)
-        t = plan.guess()
+        plan.blocks_from_factors(torch.as_tensor(prob.B), precision=_lib.PREC_DF64)
+        t = torch.zeros(plan.n, dtype=torch.complex128, device="cuda")
+        plan.mp2_into(t, torch.empty(16, dtype=torch.complex128, device="cuda"))
         g = torch.Generator(device="cuda").manual_seed(1)
         ys = [t + 1e-3 * torch.randn(t.shape, dtype=t.dtype, device=t.device, generator=g) for _ in range(8)]
         out3 = torch.empty(16, dtype=torch.complex128, device=t.device)
@@ -663,8 +686,8 @@ def profile_kernel(spec):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    unit = "TFLOP/s (8MNK)" if kind == "gemm" else "GB/s"
-    scale = 1e9 if kind == "gemm" else 1e6
+    unit = {"gemm": "TFLOP/s (8MNK)", "ao2mo": "TFLOP/s"}.get(kind, "GB/s")
+    scale = 1e9 if kind in ("gemm", "ao2mo") else 1e6
     print(f"ok {label}: {ms:.3f} ms, {work / ms / scale:.1f} {unit}")
     return 0
 

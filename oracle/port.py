@@ -271,6 +271,63 @@ def cisd_so_residual_vslab(F, blk, t1, t2, E, o: int, a0: int, a1: int, lay=None
     return r1, r2
 
 
+def cisd_spatial_residual(F, ERI_MO, t1, t2, E, no: int, singles: bool = True):
+    """Closed-shell T1/T2 residuals of apyib/ci_wfn.py:458-490 (CISD; t1 ignored and
+    r1 None for CID, :84-111) for the active-space F_MO and chemist ERI_MO."""
+    O, V = slice(0, no), slice(no, F.shape[0])
+    g = ERI_MO.swapaxes(1, 2)
+    gx = g.swapaxes(2, 3)
+    ein = lambda s, *a: np.einsum(s, *a, optimize=True)
+    r1 = None
+    if singles:
+        r1 = F.swapaxes(0, 1)[O, V].copy()
+        r1 -= ein("ji,ja->ia", F[O, O], t1)
+        r1 += ein("ab,ib->ia", F[V, V], t1)
+        r1 += ein("jabi,jb->ia", 2.0 * g[O, V, V, O] - gx[O, V, V, O], t1)
+        r1 += ein("jb,ijab->ia", F[O, V], 2.0 * t2 - t2.swapaxes(2, 3))
+        r1 += ein("ajbc,ijbc->ia", 2.0 * g[V, O, V, V] - gx[V, O, V, V], t2)
+        r1 -= ein("kjib,kjab->ia", 2.0 * g[O, O, O, V] - gx[O, O, O, V], t2)
+        r1 -= E * t1
+    r2 = g.swapaxes(0, 2).swapaxes(1, 3)[O, O, V, V].copy()
+    if singles:
+        r2 += ein("abcj,ic->ijab", g[V, V, V, O], t1)
+        r2 += ein("abic,jc->ijab", g[V, V, O, V], t1)
+        r2 -= ein("kbij,ka->ijab", g[O, V, O, O], t1)
+        r2 -= ein("akij,kb->ijab", g[V, O, O, O], t1)
+    r2 += ein("ac,ijcb->ijab", F[V, V], t2)
+    r2 += ein("bc,ijac->ijab", F[V, V], t2)
+    r2 -= ein("ki,kjab->ijab", F[O, O], t2)
+    r2 -= ein("kj,ikab->ijab", F[O, O], t2)
+    r2 += ein("klij,klab->ijab", g[O, O, O, O], t2)
+    r2 += ein("abcd,ijcd->ijab", g[V, V, V, V], t2)
+    r2 -= ein("kbcj,ikca->ijab", g[O, V, V, O], t2)
+    r2 += ein("kaci,kjcb->ijab", 2.0 * g[O, V, V, O] - gx[O, V, V, O], t2)
+    r2 -= ein("kbic,kjac->ijab", g[O, V, O, V], t2)
+    r2 -= ein("kaci,kjbc->ijab", g[O, V, V, O], t2)
+    r2 += ein("kbcj,ikac->ijab", 2.0 * g[O, V, V, O] - gx[O, V, V, O], t2)
+    r2 -= ein("kajc,ikcb->ijab", g[O, V, O, V], t2)
+    r2 -= E * t2
+    return r1, r2
+
+
+def cid_spatial_residual(F, ERI_MO, t2, E, no: int):
+    """The closed-shell CID residual in the reference's own symmetrised form,
+    apyib/ci_wfn.py:84-95 (half the terms, then r + r with (i,a) <-> (j,b) swapped)."""
+    O, V = slice(0, no), slice(no, F.shape[0])
+    g = ERI_MO.swapaxes(1, 2)
+    ein = lambda s, *a: np.einsum(s, *a, optimize=True)
+    r2 = 0.5 * g.swapaxes(0, 2).swapaxes(1, 3)[O, O, V, V]
+    r2 = r2 + ein("ijae,be->ijab", t2, F[V, V])
+    r2 -= ein("imab,mj->ijab", t2, F[O, O])
+    r2 += 0.5 * ein("mnab,mnij->ijab", t2, g[O, O, O, O])
+    r2 += 0.5 * ein("ijef,abef->ijab", t2, g[V, V, V, V])
+    r2 += ein("imae,mbej->ijab", t2 - t2.swapaxes(2, 3), g[O, V, V, O])
+    r2 += ein("imae,mbej->ijab", t2, g[O, V, V, O] - g.swapaxes(2, 3)[O, V, V, O])
+    r2 -= ein("mjae,mbie->ijab", t2, g[O, V, O, V])
+    r2 = r2 + r2.swapaxes(0, 1).swapaxes(2, 3)
+    return r2 - E * t2
+
+
 def so_denominators(eps_o_spatial, eps_v_spatial):
     """apyib/ci_wfn.py:268-271: SO denominators from np.repeat-ed spatial energies."""
     eo = np.repeat(eps_o_spatial, 2)
