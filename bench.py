@@ -780,31 +780,64 @@ def main():
     dev_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist)
     clocks = sampler.stop()
 
-    # ---- e2e: the same iteration with amplitudes resident on the host (pinned)
-    (host_t, host_out), numa_node = pinned_local(plan.n, torch.complex128, local)
-    host_t.copy_(state["t"].cpu())        # both pinned buffers written by the CPU before the timed copies
+    # ---- e2e: iterations whose amplitude vectors live in pinned host memory.  Two
+    # independent iterates (the bench's and a second one started from the same guess)
+    # alternate on the compute stream; every step copies its iterate in (H2D) before
+    # the iteration and its result out (D2H) after it, on a copy stream, so one
+    # iterate's copies overlap the other's iteration.  The device buffers of the two
+    # iterates are the ping-pong pair; the pinned buffers sit on the GPU's NUMA node.
+    it_b, state_b, diis_b = mixed_iteration(plan)
+    for _ in range(args.warmup):
+        it_b()
+    chains = [(iteration, state), (it_b, state_b)]
+    bufs = []
+    for c in range(2):
+        pair, numa_node = pinned_local(plan.n, torch.complex128, local)
+        pair[0].copy_(chains[c][1]["t"].cpu())            # the iterate starts on the host
+        bufs.append(pair)                                 # [input, output] of chain c
+    copy = torch.cuda.Stream()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    comp = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    marks = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    e0.record()
+    e0.record(comp)
+    copy.wait_event(e0)
+    ready, h2d_ev, d2h_ev = [None, None], [], []
+    for c in range(2):
+        with torch.cuda.stream(copy):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(copy)
+            chains[c][1]["t"].copy_(bufs[c][0], non_blocking=True)
+            b.record(copy)
+            h2d_ev.append((a, b))
+            ready[c] = b
     for k in range(args.steps):
-        marks[k][0].record()
-        state["t"].copy_(host_t, non_blocking=True)
-        marks[k][1].record()
-        iteration()
-        marks[k][2].record()
-        host_out.copy_(state["t"], non_blocking=True)
-        marks[k][3].record()
-        host_t, host_out = host_out, host_t
-    e1.record()
+        c = k % 2
+        comp.wait_event(ready[c])
+        chains[c][0]()
+        done = torch.cuda.Event()
+        done.record(comp)
+        with torch.cuda.stream(copy):
+            copy.wait_event(done)
+            a, b, d = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a.record(copy)
+            bufs[c][1].copy_(chains[c][1]["t"], non_blocking=True)       # D2H: the step's result
+            b.record(copy)
+            bufs[c][0], bufs[c][1] = bufs[c][1], bufs[c][0]               # the result is the next input
+            chains[c][1]["t"].copy_(bufs[c][0], non_blocking=True)       # H2D: the next step's input
+            d.record(copy)
+            d2h_ev.append((a, b))
+            h2d_ev.append((b, d))
+            ready[c] = d
+    comp.wait_stream(copy)
+    e1.record(comp)
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist)
-    h2d_ms = float(np.mean([m[0].elapsed_time(m[1]) for m in marks]))
-    d2h_ms = float(np.mean([m[2].elapsed_time(m[3]) for m in marks]))
-    e2e_iter_ms = float(np.mean([m[1].elapsed_time(m[2]) for m in marks]))
+    h2d_ms = float(np.mean([a.elapsed_time(b) for a, b in h2d_ev]))
+    d2h_ms = float(np.mean([a.elapsed_time(b) for a, b in d2h_ev]))
     nbytes = plan.n * 16
+    del it_b, state_b, diis_b, chains, bufs
 
     peaks, peak_kind = measured_peaks()
     tf32_peak = peaks["bf16_tflops"] / 2.0        # tcgen05 kind::tf32 issues at half the f16/bf16 rate
@@ -819,10 +852,13 @@ def main():
         "config": bench_config(o, v, world),
         "e2e": {"value": aggregate_throughput(world, W, e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                # per-step phases on the stream: pinned host -> HBM copy, the iteration, HBM -> pinned host
-                "h2d_ms": h2d_ms, "iteration_ms": e2e_iter_ms, "d2h_ms": d2h_ms,
+                # copies on the copy stream, overlapping the other iterate's iteration
+                "h2d_ms": h2d_ms, "d2h_ms": d2h_ms,
                 "h2d_GBps": nbytes / h2d_ms / 1e6, "d2h_GBps": nbytes / d2h_ms / 1e6,
-                "pinned_numa_node": numa_node},
+                "pinned_numa_node": numa_node,
+                "pipeline": "two independent iterates alternate on the compute stream; each step copies its "
+                            "iterate in from pinned host memory before the iteration and its result out after "
+                            "it, on a copy stream that overlaps the other iterate's iteration"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
                      "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",
@@ -838,7 +874,7 @@ def main():
     }
 
     out["hbm_kernels"] = hbm_kernels(plan, state["t"], diis, measured_peaks()[0]["hbm_gbs"])
-    del diis, state, host_t, host_out
+    del diis, state
     torch.cuda.empty_cache()
     if not args.no_solve and rank == 0:
         # Full mixed solve (fresh amplitudes) + FP64 residual timing + a-posteriori FP64 check.
