@@ -102,30 +102,6 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
       : "memory");
 }
 
-// The same MMA with the A operand kept in the tensor core's collector buffer: FILL reads A
-// from shared memory and keeps it, USE takes it from the buffer (the descriptor names the
-// same tile), LAST uses it a final time and releases the buffer.
-enum CollA { kFill, kUse, kLast };
-template <CollA C>
-__device__ __forceinline__ void mma_tf32_coll(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                              uint32_t accumulate) {
-  if constexpr (C == kFill)
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32.collector::a::fill [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
-  else if constexpr (C == kUse)
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32.collector::a::use [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
-  else
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
-}
-
 struct GemmParams {
   int64_t M, N;
   int nkb;          // k-blocks per split
@@ -138,7 +114,7 @@ struct GemmParams {
   int64_t rowsA, rowsB;  // padded rows per plane
 };
 
-template <int KB, bool COLL>
+template <int KB>
 __global__ void __launch_bounds__(THREADS, 1)
 tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    GemmParams p) {
@@ -237,36 +213,20 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
             b[pl] = make_desc_kb<KB>(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
           }
           uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-          if constexpr (COLL) {
-            // the same 12 products grouped by A plane, each plane read from shared memory once
-            mma_tf32_coll<kFill>(d_re, a[0], b[1], id_pos, acc0);      // Re += Ar_hi Br_lo
-            mma_tf32_coll<kUse>(d_re, a[0], b[0], id_pos, 1u);         // Re += Ar_hi Br_hi
-            mma_tf32_coll<kUse>(d_im, a[0], b[3], id_pos, acc0);       // Im += Ar_hi Bi_lo
-            mma_tf32_coll<kLast>(d_im, a[0], b[2], id_pos, 1u);        // Im += Ar_hi Bi_hi
-            mma_tf32_coll<kFill>(d_re, a[1], b[0], id_pos, 1u);        // Re += Ar_lo Br_hi
-            mma_tf32_coll<kLast>(d_im, a[1], b[2], id_pos, 1u);        // Im += Ar_lo Bi_hi
-            mma_tf32_coll<kFill>(d_re, a[2], b[3], id_neg, 1u);        // Re -= Ai_hi Bi_lo
-            mma_tf32_coll<kUse>(d_re, a[2], b[2], id_neg, 1u);         // Re -= Ai_hi Bi_hi
-            mma_tf32_coll<kUse>(d_im, a[2], b[1], id_pos, 1u);         // Im += Ai_hi Br_lo
-            mma_tf32_coll<kLast>(d_im, a[2], b[0], id_pos, 1u);        // Im += Ai_hi Br_hi
-            mma_tf32_coll<kFill>(d_re, a[3], b[2], id_neg, 1u);        // Re -= Ai_lo Bi_hi
-            mma_tf32_coll<kLast>(d_im, a[3], b[0], id_pos, 1u);        // Im += Ai_lo Br_hi
-          } else {
-            // Re: Ar Br - Ai Bi
-            mma_tf32(d_re, a[1], b[0], id_pos, acc0);
-            mma_tf32(d_re, a[0], b[1], id_pos, 1u);
-            mma_tf32(d_re, a[0], b[0], id_pos, 1u);
-            mma_tf32(d_re, a[3], b[2], id_neg, 1u);
-            mma_tf32(d_re, a[2], b[3], id_neg, 1u);
-            mma_tf32(d_re, a[2], b[2], id_neg, 1u);
-            // Im: Ar Bi + Ai Br
-            mma_tf32(d_im, a[1], b[2], id_pos, acc0);
-            mma_tf32(d_im, a[0], b[3], id_pos, 1u);
-            mma_tf32(d_im, a[0], b[2], id_pos, 1u);
-            mma_tf32(d_im, a[3], b[0], id_pos, 1u);
-            mma_tf32(d_im, a[2], b[1], id_pos, 1u);
-            mma_tf32(d_im, a[2], b[0], id_pos, 1u);
-          }
+          // Re: Ar Br - Ai Bi
+          mma_tf32(d_re, a[1], b[0], id_pos, acc0);
+          mma_tf32(d_re, a[0], b[1], id_pos, 1u);
+          mma_tf32(d_re, a[0], b[0], id_pos, 1u);
+          mma_tf32(d_re, a[3], b[2], id_neg, 1u);
+          mma_tf32(d_re, a[2], b[3], id_neg, 1u);
+          mma_tf32(d_re, a[2], b[2], id_neg, 1u);
+          // Im: Ar Bi + Ai Br
+          mma_tf32(d_im, a[1], b[2], id_pos, acc0);
+          mma_tf32(d_im, a[0], b[3], id_pos, 1u);
+          mma_tf32(d_im, a[0], b[2], id_pos, 1u);
+          mma_tf32(d_im, a[3], b[0], id_pos, 1u);
+          mma_tf32(d_im, a[2], b[1], id_pos, 1u);
+          mma_tf32(d_im, a[2], b[0], id_pos, 1u);
         }
         mma_commit(&empty_bar[s]);   // frees the stage once these MMAs finish
       }
@@ -324,6 +284,248 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// The same GEMM on CTA pairs (tcgen05 cta_group::2): a cluster of two CTAs on two
+// SMs computes a 256 x 256 output tile with 256-row MMAs issued by the even CTA.
+// Each CTA stages its own 128 rows of A and its own 128 of the 256 rows of B (the
+// MMA reads B from both CTAs' shared memory), so per SM the operand traffic from L2
+// and the tensor core's shared-memory reads are two thirds of the single-CTA tile's.
+// Each CTA's TMEM holds its 128 output rows (Re | Im, 512 columns).  Both CTAs'
+// TMA loads complete on the even CTA's "full" barrier; the even CTA's MMA commit
+// arrives on both CTAs' "empty" barriers and, at the end, on both "tmem" barriers.
+// Every wait is bounded as in the single-CTA kernel; the pair meets at cluster
+// barriers after set-up and before freeing TMEM, which every thread reaches.
+constexpr int P2_STAGES = 3;
+constexpr int P2_A_TILE = 128 * BK * 4;                    // 8 KB per plane (own 128 rows)
+constexpr int P2_B_TILE = 128 * BK * 4;                    // 8 KB per plane (own half of 256 rows)
+constexpr int P2_STAGE_BYTES = 4 * (P2_A_TILE + P2_B_TILE);  // 64 KB
+constexpr int P2_SMEM_BYTES = P2_STAGES * P2_STAGE_BYTES + 1024 + 256;
+
+// Instruction descriptor for the pair MMA: D = F32, A = B = TF32, K-major, N = 256, M = 256.
+__host__ __device__ constexpr uint32_t make_idesc_pair(bool negA) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(256 >> 3) << 17) |
+         ((uint32_t)(256 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Commit of the pair MMAs issued so far: one arrival on the barrier at this shared
+// offset in both CTAs of the pair.
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+      ::"r"(smem_u32(bar)), "h"((uint16_t)3)
+      : "memory");
+}
+
+// TMA load whose completion is counted on a barrier of either CTA of the pair (bar is a
+// shared::cluster address, here the even CTA's).
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint32_t bar_cluster, int x,
+                                                 int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(bar_cluster), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Shared::cluster address of the object at local shared address a in CTA rank 'rank'.
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t a, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+tf32x3_gemm2_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                    GemmParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full_bar = (uint64_t*)(smem + P2_STAGES * P2_STAGE_BYTES);
+  uint64_t* empty_bar = full_bar + P2_STAGES;
+  uint64_t* tmem_bar = empty_bar + P2_STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(tmem_bar + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();             // 0: issues the MMAs; 1: its peer
+  // pair tiles in a grouped raster (kGroupM pair rows per group); x = 2 * tile_n + rank
+  const int ntn = gridDim.x / 2, ntm = gridDim.y;
+  const int lin = blockIdx.y * ntn + (blockIdx.x >> 1);
+  const int gsz = kGroupM * ntn;
+  const int first_m = (lin / gsz) * kGroupM;
+  const int gm = min(ntm - first_m, kGroupM);
+  const int tile_m = first_m + (lin % gsz) % gm;    // 256-row pair tile
+  const int tile_n = (lin % gsz) / gm;              // 256-column tile
+  const int split = blockIdx.z;
+  const int kb0 = split * p.nkb;
+  int nk = p.nkb_total - kb0;
+  if (nk > p.nkb) nk = p.nkb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < P2_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(tmem_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  cluster_sync_all();                               // the peer's barriers exist before any load targets them
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer of this CTA's operand halves; completion counted on the even CTA's barrier
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % P2_STAGES;
+        const uint32_t ph = (uint32_t)(kb / P2_STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
+        uint8_t* st = smem + s * P2_STAGE_BYTES;
+        if (rank == 0) mbar_expect_tx(&full_bar[s], 2 * P2_STAGE_BYTES);
+        const uint32_t bar0 = map_to_rank(smem_u32(&full_bar[s]), 0);
+        const int kx = (kb0 + kb) * BK;
+        for (int pl = 0; pl < 4; ++pl) {
+          tma_load_2d_pair(st + pl * P2_A_TILE, &mapA, bar0, kx, (int)(pl * p.rowsA + tile_m * 256 + rank * 128));
+          tma_load_2d_pair(st + 4 * P2_A_TILE + pl * P2_B_TILE, &mapB, bar0, kx,
+                           (int)(pl * p.rowsB + tile_n * 256 + rank * 128));
+        }
+        issued = kb + 1;
+      }
+      if (*abort_flag && rank == 0) {
+        // wait (bounded) for the stages in flight: the even CTA's barrier counts both halves
+        for (int kb = (issued > P2_STAGES ? issued - P2_STAGES : 0); kb < issued; ++kb) {
+          long long t0 = clock64();
+          while (!mbar_try_wait(&full_bar[kb % P2_STAGES], (uint32_t)(kb / P2_STAGES) & 1u) &&
+                 clock64() - t0 < kWaitCycles) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && rank == 0) {
+      // MMA issuer (even CTA only)
+      const uint32_t id_pos = make_idesc_pair(false), id_neg = make_idesc_pair(true);
+      const uint32_t d_re = tmem_base, d_im = tmem_base + BN;
+      bool ok = true;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % P2_STAGES;
+        const uint32_t ph = (uint32_t)(kb / P2_STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem_u32(smem + s * P2_STAGE_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 8; ++ks) {
+          uint64_t a[4], b[4];
+#pragma unroll
+          for (int pl = 0; pl < 4; ++pl) {
+            a[pl] = make_desc_kb<16>(st + pl * P2_A_TILE + ks * 32);
+            b[pl] = make_desc_kb<16>(st + 4 * P2_A_TILE + pl * P2_B_TILE + ks * 32);
+          }
+          const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
+          mma_tf32_pair(d_re, a[1], b[0], id_pos, acc0);
+          mma_tf32_pair(d_re, a[0], b[1], id_pos, 1u);
+          mma_tf32_pair(d_re, a[0], b[0], id_pos, 1u);
+          mma_tf32_pair(d_re, a[3], b[2], id_neg, 1u);
+          mma_tf32_pair(d_re, a[2], b[3], id_neg, 1u);
+          mma_tf32_pair(d_re, a[2], b[2], id_neg, 1u);
+          mma_tf32_pair(d_im, a[1], b[2], id_pos, acc0);
+          mma_tf32_pair(d_im, a[0], b[3], id_pos, 1u);
+          mma_tf32_pair(d_im, a[0], b[2], id_pos, 1u);
+          mma_tf32_pair(d_im, a[3], b[0], id_pos, 1u);
+          mma_tf32_pair(d_im, a[2], b[1], id_pos, 1u);
+          mma_tf32_pair(d_im, a[2], b[0], id_pos, 1u);
+        }
+        mma_commit_pair(&empty_bar[s]);              // frees stage s in both CTAs once these MMAs finish
+      }
+      if (ok) mma_commit_pair(tmem_bar);
+    }
+  } else {
+    // Epilogue warps 2..5 of each CTA drain that CTA's 128 rows
+    const int q = warp & 3;
+    int okw = 0;
+    if (lane == 0) okw = mbar_wait(tmem_bar, 0, p.err, abort_flag, 3) ? 1 : 0;
+    const bool ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && nk > 0) {
+      const int64_t m = (int64_t)tile_m * 256 + rank * 128 + q * 32 + lane;
+      const bool use_beta = (p.beta.x != 0.0 || p.beta.y != 0.0);
+      const bool unit_alpha = p.alpha.x == 1.0 && p.alpha.y == 0.0;
+      const bool unit_beta = p.beta.x == 1.0 && p.beta.y == 0.0;
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        float vr[32], vi[32];
+        const uint32_t tl = tmem_base + ((uint32_t)(q * 32) << 16) + c * 32;
+        tmem_ld32(tl, vr);
+        tmem_ld32(tl + BN, vi);
+        if (m < p.M) {
+          const int64_t n0 = (int64_t)tile_n * BN + c * 32;
+          if (p.partial) {
+            z64* dst = p.partial + ((int64_t)split * p.M + m) * p.N + n0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (n0 + j < p.N) dst[j] = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
+          } else {
+            z64* dst = p.C + m * p.ldc + n0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (n0 + j < p.N) {
+                z64 out = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
+                if (!unit_alpha) out = zmul(p.alpha, out);
+                if (unit_beta) out = zadd(out, dst[j]);
+                else if (use_beta) out = zadd(out, zmul(p.beta, dst[j]));
+                dst[j] = out;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  if (*abort_flag) {
+    // after a timed-out wait, give loads still in flight into this CTA time to land
+    const long long t0 = clock64();
+    while (clock64() - t0 < 2000000LL) {
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  cluster_sync_all();                               // neither CTA frees TMEM while its peer may still use it
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS));
+  }
+}
 
 // planes[4][rows][Kp]: re_hi, re_lo, im_hi, im_lo of X(row, k) = src[row*s_row + k*s_k], zero padded.
 __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t K, int64_t s_row, int64_t s_k,
@@ -405,11 +607,11 @@ int pipe_kb() {
   }
   return kb;
 }
-// AGB_TF32_COLL=1: the A operand through the collector buffer.
-bool use_coll() {
+// AGB_TF32_2SM=1: the CTA-pair kernel (cta_group::2, 256 x 256 pair tiles).
+bool use_pair() {
   static int c = -1;
   if (c < 0) {
-    const char* e = getenv("AGB_TF32_COLL");
+    const char* e = getenv("AGB_TF32_2SM");
     c = (e && atoi(e) == 1) ? 1 : 0;
   }
   return c == 1;
@@ -463,27 +665,27 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
-  const int kb = pipe_kb();
+  const bool pair = use_pair();
+  const int kb = pair ? 16 : pipe_kb();
   const int64_t Mp = tf32_rows_pad(M), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K), nkb = Kp / kb;
   AGB_ARG_CHECK(Mp / BM <= 65535, "tf32_gemm_planes: grid too large");
   int splits = partials ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
   CUtensorMap mA, mB;
-  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb) || !encode_planes(&mB, (float*)PB, 4 * Np, Kp, BN, kb)) {
+  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb) ||
+      !encode_planes(&mB, (float*)PB, 4 * Np, Kp, pair ? 128 : BN, kb)) {
     agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
   static bool attr_set = false;
   if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Pipe<16>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Pipe<8>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Pipe<16>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Pipe<8>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      P2_SMEM_BYTES));
     attr_set = true;
   }
   GemmParams p;
@@ -497,15 +699,15 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     AGB_CUDA_TRY(cudaEventCreate(&ev1));
     AGB_CUDA_TRY(cudaEventRecord(ev0, stream));
   }
-  const bool coll = use_coll();
-  if (kb == 8 && coll)
-    tf32x3_gemm_kernel<8, true><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
-  else if (kb == 8)
-    tf32x3_gemm_kernel<8, false><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
-  else if (coll)
-    tf32x3_gemm_kernel<16, true><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
-  else
-    tf32x3_gemm_kernel<16, false><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
+  if (pair) {
+    AGB_ARG_CHECK(Mp / 256 <= 65535, "tf32_gemm_planes: grid too large");
+    const dim3 grid2((unsigned)(2 * (Np / 256)), (unsigned)(Mp / 256), (unsigned)splits);
+    tf32x3_gemm2_kernel<<<grid2, THREADS, P2_SMEM_BYTES, stream>>>(mA, mB, p);
+  } else if (kb == 8) {
+    tf32x3_gemm_kernel<8><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
+  } else {
+    tf32x3_gemm_kernel<16><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
+  }
   AGB_LAUNCH_CHECK();
   if (ev0) {
     AGB_CUDA_TRY(cudaEventRecord(ev1, stream));
