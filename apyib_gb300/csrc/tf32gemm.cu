@@ -8,11 +8,12 @@
 //
 // Operands arrive in FP64 (complex128, arbitrary strides); a prep kernel
 // writes four K-major FP32 planes per operand (re_hi, re_lo, im_hi, im_lo),
-// zero-padded to the tile grid.  One CTA per 128x128 output tile (or per
-// tile and K split): warp 0 issues TMA loads, warp 1 issues the MMAs from one
-// thread, warps 2-5 drain the two TMEM accumulators (Re in columns 0-127, Im
-// in 128-255) and write FP64 results.  Every mbarrier wait is bounded; on
-// timeout the kernel records an error word and returns after releasing TMEM.
+// zero-padded to the tile grid.  Large outputs run on CTA pairs (cta_group::2,
+// 256 x 256 tiles, 3 stages); the rest on single CTAs (128 x 256 tiles, or a tile
+// and K split): warp 0 issues TMA loads, warp 1 issues the MMAs from one thread,
+// warps 2-5 drain the two TMEM accumulators (Re in columns 0-255, Im in 256-511)
+// and write FP64 results.  Every mbarrier wait is bounded; on timeout the kernel
+// records an error word and returns after releasing TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -62,7 +63,8 @@ using namespace tc05;
 constexpr int BM = 128, BN = 256, BK = 16;   // K padding of the planes, in fp32 elements (64 bytes)
 constexpr int THREADS = 192;
 // Pipeline shapes: a k-block of KB fp32 elements per stage (KB * 4 bytes per row, the TMA /
-// MMA swizzle width), STAGES stages.  KB = 16: 2 stages of 96 KB; KB = 8: 4 stages of 48 KB.
+// MMA swizzle width), STAGES stages.  KB = 16: 2 stages of 96 KB (used); KB = 8: 4 stages of
+// 48 KB, measured slower (305 against 335 TFLOP/s at 14400^3).
 template <int KB> struct Pipe {
   static constexpr int STAGES = KB == 16 ? 2 : 4;
   static constexpr int A_TILE_BYTES = BM * KB * 4;
@@ -597,25 +599,9 @@ bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp
   return r == CUDA_SUCCESS;
 }
 
-// Pipeline shape of the tensor-core GEMM: AGB_TF32_KB=8 selects 4 stages of 8-wide k-blocks
-// (default: 2 stages of 16-wide ones).
-int pipe_kb() {
-  static int kb = 0;
-  if (!kb) {
-    const char* e = getenv("AGB_TF32_KB");
-    kb = (e && atoi(e) == 8) ? 8 : 16;
-  }
-  return kb;
-}
-// AGB_TF32_2SM=1: the CTA-pair kernel (cta_group::2, 256 x 256 pair tiles).
-bool use_pair() {
-  static int c = -1;
-  if (c < 0) {
-    const char* e = getenv("AGB_TF32_2SM");
-    c = (e && atoi(e) == 1) ? 1 : 0;
-  }
-  return c == 1;
-}
+// The CTA-pair kernel for large outputs (both extents at least 1024, no K split): its
+// 256-row pair tiles would mostly compute padding on a short M.
+bool use_pair(int64_t M, int64_t N, int splits) { return M >= 1024 && N >= 1024 && splits == 1; }
 
 }  // namespace
 
@@ -665,13 +651,13 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
-  const bool pair = use_pair();
-  const int kb = pair ? 16 : pipe_kb();
+  constexpr int kb = 16;
   const int64_t Mp = tf32_rows_pad(M), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K), nkb = Kp / kb;
   AGB_ARG_CHECK(Mp / BM <= 65535, "tf32_gemm_planes: grid too large");
   int splits = partials ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
+  const bool pair = use_pair(M, N, splits);
   CUtensorMap mA, mB;
   if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb) ||
       !encode_planes(&mB, (float*)PB, 4 * Np, Kp, pair ? 128 : BN, kb)) {
@@ -682,8 +668,6 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   if (!attr_set) {
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Pipe<16>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Pipe<8>::SMEM_BYTES));
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       P2_SMEM_BYTES));
     attr_set = true;
@@ -703,8 +687,6 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     AGB_ARG_CHECK(Mp / 256 <= 65535, "tf32_gemm_planes: grid too large");
     const dim3 grid2((unsigned)(2 * (Np / 256)), (unsigned)(Mp / 256), (unsigned)splits);
     tf32x3_gemm2_kernel<<<grid2, THREADS, P2_SMEM_BYTES, stream>>>(mA, mB, p);
-  } else if (kb == 8) {
-    tf32x3_gemm_kernel<8><<<grid, THREADS, Pipe<8>::SMEM_BYTES, stream>>>(mA, mB, p);
   } else {
     tf32x3_gemm_kernel<16><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
   }
