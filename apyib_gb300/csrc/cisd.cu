@@ -487,8 +487,11 @@ __device__ __forceinline__ int64_t stride_start(int64_t k0, int64_t stride, int6
 // pipe would bound this HBM stream), fixed reduction order.  Block 0 sums the small t1 part
 // alone and the other blocks the packed doubles, so a thread carries one set of double-float
 // sums (4 floats per vector) and no FP64 totals: fewer registers, more resident warps.
+// Blocks of the Gram-row kernel: three resident per SM (its registers allow three), one wave.
+constexpr int kDotBlocks = 152 * 3;
+
 template <int NY>
-__global__ void __launch_bounds__(256) dots_kernel(DotArgs A, z64* partial) {
+__global__ void __launch_bounds__(256, 3) dots_kernel(DotArgs A, z64* partial) {
   const bool t1 = blockIdx.x == 0;
   const int64_t lo = t1 ? 0 : A.n1, hi = t1 ? A.n1 : A.n1 + A.n2;
   const int64_t stride = (int64_t)(t1 ? 1 : gridDim.x - 1) * blockDim.x;
@@ -497,16 +500,25 @@ __global__ void __launch_bounds__(256) dots_kernel(DotArgs A, z64* partial) {
 #pragma unroll
   for (int j = 0; j < NY; ++j) s[j][0] = s[j][1] = s[j][2] = s[j][3] = 0.f;
   for (int64_t k = k0; k < hi; k += stride) {
-    const float4 x = split_z_fast(A.x[k]);
+    // the element's loads four vectors at a time ahead of their math (streaming hint:
+    // each value is read once)
+    const float4 x = split_z_fast(__ldcs(&A.x[k]));
 #pragma unroll
-    for (int j = 0; j < NY; ++j) {
-      if (j < A.ny) {
-        const float4 y = split_z_fast(A.ys[j][k]);
-        // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
-        df_mac(s[j][0], s[j][1], y.x, y.y, x.x, x.y);
-        df_mac(s[j][0], s[j][1], y.z, y.w, x.z, x.w);
-        df_mac(s[j][2], s[j][3], y.x, y.y, x.z, x.w);
-        df_mac(s[j][2], s[j][3], -y.z, -y.w, x.x, x.y);
+    for (int j0 = 0; j0 < NY; j0 += 4) {
+      z64 yv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) yv[u] = j0 + u < A.ny ? __ldcs(&A.ys[j0 + u][k]) : zmk(0, 0);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = j0 + u;
+        if (j < A.ny) {
+          const float4 y = split_z_fast(yv[u]);
+          // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
+          df_mac(s[j][0], s[j][1], y.x, y.y, x.x, x.y);
+          df_mac(s[j][0], s[j][1], y.z, y.w, x.z, x.w);
+          df_mac(s[j][2], s[j][3], y.x, y.y, x.z, x.w);
+          df_mac(s[j][2], s[j][3], -y.z, -y.w, x.x, x.y);
+        }
       }
     }
   }
@@ -520,18 +532,18 @@ __global__ void __launch_bounds__(256) dots_kernel(DotArgs A, z64* partial) {
 // The Gram-row kernel for ny vectors (partials [kRedBlocks][nv]); returns nv, the slot stride.
 int launch_dots(const DotArgs& A, int ny, z64* part, cudaStream_t st) {
   if (ny <= 4) {
-    dots_kernel<4><<<kRedBlocks, 256, 0, st>>>(A, part);
+    dots_kernel<4><<<kDotBlocks, 256, 0, st>>>(A, part);
     return 4;
   }
   if (ny <= 8) {
-    dots_kernel<8><<<kRedBlocks, 256, 0, st>>>(A, part);
+    dots_kernel<8><<<kDotBlocks, 256, 0, st>>>(A, part);
     return 8;
   }
   if (ny <= 12) {
-    dots_kernel<12><<<kRedBlocks, 256, 0, st>>>(A, part);
+    dots_kernel<12><<<kDotBlocks, 256, 0, st>>>(A, part);
     return 12;
   }
-  dots_kernel<16><<<kRedBlocks, 256, 0, st>>>(A, part);
+  dots_kernel<16><<<kDotBlocks, 256, 0, st>>>(A, part);
   return 16;
 }
 
@@ -546,17 +558,30 @@ struct CombArgs {
   const z64* ew;   // energy weights [F_ov | <ij||ab>_p]
 };
 
+// (ah + al) - (bh + bl) as a float pair (two-sum of the leading parts, then a fast
+// renormalisation): absolute error ~2^-48 of the operands.
+__device__ __forceinline__ void df_diff(float ah, float al, float bh, float bl, float& h, float& l) {
+  const float s = __fsub_rn(ah, bh);
+  const float z = __fsub_rn(s, ah);
+  float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, z)), __fsub_rn(-bh, z));
+  e = __fadd_rn(e, __fsub_rn(al, bl));
+  h = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(h, s));
+}
+
 // t_new = sum_j c_j y_j, E = sum t_new ew, s1 = sum_{t1} (t_old - t_new)^2 and
 // s2 = 4 sum_{t2} (t_old - t_new)^2 (apyib/utils.py:138, ci_wfn.py:355,361-365).
-// t_new = (sum_j c_j) y_0 + sum_{j>0} c_j (y_j - y_0): the first term and the differences in
-// FP64, the small difference sum in double-float (its error, ~2^-44 of sum |c_j| |y_j - y_0|,
-// vanishes as DIIS iterates converge), so t_new keeps FP64 accuracy where the convergence test
-// needs it; the squares in double-float from the FP64 differences, E in FP64.  t_old / t_new
-// and any y_j may alias: each element is read before it is written.
+// t_new = (sum_j c_j) y_0 + sum_{j>0} c_j (y_j - y_0): the first product in FP64 (so a
+// copy, ny = 1 with c = 1, is exact), the differences, the small sum, the energy and the
+// squared norms in double-float on the FP32 pipe (~2^-46 of |y_j| per element), which
+// leaves ~8 FP64 operations per element (GB300's FP64 pipe bounded the FP64 version).
+// t_old / t_new and any y_j may alias: each element is read before it is written.
 __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) {
   __shared__ float4 cs[kMaxVec];
   if (threadIdx.x < A.ny) cs[threadIdx.x] = split_z(zmk(A.c[2 * threadIdx.x], A.c[2 * threadIdx.x + 1]));
   __syncthreads();
+  const bool csum_real = A.csum.y == 0.0;
+  float er = 0.f, erc = 0.f, ei = 0.f, eic = 0.f;  // E = sum t ew
   z64 acc[3] = {zmk(0, 0), zmk(0, 0), zmk(0, 0)};  // E, s1, s2
   const int64_t n = A.n1 + A.n2, stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -565,11 +590,15 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) 
     const int64_t hi = part ? n : A.n1;
     for (int64_t k = stride_start(k0, stride, part ? A.n1 : 0); k < hi; k += stride) {
       const z64 y0 = A.ys[0][k];
-      z64 t = zmul(A.csum, y0);
+      z64 t = csum_real ? zmk(A.csum.x * y0.x, A.csum.x * y0.y) : zmul(A.csum, y0);
       if (A.ny > 1) {
+        const float4 y0s = split_z_fast(y0);
         float dr = 0.f, drc = 0.f, di = 0.f, dic = 0.f;
         for (int j = 1; j < A.ny; ++j) {
-          const float4 d = split_z_fast(zsub(A.ys[j][k], y0));
+          const float4 yj = split_z_fast(A.ys[j][k]);
+          float4 d;
+          df_diff(yj.x, yj.y, y0s.x, y0s.y, d.x, d.y);
+          df_diff(yj.z, yj.w, y0s.z, y0s.w, d.z, d.w);
           const float4 c = cs[j];
           // c d = (cr dr - ci di) + i (cr di + ci dr)
           df_mac(dr, drc, c.x, c.y, d.x, d.y);
@@ -583,7 +612,13 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) 
       const z64 old = A.t_old[k];
       const z64 w = A.ew[k];
       A.t_new[k] = t;
-      acc[0] = zadd(acc[0], zmul(t, w));
+      const float4 ts = split_z_fast(t);
+      const float4 ws = split_z_fast(w);
+      // t w = (tr wr - ti wi) + i (tr wi + ti wr)
+      df_mac(er, erc, ts.x, ts.y, ws.x, ws.y);
+      df_mac(er, erc, -ts.z, -ts.w, ws.z, ws.w);
+      df_mac(ei, eic, ts.x, ts.y, ws.z, ws.w);
+      df_mac(ei, eic, ts.z, ts.w, ws.x, ws.y);
       const float4 e = split_z_fast(zsub(old, t));
       // (old - t)^2, unconjugated
       df_mac(q[0], q[1], e.x, e.y, e.x, e.y);
@@ -594,6 +629,7 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) 
     if (part) acc[2] = zadd(acc[2], qs);
     else acc[1] = zadd(acc[1], qs);
   }
+  acc[0] = zmk(df_to_double(er, erc), df_to_double(ei, eic));
   acc[2] = zscale(acc[2], 4.0);
   block_reduce_store<3>(acc, partial);
 }
@@ -1108,7 +1144,7 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
   const int nv = launch_dots(A, ny, part, st);
   AGB_LAUNCH_CHECK();
   // finish only the first ny of the nv slots (stride nv)
-  finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, ny, (z64*)out);
+  finish_partials_kernel<<<1, 32, 0, st>>>(part, kDotBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -1201,7 +1237,7 @@ agb_status agb_vec_dots_noalloc(int64_t n1, int64_t n2, double w1, double w2, co
   z64* part = (z64*)scratch;
   const int nv = launch_dots(A, ny, part, st);
   AGB_LAUNCH_CHECK();
-  finish_partials_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, nv, ny, (z64*)out);
+  finish_partials_kernel<<<1, 32, 0, st>>>(part, kDotBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
