@@ -314,18 +314,40 @@ def water_workloads():
 
     p = dict(geom=H2O_GEOM, basis="cc-pVDZ", method="CISD_SO", e_convergence=1e-10, d_convergence=1e-10,
              DIIS=True, max_iterations=120, freeze_core=False, F_el=[0.0, 0.0, 0.0], F_mag=[0.0, 0.0, 1e-4])
+    from apyib_gb300.ci_wfn import ci_wfn
     energy(dict(p, method="RHF"))                      # warm-up: library load, first kernels
-    res = {}
+    res, phases = {}, {}
     for prec in ("fp64", "mixed"):
+        pp = dict(p, precision=prec)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        E_list, T_list, C, basis = energy(dict(p, precision=prec))
+        E_list, T_list, C, basis = energy(pp)
         torch.cuda.synchronize()
         res[prec] = (time.perf_counter() - t0, complex(E_list[1]))
+        # the same run phase by phase: AO integrals, RHF, F_MO + AO->MO transform, CISD_SO solve
+        marks = [time.perf_counter()]
+        H = Hamiltonian(pp)
+        torch.cuda.synchronize()
+        marks.append(time.perf_counter())
+        wfn = hf_wfn(H)
+        wfn.solve_SCF(pp)
+        torch.cuda.synchronize()
+        marks.append(time.perf_counter())
+        ci = ci_wfn(pp, wfn)
+        torch.cuda.synchronize()
+        marks.append(time.perf_counter())
+        ci.solve_CISD_SO()
+        torch.cuda.synchronize()
+        marks.append(time.perf_counter())
+        phases[prec] = {name: marks[i + 1] - marks[i]
+                        for i, name in enumerate(("integrals_s", "rhf_s", "fock_and_transform_s", "cisd_so_solve_s"))}
     out = {"cisd_fp64_s": res["fp64"][0], "cisd_mixed_s": res["mixed"][0],
            "E_cisd": [res["fp64"][1].real, res["fp64"][1].imag],
            "abs_dE_mixed_vs_fp64": abs(res["mixed"][1] - res["fp64"][1]),
-           "note": "nso = 48: launch-bound at this size; the solves include integrals and RHF"}
+           "phases": phases,
+           "note": "nso = 48: launch-bound at this size; the solves include integrals and RHF; phases: the "
+                   "same run split into AO integrals, RHF, F_MO + AO->MO transform (FP64 / Ozaki) and the "
+                   "CISD_SO solve (FP64 / mixed)"}
     h, b = 1e-4, 1e-5
     E_list, T_list, C, basis = energy(p)
     torch.cuda.synchronize()
