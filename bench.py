@@ -495,6 +495,20 @@ def mixed_iteration(plan):
     return iteration, state, diis
 
 
+def gemm_traffic_60_240():
+    """DRAM bytes per launch of the bench's two tensor-core GEMMs at o/v = 60/240 (the ring
+    GEMM 14400 x 14400 x 14400 and the vvvv ladder 1770 x 28680 x 28680, complex), mean of
+    the two.  Counters are taken on smaller GEMMs with the same K and the same 256 x 256
+    pair tiles, which hold a few GB on the device (profiles/tf32x3_gemm_traffic_small.md):
+    3584 x 3584 x 14400 read 3.893e9 B over 14 x 14 pair tiles, 1770 x 3584 x 28680 read
+    3.411e9 B over 7 x 14.  Each tile streams its own A and B panels through L2, so the
+    read traffic is scaled by the pair-tile count of the full launch (57 x 57 and 7 x 113);
+    the output is counted as written once (16 B per element)."""
+    ring = 3.893e9 / (14 * 14) * (57 * 57) + 16.0 * 14400 * 14400
+    vvvv = 3.411e9 / (7 * 14) * (7 * 113) + 16.0 * 1770 * 28680
+    return 0.5 * (ring + vvvv)
+
+
 def timed_iterations(iteration, steps, warmup):
     import torch
     for _ in range(warmup):
@@ -818,6 +832,14 @@ def main():
         pair[0].copy_(chains[c][1]["t"].cpu())            # the iterate starts on the host
         bufs.append(pair)                                 # [input, output] of chain c
     copy = torch.cuda.Stream()
+    # the vector crosses in 32 pieces, so a small blocking read-back of the iteration (its
+    # DIIS Gram row and energy) queues behind one piece, not behind the whole vector, on
+    # the shared device-to-host copy engine
+    pieces = [(a, min(plan.n, a + (plan.n + 31) // 32)) for a in range(0, plan.n, (plan.n + 31) // 32)]
+
+    def copy_pieces(dst, src):
+        for a, b in pieces:
+            dst[a:b].copy_(src[a:b], non_blocking=True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -830,7 +852,7 @@ def main():
         with torch.cuda.stream(copy):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(copy)
-            chains[c][1]["t"].copy_(bufs[c][0], non_blocking=True)
+            copy_pieces(chains[c][1]["t"], bufs[c][0])
             b.record(copy)
             h2d_ev.append((a, b))
             ready[c] = b
@@ -844,10 +866,10 @@ def main():
             copy.wait_event(done)
             a, b, d = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             a.record(copy)
-            bufs[c][1].copy_(chains[c][1]["t"], non_blocking=True)       # D2H: the step's result
+            copy_pieces(bufs[c][1], chains[c][1]["t"])                   # D2H: the step's result
             b.record(copy)
             bufs[c][0], bufs[c][1] = bufs[c][1], bufs[c][0]               # the result is the next input
-            chains[c][1]["t"].copy_(bufs[c][0], non_blocking=True)       # H2D: the next step's input
+            copy_pieces(chains[c][1]["t"], bufs[c][0])                   # H2D: the next step's input
             d.record(copy)
             d2h_ev.append((a, b))
             h2d_ev.append((b, d))
@@ -885,10 +907,9 @@ def main():
         "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm_kernel (vvvv ladder + ring GEMMs)",
                      "achieved": kern_ach, "peak": gemm_peak, "unit": "TFLOP/s",
                      "frac": (kern_ach / gemm_peak) if kern_ach else None,
-                     # DRAM bytes per launch of the same two launches (vvvv ladder, rings) at this size,
-                     # read + written, from one ncu capture of this command at this size
-                     "traffic": 0.5 * ((46.15 + 0.79) + (53.15 + 3.30)) * 1e9,
-                     "traffic_unit": "bytes per launch (mean of the vvvv and ring launches)",
+                     "traffic": gemm_traffic_60_240(),
+                     "traffic_unit": "bytes per launch (mean of the vvvv and ring launches), DRAM read from "
+                                     "small-case ncu captures scaled by pair tiles + C written once",
                      "peak_note": f"{peak_kind} bf16 {peaks['bf16_tflops']} TF/s / 2 (tf32 rate) / 3 (3xTF32)",
                      "launches_timed": nl.value},
         "clocks": clocks,
