@@ -485,47 +485,53 @@ __device__ __forceinline__ int64_t stride_start(int64_t k0, int64_t stride, int6
 // Weighted Gram row: out_j = w(k) sum_k conj(y_j[k]) x[k], w = w1 on the t1 part (k < n1), w2 on t2.
 // Products and running sums in double-float on the FP32 pipe (~2^-44 relative; GB300's FP64
 // pipe would bound this HBM stream), fixed reduction order.  Block 0 sums the small t1 part
-// alone and the other blocks the packed doubles, so a thread carries one set of double-float
-// sums (4 floats per vector) and no FP64 totals: fewer registers, more resident warps.
-// Blocks of the Gram-row kernel: three resident per SM (its registers allow three), one wave.
-constexpr int kDotBlocks = 152 * 3;
+// alone and the other blocks the packed doubles.  The two halves of a block take the even and
+// the odd vectors of the same elements (x is read by both, the second time from L1), so a
+// thread carries half the double-float sums: fewer registers, four blocks per SM, and each
+// thread's loads and math alternate over half as many vectors.
+constexpr int kDotBlocks = 152 * 4;
 
 template <int NY>
-__global__ void __launch_bounds__(256, 3) dots_kernel(DotArgs A, z64* partial) {
+__global__ void __launch_bounds__(256, 4) dots_kernel(DotArgs A, z64* partial) {
+  constexpr int NH = (NY + 1) / 2;
+  const int half = threadIdx.x >> 7, tid = threadIdx.x & 127;
   const bool t1 = blockIdx.x == 0;
   const int64_t lo = t1 ? 0 : A.n1, hi = t1 ? A.n1 : A.n1 + A.n2;
-  const int64_t stride = (int64_t)(t1 ? 1 : gridDim.x - 1) * blockDim.x;
-  const int64_t k0 = lo + (int64_t)(t1 ? 0 : blockIdx.x - 1) * blockDim.x + threadIdx.x;
-  float s[NY][4];
+  const int64_t stride = (int64_t)(t1 ? 1 : gridDim.x - 1) * 128;
+  const int64_t k0 = lo + (int64_t)(t1 ? 0 : blockIdx.x - 1) * 128 + tid;
+  float s[NH][4];
 #pragma unroll
-  for (int j = 0; j < NY; ++j) s[j][0] = s[j][1] = s[j][2] = s[j][3] = 0.f;
+  for (int h = 0; h < NH; ++h) s[h][0] = s[h][1] = s[h][2] = s[h][3] = 0.f;
   for (int64_t k = k0; k < hi; k += stride) {
-    // the element's loads four vectors at a time ahead of their math (streaming hint:
-    // each value is read once)
-    const float4 x = split_z_fast(__ldcs(&A.x[k]));
+    const float4 x = split_z_fast(A.x[k]);
+    z64 yv[NH];
 #pragma unroll
-    for (int j0 = 0; j0 < NY; j0 += 4) {
-      z64 yv[4];
+    for (int h = 0; h < NH; ++h) {
+      const int j = 2 * h + half;
+      yv[h] = j < A.ny ? __ldcs(&A.ys[j][k]) : zmk(0, 0);
+    }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) yv[u] = j0 + u < A.ny ? __ldcs(&A.ys[j0 + u][k]) : zmk(0, 0);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int j = j0 + u;
-        if (j < A.ny) {
-          const float4 y = split_z_fast(yv[u]);
-          // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
-          df_mac(s[j][0], s[j][1], y.x, y.y, x.x, x.y);
-          df_mac(s[j][0], s[j][1], y.z, y.w, x.z, x.w);
-          df_mac(s[j][2], s[j][3], y.x, y.y, x.z, x.w);
-          df_mac(s[j][2], s[j][3], -y.z, -y.w, x.x, x.y);
-        }
+    for (int h = 0; h < NH; ++h) {
+      if (2 * h + half < A.ny) {
+        const float4 y = split_z_fast(yv[h]);
+        // conj(y) * x = (yr xr + yi xi) + i (yr xi - yi xr)
+        df_mac(s[h][0], s[h][1], y.x, y.y, x.x, x.y);
+        df_mac(s[h][0], s[h][1], y.z, y.w, x.z, x.w);
+        df_mac(s[h][2], s[h][3], y.x, y.y, x.z, x.w);
+        df_mac(s[h][2], s[h][3], -y.z, -y.w, x.x, x.y);
       }
     }
   }
   const double w = t1 ? A.w1 : A.w2;
   z64 acc[NY];
 #pragma unroll
-  for (int j = 0; j < NY; ++j) acc[j] = zmk(w * df_to_double(s[j][0], s[j][1]), w * df_to_double(s[j][2], s[j][3]));
+  for (int j = 0; j < NY; ++j) acc[j] = zmk(0, 0);
+#pragma unroll
+  for (int h = 0; h < NH; ++h) {
+    const z64 v = zmk(w * df_to_double(s[h][0], s[h][1]), w * df_to_double(s[h][2], s[h][3]));
+    if (half == 0 && 2 * h < NY) acc[2 * h] = v;
+    if (half == 1 && 2 * h + 1 < NY) acc[2 * h + 1] = v;
+  }
   block_reduce_store<NY>(acc, partial);
 }
 
