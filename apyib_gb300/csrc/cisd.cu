@@ -27,6 +27,8 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
 agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
                  cudaStream_t stream);
+agb_status zgemv_f32(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
+                     cudaStream_t stream);
 agb_status zgemv_df(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
                     cudaStream_t stream);
 agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
@@ -34,6 +36,8 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
                         void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
 size_t tf32_planes_bytes(int64_t rows, int64_t K);
+int64_t tf32_rows_pad(int64_t rows);
+int64_t tf32_k_pad(int64_t K);
 size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K);
 size_t dfgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
 size_t ozgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
@@ -215,6 +219,67 @@ __global__ void unpack_ring_kernel(const z64* __restrict__ t2p, int o, int v, in
       if (s < 0) val = zneg(val);
     }
     out[e] = val;
+  }
+}
+
+// The ring GEMM's A operand straight from the packed amplitudes, as the four zero-padded
+// K-major TF32 planes the tensor-core GEMM reads (re_hi, re_lo, im_hi, im_lo of
+// Tring[(i,a)][(k,c)] = t2[i,k,a,c]), for 3xTF32 residuals: no FP64 Tring is written and
+// re-read by a separate operand split.
+__global__ void unpack_ring_planes_kernel(const z64* __restrict__ t2p, int o, int v, int64_t pv, int64_t rows_pad,
+                                          int64_t Kp, float* __restrict__ planes) {
+  const int64_t ov = (int64_t)o * v, plane = rows_pad * Kp;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < plane; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / Kp, col = e % Kp;
+    z64 val = zmk(0, 0);
+    if (row < ov && col < ov) {
+      const int i = (int)(row / v), a = (int)(row % v), k = (int)(col / v), c = (int)(col % v);
+      const int sg = sgn_pair(i, k) * sgn_pair(a, c);
+      if (sg != 0) {
+        val = t2p[pair_index(min(i, k), max(i, k), o) * pv + pair_index(min(a, c), max(a, c), v)];
+        if (sg < 0) val = zneg(val);
+      }
+    }
+    uint32_t rh, rl, ih, il;
+    split_tf32_fast((uint32_t)__double2hiint(val.x), (uint32_t)__double2loint(val.x), rh, rl);
+    split_tf32_fast((uint32_t)__double2hiint(val.y), (uint32_t)__double2loint(val.y), ih, il);
+    planes[e] = __uint_as_float(rh);
+    planes[plane + e] = __uint_as_float(rl);
+    planes[2 * plane + e] = __uint_as_float(ih);
+    planes[3 * plane + e] = __uint_as_float(il);
+  }
+}
+
+// r1[i,a] += sum_{k,c} t2[i,k,a,c] F_kc (the F_jb t2_ijab term of apyib/ci_wfn.py:313) from the
+// half-unpacked t2h[i][k][(a<c)], FP32 arithmetic for 3xTF32 residuals; one warp per (i,a),
+// the warps of one i sharing its slice of t2h in L2.
+__global__ void r1_fov_t2_kernel(const z64* __restrict__ t2h, int o, int v, int64_t pv, const z64* __restrict__ Fov,
+                                 z64* __restrict__ r1) {
+  const int lane = threadIdx.x & 31;
+  const int64_t ov = (int64_t)o * v;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = warp; row < ov; row += nwarps) {
+    const int i = (int)(row / v), a = (int)(row % v);
+    float re = 0.f, im = 0.f;
+    for (int64_t idx = lane; idx < ov; idx += 32) {
+      const int k = (int)(idx / v), c = (int)(idx % v);
+      if (c == a) continue;
+      z64 t = t2h[((int64_t)i * o + k) * pv + pair_index(min(a, c), max(a, c), v)];
+      if (c < a) t = zneg(t);
+      const float4 tv = split_z_fast(t);
+      const float4 fv = split_z_fast(Fov[idx]);
+      re = fmaf(tv.x, fv.x, re);
+      re = fmaf(-tv.z, fv.z, re);
+      im = fmaf(tv.x, fv.z, im);
+      im = fmaf(tv.z, fv.x, im);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, off);
+      im += __shfl_xor_sync(0xffffffffu, im, off);
+    }
+    if (lane == 0) r1[row] = zadd(r1[row], zmk(f2d_exact(re), f2d_exact(im)));
   }
 }
 
@@ -678,7 +743,8 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   P->VT = (z64*)take(Z * ov * ov);
   P->WooooT = (z64*)take(Z * po * po);
   P->Wvp = (z64*)take(Z * pv * pv);
-  P->Tring = (z64*)take(Z * ov * ov);
+  // FP64 Tring, or (mixed plans) the ring operand's TF32 planes in 3xTF32 residuals
+  P->Tring = (z64*)take(P->mixed ? std::max(Z * ov * ov, agb::tf32_planes_bytes(ov, ov)) : Z * ov * ov);
   P->X = (z64*)take(Z * ov * ov);
   P->PQ = (z64*)take(Z * po * pv);
   // t2h/t2q serve the singles terms and the non-diagonal Fock terms
@@ -1046,7 +1112,14 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
   const z64 E = zmk(E_re, E_im);
   const bool need_hq = P->singles || !P->f_diag;
 
-  unpack_ring_kernel<<<grid_for(ov * ov, 256), 256, 0, st>>>(t2p, o, v, pv, P->Tring);
+  // 3xTF32 residuals take the ring operand as TF32 planes written straight from t2p
+  const bool ring_planes = prec == AGB_PREC_TF32X3;
+  if (ring_planes) {
+    const int64_t rp = tf32_rows_pad(ov), kp = tf32_k_pad(ov);
+    unpack_ring_planes_kernel<<<grid_for(rp * kp, 256), 256, 0, st>>>(t2p, o, v, pv, rp, kp, (float*)P->Tring);
+  } else {
+    unpack_ring_kernel<<<grid_for(ov * ov, 256), 256, 0, st>>>(t2p, o, v, pv, P->Tring);
+  }
   AGB_LAUNCH_CHECK();
   if (need_hq) {
     unpack_h_kernel<<<grid_for((int64_t)o * o * pv, 256), 256, 0, st>>>(t2p, o, pv, P->t2h);
@@ -1062,10 +1135,16 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     AGB_LAUNCH_CHECK();
     AGB_STATUS_TRY(gemm(P, prec, o, v, o, zmk(-1, 0), P->Foo, 1, o, t1, v, 1, one, r1, v, st));
     AGB_STATUS_TRY(gemm(P, prec, o, v, v, one, t1, v, 1, P->Fvv, 1, v, one, r1, v, st));
-    // FP64 mode keeps the FP64 pipe; the other modes take the double-float GEMV (~2^-44)
-    auto gemv = prec == AGB_PREC_FP64 ? zgemv : zgemv_df;
+    // FP64 mode keeps the FP64 pipe, the FP64-accurate modes take the double-float GEMV
+    // (~2^-44), the 3xTF32 mode an FP32 one (its GEMM terms carry FP32-level error)
+    auto gemv = prec == AGB_PREC_FP64 ? zgemv : (prec == AGB_PREC_TF32X3 ? zgemv_f32 : zgemv_df);
     AGB_STATUS_TRY(gemv(ov, ov, one, P->VT, ov, t1, one, r1, st));
-    AGB_STATUS_TRY(gemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
+    if (ring_planes) {
+      r1_fov_t2_kernel<<<grid_for(ov * 32, 256), 256, 0, st>>>(P->t2h, o, v, pv, P->EW, r1);
+      AGB_LAUNCH_CHECK();
+    } else {
+      AGB_STATUS_TRY(gemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
+    }
     AGB_STATUS_TRY(gemm(P, prec, o, v, (int64_t)o * pv, one, P->t2h, (int64_t)o * pv, 1, P->WvovvH, 1,
                         (int64_t)o * pv, one, r1, v, st, nullptr, P->P_Wvovv));
     AGB_STATUS_TRY(gemm(P, prec, o, v, po * v, one, P->WooovP, po * v, 1, P->t2q, v, 1, one, r1, v, st, P->P_Wooov));
@@ -1082,7 +1161,8 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
   AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st, P->P_Woooo));
   AGB_STATUS_TRY(gemm(P, prec, po, pv, pv, one, t2p, pv, 1, P->Wvp, 1, pv, one, P->PQ, pv, st, nullptr, P->P_Wvp));
   // rings: X[(i,a),(j,b)] = sum_(k,c) t2[i,k,a,c] <kb||cj>
-  AGB_STATUS_TRY(gemm(P, prec, ov, ov, ov, one, P->Tring, ov, 1, P->VT, 1, ov, zero, P->X, ov, st, nullptr, P->P_VT));
+  AGB_STATUS_TRY(gemm(P, prec, ov, ov, ov, one, P->Tring, ov, 1, P->VT, 1, ov, zero, P->X, ov, st,
+                      ring_planes ? (const float*)P->Tring : nullptr, P->P_VT));
   if (!P->f_diag) {
     AGB_STATUS_TRY(gemm(P, prec, po * v, v, v, one, P->t2q, v, 1, P->Fvv, 1, v, zero, P->Gq, v, st));
     AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, o, one, P->Foo, 1, o, P->t2h, (int64_t)o * pv, 1, zero, P->H2h,

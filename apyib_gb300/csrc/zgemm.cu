@@ -243,7 +243,47 @@ __global__ void zgemv_df_kernel(int64_t M, int64_t K, z64 alpha, const z64* __re
     }
   }
 }
+// y = alpha A x + beta y in FP32 arithmetic (each FP64 value truncated to its leading 24
+// significant bits on the integer pipe, FP32 multiply-adds, a warp per row): for residuals
+// whose other terms come from 3xTF32 tensor-core products (FP32-level error), where the
+// double-float GEMV's instruction count, not the HBM stream, would set the time.
+__global__ void zgemv_f32_kernel(int64_t M, int64_t K, z64 alpha, const z64* __restrict__ A, int64_t lda,
+                                 const z64* __restrict__ x, z64 beta, z64* y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t m = warp; m < M; m += nwarps) {
+    float re = 0.f, im = 0.f;
+    const z64* a = A + m * lda;
+    for (int64_t k = lane; k < K; k += 32) {
+      const float4 av = split_z_fast(__ldcs(&a[k]));
+      const float4 xv = split_z_fast(x[k]);
+      re = fmaf(av.x, xv.x, re);
+      re = fmaf(-av.z, xv.z, re);
+      im = fmaf(av.x, xv.z, im);
+      im = fmaf(av.z, xv.x, im);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, off);
+      im += __shfl_xor_sync(0xffffffffu, im, off);
+    }
+    if (lane == 0) {
+      z64 out = zmul(alpha, zmk(f2d_exact(re), f2d_exact(im)));
+      if (beta.x != 0.0 || beta.y != 0.0) out = zadd(out, zmul(beta, y[m]));
+      y[m] = out;
+    }
+  }
+}
 }  // namespace
+
+agb_status zgemv_f32(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
+                     cudaStream_t stream) {
+  if (M == 0) return AGB_OK;
+  zgemv_f32_kernel<<<grid_for(M * 32, 256), 256, 0, stream>>>(M, K, alpha, A, lda, x, beta, y);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
 
 agb_status zgemv(int64_t M, int64_t K, z64 alpha, const z64* A, int64_t lda, const z64* x, z64 beta, z64* y,
                  cudaStream_t stream) {
