@@ -51,7 +51,8 @@ constexpr int64_t kOzMinTiles = 152;
 agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
                             float* dst, cudaStream_t stream);
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
-                            z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream);
+                            z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
+                            int trans_c);
 
 namespace {
 
@@ -787,10 +788,15 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
     upd(po * v, v, v, false, false);
     upd(o, o * pv, o, false, false);
     if (P->singles) {
+      // the singles GEMMs in both orientations (3xTF32 runs them with transposed outputs)
       upd(o, v, o * pv, false, true);
       upd(o, v, po * v, true, false);
       upd(po * v, v, o, true, false);
       upd(o, o * pv, v, false, true);
+      upd(v, o, o * pv, true, false);
+      upd(v, o, po * v, false, true);
+      upd(v, po * v, o, false, true);
+      upd(o * pv, o, v, true, false);
     }
     P->P_VT = (float*)take(agb::tf32_planes_bytes(ov, ov));
     P->P_Wvp = (float*)take(agb::tf32_planes_bytes(pv, pv));
@@ -824,9 +830,11 @@ namespace {
 
 // GEMM on the selected backend.  conj flags are never needed on the hot path.
 // PA / PB: TF32 planes of a static operand prepared at set-up (tensor-core path only).
+// trans_c: C(m, n) lives at C[n * ldc + m]; the 3xTF32 kernel stores it so, the other
+// backends compute the same product as C^T = B^T A^T.
 agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm,
                 int64_t sAk, const z64* B, int64_t sBk, int64_t sBn, z64 beta, z64* C, int64_t ldc,
-                cudaStream_t st, const float* PA = nullptr, const float* PB = nullptr) {
+                cudaStream_t st, const float* PA = nullptr, const float* PB = nullptr, int trans_c = 0) {
   if (prec == AGB_PREC_TF32X3) {
     if (M == 0 || N == 0) return AGB_OK;
     if (K == 0) return zgemm_ex(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, nullptr, 0, st);
@@ -847,8 +855,9 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
       return AGB_ERR_WORKSPACE;
     }
     return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
-                            P->gemm_scratch_bytes - off, st);
+                            P->gemm_scratch_bytes - off, st, trans_c);
   }
+  if (trans_c) return gemm(P, prec, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, ldc, st);
   if (prec == AGB_PREC_OZAKI && ozgemm_tiles(M, N) >= kOzMinTiles)
     return ozgemm_ex(M, N, K, alpha, A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, P->gemm_scratch,
                      P->gemm_scratch_bytes, st);
@@ -1145,17 +1154,24 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     } else {
       AGB_STATUS_TRY(gemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
     }
-    AGB_STATUS_TRY(gemm(P, prec, o, v, (int64_t)o * pv, one, P->t2h, (int64_t)o * pv, 1, P->WvovvH, 1,
-                        (int64_t)o * pv, one, r1, v, st, nullptr, P->P_Wvovv));
-    AGB_STATUS_TRY(gemm(P, prec, o, v, po * v, one, P->WooovP, po * v, 1, P->t2q, v, 1, one, r1, v, st, P->P_Wooov));
+    // The singles GEMMs run with the long or static extent as M and the o-wide one as N:
+    // under 3xTF32 an o-wide N takes the 64-wide tile and the transposed store keeps the
+    // output's writes coalesced (r1 and Yh are i-major, Zq a-minor).
+    // r1[i][a] += sum_(j,p(cb)) <aj||cb> t2h[i][j][p(cb)]
+    AGB_STATUS_TRY(gemm(P, prec, v, o, (int64_t)o * pv, one, P->WvovvH, (int64_t)o * pv, 1, P->t2h, 1,
+                        (int64_t)o * pv, one, r1, v, st, P->P_Wvovv, nullptr, 1));
+    // r1[i][a] += sum_(p(kj),b) <kj||ib> t2q[p(kj)][b][a]
+    AGB_STATUS_TRY(gemm(P, prec, v, o, po * v, one, P->t2q, 1, v, P->WooovP, 1, po * v, one, r1, v, st, nullptr,
+                        P->P_Wooov, 1));
     if (flags & AGB_RES_ETERM) {
       axpy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(n1, zneg(E), t1, r1);
       AGB_LAUNCH_CHECK();
     }
     // Zq[p(ij)][b][a] = sum_k <kb||ij> t1[k,a];  Yh[i][j][p(ab)] = sum_c t1[i,c] <ab||cj>
-    AGB_STATUS_TRY(gemm(P, prec, po * v, v, o, one, P->WovooP, o, 1, t1, v, 1, zero, P->Zq, v, st, P->P_Wovoo));
-    AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, v, one, t1, v, 1, P->WvvvoP, (int64_t)o * pv, 1, zero, P->Yh,
-                        (int64_t)o * pv, st, nullptr, P->P_Wvvvo));
+    AGB_STATUS_TRY(gemm(P, prec, v, po * v, o, one, t1, 1, v, P->WovooP, 1, o, zero, P->Zq, v, st, nullptr,
+                        P->P_Wovoo, 1));
+    AGB_STATUS_TRY(gemm(P, prec, (int64_t)o * pv, o, v, one, P->WvvvoP, 1, (int64_t)o * pv, t1, 1, v, zero, P->Yh,
+                        (int64_t)o * pv, st, P->P_Wvvvo, nullptr, 1));
   }
   // ladders: PQ = sum_{k<l} <kl||ij> t2p[kl,ab] + sum_{c<d} t2p[ij,cd] <ab||cd>
   AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st, P->P_Woooo));

@@ -62,35 +62,38 @@ using namespace tc05;
 
 constexpr int BM = 128, BN = 256, BK = 16;   // K padding of the planes, in fp32 elements (64 bytes)
 constexpr int THREADS = 192;
-// Pipeline shapes: a k-block of KB fp32 elements per stage (KB * 4 bytes per row, the TMA /
-// MMA swizzle width), STAGES stages.  KB = 16: 2 stages of 96 KB (used); KB = 8: 4 stages of
-// 48 KB, measured slower (305 against 335 TFLOP/s at 14400^3).
-template <int KB> struct Pipe {
-  static constexpr int STAGES = KB == 16 ? 2 : 4;
-  static constexpr int A_TILE_BYTES = BM * KB * 4;
-  static constexpr int B_TILE_BYTES = BN * KB * 4;
+// Single-CTA tile shapes: 128 x NB outputs, NB = 256 (2 stages of 96 KB, one CTA per SM) or,
+// for outputs at most 64 wide, NB = 64 (2 stages of 48 KB, two CTAs per SM, so one CTA's
+// epilogue overlaps the other's loads): a 60-wide output then pays for 64 columns of MMA
+// work and operand traffic, not 256.
+template <int NB> struct Tile {
+  static constexpr int STAGES = 2;
+  static constexpr int CTAS_PER_SM = NB == 256 ? 1 : 2;
+  static constexpr int A_TILE_BYTES = BM * BK * 4;
+  static constexpr int B_TILE_BYTES = NB * BK * 4;
   static constexpr int STAGE_BYTES = 4 * (A_TILE_BYTES + B_TILE_BYTES);
   static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-  static constexpr uint32_t SBO = 8 * KB * 4;                 // 8-row group stride of the swizzled layout
-  static constexpr uint64_t LAYOUT = KB == 16 ? 4 : 6;        // tcgen05 descriptor: 64-byte / 32-byte swizzle
+  static constexpr unsigned TMEM_COLS = 2 * NB;                // Re and Im accumulators
 };
 
-// tcgen05 shared-memory descriptor of a K-major swizzled tile for the pipeline shape KB.
-template <int KB> __device__ __forceinline__ uint64_t make_desc_kb(uint32_t saddr) {
+// tcgen05 shared-memory descriptor of a K-major tile with 64-byte swizzle (16 fp32 per row),
+// 8-row groups 512 bytes apart.
+__device__ __forceinline__ uint64_t make_desc_sw64(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
   d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(Pipe<KB>::SBO >> 4) << 32;
+  d |= (uint64_t)(512 >> 4) << 32;
   d |= (uint64_t)1 << 46;
-  d |= Pipe<KB>::LAYOUT << 61;
+  d |= (uint64_t)4 << 61;
   return d;
 }
-constexpr unsigned TMEM_COLS = 2 * BN;                       // Re and Im accumulators
+constexpr unsigned TMEM_COLS = 2 * BN;                       // Re and Im accumulators (256-wide tiles)
 constexpr int kGroupM = 12;                      // tile rows per raster group
 
-// Instruction descriptor: D=F32, A=B=TF32, K-major both, N=128, M=128.
+// Instruction descriptor: D=F32, A=B=TF32, K-major both, N=NB, M=128.
+template <int NB>
 __host__ __device__ constexpr uint32_t make_idesc(bool negA) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(NB >> 3) << 17) |
          ((uint32_t)(BM >> 4) << 24);
 }
 
@@ -114,14 +117,16 @@ struct GemmParams {
   z64* partial;     // split-K partials [splits][M][N] or null
   int* err;
   int64_t rowsA, rowsB;  // padded rows per plane
+  int trans_c;           // store C(m, n) at C[n * ldc + m] instead of C[m * ldc + n]
 };
 
-template <int KB>
-__global__ void __launch_bounds__(THREADS, 1)
+template <int NB>
+__global__ void __launch_bounds__(THREADS, Tile<NB>::CTAS_PER_SM)
 tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    GemmParams p) {
-  constexpr int STAGES = Pipe<KB>::STAGES, STAGE_BYTES = Pipe<KB>::STAGE_BYTES;
-  constexpr int A_TILE_BYTES = Pipe<KB>::A_TILE_BYTES, B_TILE_BYTES = Pipe<KB>::B_TILE_BYTES;
+  constexpr int STAGES = Tile<NB>::STAGES, STAGE_BYTES = Tile<NB>::STAGE_BYTES;
+  constexpr int A_TILE_BYTES = Tile<NB>::A_TILE_BYTES, B_TILE_BYTES = Tile<NB>::B_TILE_BYTES;
+  constexpr unsigned NCOLS = Tile<NB>::TMEM_COLS;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -157,7 +162,7 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(NCOLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -175,11 +180,11 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
         if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
         uint8_t* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-        int kx = (kb0 + kb) * KB;
+        int kx = (kb0 + kb) * BK;
         for (int pl = 0; pl < 4; ++pl) {
           tma_load_2d(st + pl * A_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
           tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kx,
-                      (int)(pl * p.rowsB + tile_n * BN));
+                      (int)(pl * p.rowsB + tile_n * NB));
         }
         issued = kb + 1;
       }
@@ -196,8 +201,8 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
   } else if (warp == 1) {
     if (lane == 0) {
       // MMA issuer
-      const uint32_t id_pos = make_idesc(false), id_neg = make_idesc(true);
-      const uint32_t d_re = tmem_base, d_im = tmem_base + BN;
+      const uint32_t id_pos = make_idesc<NB>(false), id_neg = make_idesc<NB>(true);
+      const uint32_t d_re = tmem_base, d_im = tmem_base + NB;
       bool ok = true;
       for (int kb = 0; kb < nk; ++kb) {
         int s = kb % STAGES;
@@ -207,12 +212,12 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
         uint32_t st = smem_u32(smem + s * STAGE_BYTES);
         // planes: 0 Ar_hi 1 Ar_lo 2 Ai_hi 3 Ai_lo | 4 Br_hi 5 Br_lo 6 Bi_hi 7 Bi_lo
 #pragma unroll
-        for (int ks = 0; ks < KB / 8; ++ks) {
+        for (int ks = 0; ks < BK / 8; ++ks) {
           uint64_t a[4], b[4];
 #pragma unroll
           for (int pl = 0; pl < 4; ++pl) {
-            a[pl] = make_desc_kb<KB>(st + pl * A_TILE_BYTES + ks * 32);
-            b[pl] = make_desc_kb<KB>(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
+            a[pl] = make_desc_sw64(st + pl * A_TILE_BYTES + ks * 32);
+            b[pl] = make_desc_sw64(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
           }
           uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
           // Re: Ar Br - Ai Bi
@@ -250,28 +255,31 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
       const bool unit_alpha = p.alpha.x == 1.0 && p.alpha.y == 0.0;
       const bool unit_beta = p.beta.x == 1.0 && p.beta.y == 0.0;
 #pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
+      for (int c = 0; c < NB / 32; ++c) {
         float vr[32], vi[32];
         uint32_t tl = tmem_base + ((uint32_t)(q * 32) << 16) + c * 32;
         tmem_ld32(tl, vr);
-        tmem_ld32(tl + BN, vi);
+        tmem_ld32(tl + NB, vi);
         if (m < p.M) {
-          int64_t n0 = (int64_t)tile_n * BN + c * 32;
+          int64_t n0 = (int64_t)tile_n * NB + c * 32;
           if (p.partial) {
             z64* dst = p.partial + ((int64_t)split * p.M + m) * p.N + n0;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
               if (n0 + j < p.N) dst[j] = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
           } else {
-            z64* dst = p.C + m * p.ldc + n0;
+            // row-major C: a thread writes its row's 32 columns; transposed C: for each column
+            // the warp's 32 rows are consecutive addresses
+            const int64_t sj = p.trans_c ? p.ldc : 1;
+            z64* dst = p.trans_c ? p.C + n0 * p.ldc + m : p.C + m * p.ldc + n0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               if (n0 + j < p.N) {
                 z64 out = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
                 if (!unit_alpha) out = zmul(p.alpha, out);
-                if (unit_beta) out = zadd(out, dst[j]);
-                else if (use_beta) out = zadd(out, zmul(p.beta, dst[j]));
-                dst[j] = out;
+                if (unit_beta) out = zadd(out, dst[j * sj]);
+                else if (use_beta) out = zadd(out, zmul(p.beta, dst[j * sj]));
+                dst[j * sj] = out;
               }
             }
           }
@@ -282,7 +290,7 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(NCOLS));
   }
 }
 
@@ -451,8 +459,8 @@ tf32x3_gemm2_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_const
           uint64_t a[4], b[4];
 #pragma unroll
           for (int pl = 0; pl < 4; ++pl) {
-            a[pl] = make_desc_kb<16>(st + pl * P2_A_TILE + ks * 32);
-            b[pl] = make_desc_kb<16>(st + 4 * P2_A_TILE + pl * P2_B_TILE + ks * 32);
+            a[pl] = make_desc_sw64(st + pl * P2_A_TILE + ks * 32);
+            b[pl] = make_desc_sw64(st + 4 * P2_A_TILE + pl * P2_B_TILE + ks * 32);
           }
           const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
           mma_tf32_pair(d_re, a[1], b[0], id_pos, acc0);
@@ -569,13 +577,16 @@ __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t 
 }
 
 __global__ void splitk_sum_kernel(const z64* __restrict__ partial, int splits, int64_t M, int64_t N, z64 alpha,
-                                  z64 beta, z64* C, int64_t ldc) {
+                                  z64 beta, z64* C, int64_t ldc, int trans_c) {
   int64_t total = M * N;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    // e runs along C's rows in memory: (m, n) for a row-major C, (n, m) for a transposed one
+    int64_t m, n;
+    if (trans_c) { n = e / M; m = e % M; } else { m = e / N; n = e % N; }
+    const int64_t pe = m * N + n;
     z64 s = zmk(0, 0);
-    for (int z = 0; z < splits; ++z) s = zadd(s, partial[(int64_t)z * total + e]);
-    int64_t m = e / N, n = e % N;
-    z64* c = C + m * ldc + n;
+    for (int z = 0; z < splits; ++z) s = zadd(s, partial[(int64_t)z * total + pe]);
+    z64* c = trans_c ? C + n * ldc + m : C + m * ldc + n;
     z64 out = zmul(alpha, s);
     if (beta.x != 0.0 || beta.y != 0.0) out = zadd(out, zmul(beta, *c));
     *c = out;
@@ -605,8 +616,11 @@ bool use_pair(int64_t M, int64_t N, int splits) { return M >= 1024 && N >= 1024 
 
 }  // namespace
 
-// Plane rows are padded to the larger tile edge so one layout serves as A or B.
-int64_t tf32_rows_pad(int64_t rows) { return round_up(rows, BN > BM ? BN : BM); }
+// Plane rows are padded to the 256-row tile edge, or to 64 rows for operands of at most 64
+// rows (the narrow B tile), so one layout serves as A or B.  A 128-row A tile over a 64-row
+// plane reads past it (the next plane, or zeros beyond the last): those rows only feed
+// output rows >= M, which are never stored; a 256-row B tile over it likewise.
+int64_t tf32_rows_pad(int64_t rows) { return rows <= 64 ? 64 : round_up(rows, BN); }
 int64_t tf32_k_pad(int64_t K) { return round_up(K, BK); }
 size_t tf32_planes_bytes(int64_t rows, int64_t K) {
   return (size_t)4 * (size_t)tf32_rows_pad(rows) * (size_t)tf32_k_pad(K) * sizeof(float);
@@ -625,13 +639,17 @@ agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_r
 }
 
 namespace {
+// Tile width of the single-CTA kernel for an N-wide output.
+int tile_n_for(int64_t N) { return N <= 64 ? 64 : BN; }
+
 int choose_splits(int64_t M, int64_t N, int64_t nkb, size_t partial_cap) {
-  int64_t tiles = (round_up(M, BM) / BM) * (round_up(N, BN) / BN);
+  const int nb = tile_n_for(N);
+  int64_t tiles = (round_up(M, BM) / BM) * (round_up(N, nb) / nb);
   if (tiles >= 152 || nkb < 16) return 1;
   int64_t want = (2 * 152 + tiles - 1) / tiles;
   int64_t kmax = nkb / 8;
   if (want > kmax) want = kmax;
-  if (want > 128) want = 128;
+  if (want > 152) want = 152;
   int64_t fit = (int64_t)(partial_cap / ((size_t)M * N * sizeof(z64)));
   if (want > fit) want = fit;
   return want < 2 ? 1 : (int)want;
@@ -646,8 +664,11 @@ size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K) {
 }
 
 // C = alpha * A B^T + beta C on prepared planes (A: rows M, B: rows N, both K-major over K).
+// trans_c: C(m, n) lives at C[n * ldc + m] (the output written column by column, which keeps
+// the stores of an output with a short row extent coalesced).
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
-                            z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream) {
+                            z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
+                            int trans_c) {
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
@@ -657,17 +678,20 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   int splits = partials ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
-  const bool pair = use_pair(M, N, splits);
+  const bool pair = use_pair(M, N, splits) && !trans_c;
+  const int nb = tile_n_for(N);
   CUtensorMap mA, mB;
   if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb) ||
-      !encode_planes(&mB, (float*)PB, 4 * Np, Kp, pair ? 128 : BN, kb)) {
+      !encode_planes(&mB, (float*)PB, 4 * Np, Kp, pair ? 128 : nb, kb)) {
     agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
   static bool attr_set = false;
   if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Pipe<16>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<256>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<64>::SMEM_BYTES));
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       P2_SMEM_BYTES));
     attr_set = true;
@@ -675,8 +699,8 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   GemmParams p;
   p.M = M; p.N = N; p.nkb = nkb_split; p.nkb_total = (int)nkb;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = splits > 1 ? partials : nullptr; p.err = err;
-  p.rowsA = Mp; p.rowsB = Np;
-  dim3 grid((unsigned)(round_up(N, BN) / BN), (unsigned)(round_up(M, BM) / BM), (unsigned)splits);
+  p.rowsA = Mp; p.rowsB = Np; p.trans_c = trans_c;
+  dim3 grid((unsigned)(round_up(N, nb) / nb), (unsigned)(round_up(M, BM) / BM), (unsigned)splits);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (g_timing.load(std::memory_order_relaxed)) {
     AGB_CUDA_TRY(cudaEventCreate(&ev0));
@@ -688,7 +712,8 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     const dim3 grid2((unsigned)(2 * (Np / 256)), (unsigned)(Mp / 256), (unsigned)splits);
     tf32x3_gemm2_kernel<<<grid2, THREADS, P2_SMEM_BYTES, stream>>>(mA, mB, p);
   } else {
-    tf32x3_gemm_kernel<16><<<grid, THREADS, Pipe<16>::SMEM_BYTES, stream>>>(mA, mB, p);
+    if (nb == 64) tf32x3_gemm_kernel<64><<<grid, THREADS, Tile<64>::SMEM_BYTES, stream>>>(mA, mB, p);
+    else tf32x3_gemm_kernel<256><<<grid, THREADS, Tile<256>::SMEM_BYTES, stream>>>(mA, mB, p);
   }
   AGB_LAUNCH_CHECK();
   if (ev0) {
@@ -697,7 +722,8 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     g_timing_recs.push_back(TimingRec{ev0, ev1, 8.0 * (double)M * (double)N * (double)K, M, N, K});
   }
   if (splits > 1) {
-    splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>(partials, splits, M, N, alpha, beta, C, ldc);
+    splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>(partials, splits, M, N, alpha, beta, C, ldc,
+                                                                 trans_c);
     AGB_LAUNCH_CHECK();
   }
   return AGB_OK;
@@ -731,7 +757,7 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
   AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream));
   size_t used = 256 + a_bytes + b_bytes;
   return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + used),
-                          scratch_bytes - used, stream);
+                          scratch_bytes - used, stream, 0);
 }
 
 }  // namespace agb

@@ -56,3 +56,19 @@ def test_c3_iteration_matches_reference(case, prec):
         assert abs(proj - complex(g["t2_proj"][k])) < 1e-10 * max(1.0, abs(complex(g["t2_proj"][k])))
     assert abs(torch.sum(t2.abs() ** 2).item() - float(g["t2_norm2"])) < 1e-10 * float(g["t2_norm2"])
     assert abs(E1 - complex(g["E_iter1"])) < 1e-11
+
+
+def test_c3_tf32x3_residual_tracks_fp64(case):
+    """The 3xTF32 residual (every singles GEMM with o = 40 as its narrow, transposed-store
+    side) against the FP64 residual on the same amplitudes: FP32-level agreement."""
+    _, plan = case
+    t = plan.guess()
+    E0, _, _ = plan.combine([t], [1.0], t, t)
+    r64 = plan.residual(t, E0, _lib.PREC_FP64)
+    r32 = plan.residual(t, E0, _lib.PREC_TF32X3)
+    plan.check_status()
+    n1 = O * V
+    for part in (slice(0, n1), slice(n1, None)):
+        ref = r64[part]
+        err = (r32[part] - ref).abs().max().item() / ref.abs().max().item()
+        assert err < 2e-5, err

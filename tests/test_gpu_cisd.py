@@ -138,3 +138,34 @@ def test_df64_residual_matches_fp64_residual():
     rdf = plan.residual(t, 0.1 - 0.01j, _lib.PREC_DF64)
     err = (rdf - r64).abs().max().item() / r64.abs().max().item()
     assert err < 1e-11, err
+
+
+@pytest.mark.parametrize("o,v,offdiag", [(6, 30, True), (20, 80, True), (64, 96, False), (70, 100, True)])
+def test_tf32x3_residual_tracks_fp64(o, v, offdiag):
+    """3xTF32 residual against the FP64 residual on the same amplitudes (every term,
+    singles included): o <= 64 takes the 64-wide tile and the transposed stores for the
+    singles GEMMs, o = 70 the 256-wide tile over the same transposed orientation."""
+    prob = synthetic.so_factors(o, v, seed=o + v)
+    F = prob.fock_so()
+    if offdiag:
+        n = F.shape[0]
+        rng = np.random.default_rng(o)
+        X = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * 0.01
+        mask = np.add.outer(np.arange(n) % 2, np.arange(n) % 2) % 2 == 0
+        F = F + (X + X.conj().T) * mask
+    plan = CISDPlan(o, v, mixed=True)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    plan.set_fock(torch.as_tensor(F), eps_so)
+    plan.blocks_from_factors(torch.as_tensor(prob.B))
+    t = plan.guess()
+    torch.manual_seed(o)
+    t = t + 0.01 * torch.randn_like(t)          # singles non-zero
+    E0, _, _ = plan.combine([t], [1.0], t, t)
+    r64 = plan.residual(t, E0, _lib.PREC_FP64)
+    r32 = plan.residual(t, E0, _lib.PREC_TF32X3)
+    plan.check_status()
+    n1 = o * v
+    for part in (slice(0, n1), slice(n1, None)):
+        ref = r64[part]
+        err = (r32[part] - ref).abs().max().item() / ref.abs().max().item()
+        assert err < 2e-5, err

@@ -53,9 +53,13 @@ def tf32_gemm(A, B, alpha=1.0, beta=0.0, C=None, transB=False):
     return out.cpu().numpy()
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 16), (1, 1, 1), (200, 300, 77), (60, 240, 6000), (513, 129, 1000)])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 16), (1, 1, 1), (200, 300, 77), (60, 240, 6000), (513, 129, 1000),
+                                   (2000, 60, 240), (240, 60, 60000), (300, 64, 500), (100, 65, 100), (33, 17, 100),
+                                   (64, 64, 64)])
 def test_tf32x3_gemm_accuracy(M, N, K):
-    """3xTF32 complex GEMM: error ~1e-6 relative to sum|a||b| (FP32-level)."""
+    """3xTF32 complex GEMM: error ~1e-6 relative to sum|a||b| (FP32-level).  N <= 64 takes
+    the 64-wide tile (split over K for (240, 60, 60000)); M <= 64 an A operand whose
+    64-row planes the 128-row tile reads past."""
     rng = np.random.default_rng(M + N + K)
     A = crandn(rng, M, K)
     B = crandn(rng, K, N)
@@ -73,6 +77,11 @@ def test_tf32x3_gemm_alpha_beta_and_transposed_b():
     C0 = crandn(rng, 150, 170)
     ref = (0.5 + 2j) * A @ Bt.T + (1 - 1j) * C0
     got = tf32_gemm(A, Bt, alpha=0.5 + 2j, beta=1 - 1j, C=C0, transB=True)
+    assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5
+    # the same on the 64-wide tile
+    Bn, Cn = Bt[:40], C0[:, :40]
+    ref = (0.5 + 2j) * A @ Bn.T + (1 - 1j) * Cn
+    got = tf32_gemm(A, Bn, alpha=0.5 + 2j, beta=1 - 1j, C=Cn, transB=True)
     assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5
 
 
