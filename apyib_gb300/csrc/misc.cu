@@ -20,6 +20,7 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
                      const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t ozgemm_scratch_bytes(int64_t M, int64_t N, int64_t K);
+size_t ozgemm_scratch_bytes_fused(int64_t M, int64_t N, int64_t K);
 
 namespace {
 
@@ -643,7 +644,7 @@ size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision) {
     size_t need = 0;
     if (precision == AGB_PREC_TF32X3) need = cgemm_tf32x3_scratch(rows[i], nmo, nbf);
     else if (precision == AGB_PREC_DF64) need = dfgemm_scratch_bytes(rows[i], nmo, nbf);
-    else if (precision == AGB_PREC_OZAKI) need = ozgemm_scratch_bytes(rows[i], nmo, nbf);
+    else if (precision == AGB_PREC_OZAKI) need = ozgemm_scratch_bytes_fused(rows[i], nmo, nbf);   // A sliced once
     if (need > gs) gs = need;
   }
   return 2 * s + sizeof(z64) * (size_t)(nbf * nmo) + 256 + gs + 256;

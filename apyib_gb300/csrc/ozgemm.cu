@@ -89,11 +89,70 @@ struct OzParams {
   z64* C;                    // complex output [M][ldc]
   int64_t ldc;
   z64 coef;                  // C = (use_beta ? beta C : C) + coef * P  (first part: C = coef * P without beta)
+  int csx, csy;              // coef.x, coef.y as -1 / 0 / 1 (applied as sign flips), or 2: multiply
   z64 beta;
   int mode;                  // 0: overwrite, 1: beta C + coef P, 2: C + coef P
+  int fixed;                 // 1: combine groups and tail in int64 (|sum| < 2^62 for K <= 2^16)
   int* err;
   int64_t rowsA, rowsB;      // padded rows per slice plane
 };
+
+// round(t * 2^32) for a float t with |t| < 2^29, by integer instructions.
+__device__ __forceinline__ long long f32_fixed32(float t) {
+  const unsigned int f = __float_as_uint(t);
+  const int ex = (int)((f >> 23) & 0xFFu);
+  if (ex == 0) return 0;                                  // zero or subnormal: below 2^-32
+  const long long mant = (long long)((f & 0x7FFFFFu) | 0x800000u);
+  const int sh = ex - 118;                                // t * 2^32 = mant * 2^(ex - 150 + 32)
+  long long r;
+  if (sh >= 0) r = mant << sh;
+  else if (sh < -25) r = 0;
+  else r = (mant + (1ll << (-sh - 1))) >> (-sh);
+  return (f >> 31) ? -r : r;
+}
+
+// T * 2^e2 rounded to the nearest double (ties to even, subnormal and overflowing results
+// included), by integer instructions: GB300 runs FP64 conversions and multiplies on its
+// narrow FP64 pipe, which made the FP64 epilogue the bottleneck of short-K products.
+__device__ __forceinline__ double i64_ldexp_rn(long long T, int e2) {
+  if (T == 0) return 0.0;
+  const unsigned long long sgn = T < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long a = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
+  const int lz = __clzll((long long)a);
+  const unsigned long long m = a << lz;                   // leading one at bit 63
+  const int E = 1086 - lz + e2;                           // biased exponent of (m >> 11) * 2^(11 - lz + e2)
+  unsigned long long bits;
+  if (E >= 1) {
+    unsigned long long mant = m >> 11;                    // 53 bits with the leading one
+    const unsigned long long rem = m & 0x7FFull;
+    mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+    // (E - 1) << 52 plus the mantissa with its leading one: a carry out of rounding bumps E
+    // (to the infinity pattern from E = 2046)
+    bits = E >= 2047 ? (0x7FFull << 52) : (((unsigned long long)(E - 1)) << 52) + mant;
+  } else {
+    // subnormal: m * 2^-sh units of 2^-1074, rounded once
+    const int sh = 12 - E;
+    if (sh > 64) {
+      bits = 0;
+    } else if (sh == 64) {
+      bits = m > (1ull << 63) ? 1ull : 0ull;
+    } else {
+      unsigned long long q = m >> sh;
+      const unsigned long long r = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+      q += (r > half || (r == half && (q & 1ull))) ? 1ull : 0ull;
+      bits = q;
+    }
+  }
+  return __longlong_as_double((long long)(bits | sgn));
+}
+
+// c * v for a coefficient component c in {-1, 0, 1} (cs = c) by a sign flip, else a multiply.
+__device__ __forceinline__ double coef_mul(int cs, double c, double v) {
+  if (cs == 0) return 0.0;
+  if (cs == 1) return v;
+  if (cs == -1) return __longlong_as_double(__double_as_longlong(v) ^ (1ll << 63));
+  return c * v;
+}
 
 __global__ void __launch_bounds__(THREADS, 1)
 ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, OzParams p) {
@@ -250,11 +309,18 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
           for (int j = 0; j < 16; ++j) {
             const int64_t n = n0 + c4 * 16 + j;
             if (n < p.N) {
-              // 2^(fa + fb) as a double built from its exponent field
-              const double sc = __longlong_as_double((long long)(fa + p.fB[n] + 1023) << 52);
-              const double v = ((double)acc[c4 * 16 + j] * 4.76837158203125e-07 + (double)tl[j]) * sc;   // I 2^-21 + tail
+              double v;
+              if (p.fixed) {
+                // exact groups (units 2^-21) and the FP32 tail in units of 2^-32, one rounding
+                const long long T = (acc[c4 * 16 + j] << 11) + f32_fixed32(tl[j]);
+                v = i64_ldexp_rn(T, fa + p.fB[n] - 32);
+              } else {
+                // 2^(fa + fb) as a double built from its exponent field
+                const double sc = __longlong_as_double((long long)(fa + p.fB[n] + 1023) << 52);
+                v = ((double)acc[c4 * 16 + j] * 4.76837158203125e-07 + (double)tl[j]) * sc;   // I 2^-21 + tail
+              }
               z64* c = p.C + m * p.ldc + n;
-              z64 out = zmk(p.coef.x * v, p.coef.y * v);
+              z64 out = zmk(coef_mul(p.csx, p.coef.x, v), coef_mul(p.csy, p.coef.y, v));
               if (p.mode == 1) out = zadd(out, zmul(p.beta, *c));
               else if (p.mode == 2) out = zadd(out, *c);
               *c = out;
@@ -271,19 +337,24 @@ ozgemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ 
   }
 }
 
-// Value of part `part` (0 Re, 1 Im, 2 Re + Im) of X(r, k) = src[r*s_row + k*s_k]; conj == 1 negates Im,
-// conj == kSrcReal reads a real array.
-__device__ __forceinline__ double oz_part(const z64* src, int64_t off, int conj, int part) {
-  if (conj == kSrcReal) return part == 1 ? 0.0 : ((const double*)src)[off];
+// (Re, Im) of X(r, k) = src[r*s_row + k*s_k]; conj == 1 negates Im, conj == kSrcReal reads a real array.
+__device__ __forceinline__ z64 oz_load(const z64* src, int64_t off, int conj) {
+  if (conj == kSrcReal) return zmk(((const double*)src)[off], 0.0);
   const z64 v = src[off];
-  const double im = conj == 1 ? -v.y : v.y;
-  return part == 0 ? v.x : (part == 1 ? im : v.x + im);
+  return zmk(v.x, conj == 1 ? -v.y : v.y);
 }
 
-// Largest biased FP64 exponent per row (emax must start at zero).
+// Part `part` (0 Re, 1 Im, 2 Re + Im) of a loaded value.
+__device__ __forceinline__ double oz_part(z64 v, int part) { return part == 0 ? v.x : (part == 1 ? v.y : v.x + v.y); }
+
+__device__ __forceinline__ int oz_bexp(double v) { return (__double2hiint(v) >> 20) & 0x7ff; }
+
+// Largest biased FP64 exponent per row of NP parts (part0, ...), from one read of the
+// source; emax[p * estride + r] must start at zero.
+template <int NP>
 __global__ void oz_rowexp_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
-                                 int conj, int part, int* __restrict__ emax) {
-  __shared__ int tile[32][33];
+                                 int conj, int part0, int64_t estride, int* __restrict__ emax) {
+  __shared__ int tile[NP][32][33];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
   const int64_t tiles_k = (K + 31) / 32, tiles = ((rows + 31) / 32) * tiles_k;
@@ -292,16 +363,23 @@ __global__ void oz_rowexp_kernel(const z64* __restrict__ src, int64_t rows, int6
     for (int i = ty; i < 32; i += 8) {
       int64_t r, k;
       if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
-      int e = 0;
-      if (r < rows && k < K) e = (__double2hiint(oz_part(src, r * s_row + k * s_k, conj, part)) >> 20) & 0x7ff;
-      if (kfast) tile[i][tx] = e; else tile[tx][i] = e;
+      z64 v = zmk(0.0, 0.0);
+      if (r < rows && k < K) v = oz_load(src, r * s_row + k * s_k, conj);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const int e = oz_bexp(oz_part(v, part0 + q));
+        if (kfast) tile[q][i][tx] = e; else tile[q][tx][i] = e;
+      }
     }
     __syncthreads();
     for (int i = ty; i < 32; i += 8) {
-      int e = tile[i][tx];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-      if (tx == 0 && r0 + i < rows && e > 0) atomicMax(&emax[r0 + i], e);
+      for (int q = 0; q < NP; ++q) {
+        int e = tile[q][i][tx];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        if (tx == 0 && r0 + i < rows && e > 0) atomicMax(&emax[q * estride + r0 + i], e);
+      }
     }
     __syncthreads();
   }
@@ -313,11 +391,14 @@ __device__ __forceinline__ uint16_t oz_digit_bf16(long long d, float scale) {
   return (uint16_t)(__float_as_uint(__fmul_rn(f, scale)) >> 16);
 }
 
-// Slices [OZ_S][rows_pad][Kp] (bf16, K-major, zero padded) and row scale exponents f_r.
+// Slices [OZ_S][rows_pad][Kp] (bf16, K-major, zero padded) and row scale exponents f_r of
+// NP parts from one read of the source: part q's slices start at slices + q * OZ_S * rows_pad * Kp,
+// its exponents at emax / fexp + q * estride (estride 0: one exponent shared by the parts).
+template <int NP>
 __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
-                                int conj, int part, int64_t rows_pad, int64_t Kp, const int* __restrict__ emax,
-                                int* __restrict__ fexp, uint16_t* __restrict__ slices) {
-  __shared__ double tile[32][33];
+                                int conj, int part0, int64_t rows_pad, int64_t Kp, int64_t estride,
+                                const int* __restrict__ emax, int* __restrict__ fexp, uint16_t* __restrict__ slices) {
+  __shared__ z64 tile[32][33];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
   const int64_t tiles_k = Kp / 32, tiles = (rows_pad / 32) * tiles_k;
@@ -327,59 +408,341 @@ __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64
     for (int i = ty; i < 32; i += 8) {
       int64_t r, k;
       if (kfast) { r = r0 + i; k = k0 + tx; } else { r = r0 + tx; k = k0 + i; }
-      double v = 0.0;
-      if (r < rows && k < K) v = oz_part(src, r * s_row + k * s_k, conj, part);
+      z64 v = zmk(0.0, 0.0);
+      if (r < rows && k < K) v = oz_load(src, r * s_row + k * s_k, conj);
       if (kfast) tile[i][tx] = v; else tile[tx][i] = v;
     }
     __syncthreads();
     for (int i = ty; i < 32; i += 8) {
       const int64_t r = r0 + i, k = k0 + tx;
-      const int eb = r < rows ? emax[r] : 0;
-      if (k0 == 0 && tx == 0 && r < rows_pad) fexp[r] = eb > 0 ? eb - 1023 + 1 - 7 : 0;
-      const double v = tile[i][tx];
-      const uint32_t hw = (uint32_t)__double2hiint(v), lw = (uint32_t)__double2loint(v);
-      const int ex = (int)((hw >> 20) & 0x7ffu);
-      long long X = 0;
-      const int shift = 11 + (eb - ex);
-      if (ex > 0 && eb > 0 && shift < 64) {
-        const unsigned long long M = ((unsigned long long)(hw & 0xfffffu) << 32 | lw) | (1ull << 52);
-        X = (long long)((M + (1ull << (shift - 1))) >> shift);   // nearest (|X| <= 2^42 keeps |d_0| <= 128)
-        if (hw >> 31) X = -X;
-      }
-      // balanced base-2^7 digits of X (|X| < 2^42)
-      long long d[OZ_S];
+      const z64 vz = tile[i][tx];
+#pragma unroll 1
+      for (int q = 0; q < NP; ++q) {
+        const int eb = r < rows ? emax[q * estride + r] : 0;
+        if (k0 == 0 && tx == 0 && r < rows_pad) fexp[q * estride + r] = eb > 0 ? eb - 1023 + 1 - 7 : 0;
+        const double v = oz_part(vz, part0 + q);
+        const uint32_t hw = (uint32_t)__double2hiint(v), lw = (uint32_t)__double2loint(v);
+        const int ex = (int)((hw >> 20) & 0x7ffu);
+        long long X = 0;
+        const int shift = 11 + (eb - ex);
+        if (ex > 0 && eb > 0 && shift < 64) {
+          const unsigned long long M = ((unsigned long long)(hw & 0xfffffu) << 32 | lw) | (1ull << 52);
+          X = (long long)((M + (1ull << (shift - 1))) >> shift);   // nearest (|X| <= 2^42 keeps |d_0| <= 128)
+          if (hw >> 31) X = -X;
+        }
+        // balanced base-2^7 digits of X (|X| < 2^42)
+        long long d[OZ_S];
 #pragma unroll
-      for (int s = 0; s < OZ_S - 1; ++s) {
-        const int sh = 35 - 7 * s;
-        d[s] = (X + (1ll << (sh - 1))) >> sh;
-        X -= d[s] << sh;
-      }
-      d[OZ_S - 1] = X;
-      const int64_t off = r * Kp + k;
-      float sc = 1.0f;
+        for (int s = 0; s < OZ_S - 1; ++s) {
+          const int sh = 35 - 7 * s;
+          d[s] = (X + (1ll << (sh - 1))) >> sh;
+          X -= d[s] << sh;
+        }
+        d[OZ_S - 1] = X;
+        uint16_t* dst = slices + (int64_t)q * OZ_S * plane + r * Kp + k;
+        float sc = 1.0f;
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) {
-        slices[s * plane + off] = oz_digit_bf16(d[s], sc);
-        sc *= 0.0078125f;   // 2^-7
+        for (int s = 0; s < OZ_S; ++s) {
+          dst[s * plane] = oz_digit_bf16(d[s], sc);
+          sc *= 0.0078125f;   // 2^-7
+        }
       }
     }
     __syncthreads();
   }
 }
 
+// ---------------------------------------------------------------------------
+// One-pass complex Ozaki GEMM for short K (4M, Re and Im accumulated side by side).
+//
+// Rows of A and columns of B are sliced with one exponent shared by their Re and Im
+// parts, so the four real products Re.Re, Im.Im, Re.Im and Im.Re are sums in the same
+// fixed-point units: Re C = Re.Re - Im.Im accumulates in one set of TMEM columns
+// (the Im.Im MMAs negate A) and Im C = Re.Im + Im.Re in another.  Each set is the
+// 3M kernel's five accumulators (exact groups 0..3 and the tail); two products per
+// accumulator double the group bounds (group 3: 2 (2^14 + 2^13) units per k), so the
+// exact chunk is 256 k (< 2^24 units).  The tile is 128 x 32 outputs: 2 sets x 5 x 32
+// = 320 TMEM columns.  The epilogue turns the int64 group sums and the tail into FP64
+// with integer instructions and writes C once: no read-modify-write of C between
+// products and no FP64 arithmetic when alpha = 1 and beta = 0.  A real A (the first
+// AO->MO quarter step) has no Im slices and runs the Re.Re and Re.Im products only.
+namespace ozc {
+constexpr int BM = 128, BN = 32, BK = 16;            // BK in bf16 elements (32-byte rows)
+constexpr int NSL = 2 * OZ_S;                         // slice tiles per operand: Re 0..5, Im 6..11
+constexpr int A_TILE = BM * BK * 2;                   // 4 KB
+constexpr int B_TILE = BN * BK * 2;                   // 1 KB
+constexpr int STAGE_BYTES = NSL * (A_TILE + B_TILE);  // 60 KB
+constexpr int STAGES = 3;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 320;
+constexpr unsigned TMEM_COLS = 512;                   // Re G0..G3 T | Im G0..G3 T, 32 columns each (320 used)
+constexpr int CHUNK_KB = 16;                          // k-blocks per exact chunk (256 k)
+constexpr int EPI_COLS = BN / 2;                      // columns per epilogue warp
+}  // namespace ozc
+
+// tcgen05 shared-memory descriptor: K-major, 32-byte swizzle, 8-row groups 256 B apart.
+__device__ __forceinline__ uint64_t make_desc_sw32(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(256 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)6 << 61;
+  return d;
+}
+
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, K-major both, N = 32, M = 128, optional -A.
+__host__ __device__ constexpr uint32_t make_idesc_ozc(bool negA) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(ozc::BN >> 3) << 17) |
+         ((uint32_t)(ozc::BM >> 4) << 24);
+}
+
+struct OzcParams {
+  int64_t M, N;
+  int nkb;                   // k-blocks of ozc::BK
+  int a_parts;               // 2, or 1 for a real A (no Im slices)
+  const int* fA;             // per-row scale exponents of A (shared by Re and Im)
+  const int* fB;             // per-column scale exponents of B
+  z64* C;
+  int64_t ldc;
+  z64 alpha, beta;
+  int plain;                 // alpha == 1 and beta == 0
+  int* err;
+  int64_t rowsA, rowsB;      // padded rows per slice plane
+};
+
+__global__ void __launch_bounds__(ozc::THREADS, 1)
+ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, OzcParams p) {
+  constexpr int STAGES = ozc::STAGES, STAGE_BYTES = ozc::STAGE_BYTES, A_TILE = ozc::A_TILE, B_TILE = ozc::B_TILE;
+  constexpr int CBM = ozc::BM, CBN = ozc::BN, CBK = ozc::BK, NSL = ozc::NSL, EPI = ozc::EPI_COLS;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty_bar = full_bar + STAGES;
+  uint64_t* chunk_bar = empty_bar + STAGES;   // MMA -> epilogue: the chunk's MMAs completed
+  uint64_t* drained_bar = chunk_bar + 1;      // epilogue -> MMA: exact accumulators read (8 warps)
+  uint32_t* tmem_slot = (uint32_t*)(drained_bar + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntn = gridDim.x, ntm = gridDim.y;
+  const int lin = blockIdx.y * ntn + blockIdx.x;
+  const int gsz = kGroupM * ntn;
+  const int first_m = (lin / gsz) * kGroupM;
+  const int gm = min(ntm - first_m, kGroupM);
+  const int tile_m = first_m + (lin % gsz) % gm;
+  const int tile_n = (lin % gsz) / gm;
+  const int nk = p.nkb;
+  const int nchunks = (nk + ozc::CHUNK_KB - 1) / ozc::CHUNK_KB;
+  const int na = p.a_parts;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(chunk_bar, 1);
+    mbar_init(drained_bar, 8);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(ozc::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)(na * OZ_S * A_TILE + NSL * B_TILE);
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        mbar_expect_tx(&full_bar[s], bytes);
+        const int kx = kb * CBK;
+        for (int q = 0; q < na * OZ_S; ++q)
+          tma_load_2d(st + q * A_TILE, &mapA, &full_bar[s], kx, (int)(q * p.rowsA + tile_m * CBM));
+        for (int q = 0; q < NSL; ++q)
+          tma_load_2d(st + NSL * A_TILE + q * B_TILE, &mapB, &full_bar[s], kx, (int)(q * p.rowsB + tile_n * CBN));
+        issued = kb + 1;
+      }
+      if (*abort_flag) {
+        for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb) {
+          long long t0 = clock64();
+          while (!mbar_try_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u) &&
+                 clock64() - t0 < kWaitCycles) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t id_pos = make_idesc_ozc(false), id_neg = make_idesc_ozc(true);
+      for (int kb = 0; kb < nk; ++kb) {
+        const int kc = kb % ozc::CHUNK_KB, chunk = kb / ozc::CHUNK_KB;
+        if (kc == 0 && chunk > 0) {
+          // the epilogue must have read the previous chunk's exact accumulators
+          if (!mbar_wait(drained_bar, (uint32_t)(chunk - 1) & 1u, p.err, abort_flag, 4)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        const int s = kb % STAGES;
+        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint64_t a0 = make_desc_sw32(smem_u32(smem + s * STAGE_BYTES));
+        const uint64_t b0 = make_desc_sw32(smem_u32(smem + s * STAGE_BYTES + NSL * A_TILE));
+        // products (A part, B part, accumulator set, -A): Re.Re, Im.Im -> Re; Re.Im, Im.Re -> Im
+#pragma unroll
+        for (int pr = 0; pr < 4; ++pr) {
+          const int aq = (pr == 1 || pr == 3) ? 1 : 0, bq = (pr == 1 || pr == 2) ? 1 : 0;
+          const int set = pr >= 2 ? 1 : 0;
+          if (aq == 1 && na == 1) continue;                 // a real A has no Im part
+          const uint32_t idesc = pr == 1 ? id_neg : id_pos;
+#pragma unroll
+          for (int sa = 0; sa < OZ_S; ++sa) {
+#pragma unroll
+            for (int tb = 0; tb + sa < OZ_S; ++tb) {
+              const int g = sa + tb;
+              const int d = g < 4 ? g : 4;
+              const uint64_t a = a0 + (uint64_t)(((aq * OZ_S + sa) * A_TILE) >> 4);
+              const uint64_t b = b0 + (uint64_t)(((bq * OZ_S + tb) * B_TILE) >> 4);
+              // the set's first product opens each exact group per chunk and the tail once
+              const bool first = (pr == 0 || pr == 2) && sa == 0 && ((g < 4 && kc == 0) || (g == 4 && kb == 0));
+              mma_bf16(tmem_base + (uint32_t)((set * 5 + d) * CBN), a, b, idesc, first ? 0u : 1u);
+            }
+          }
+        }
+        mma_commit(&empty_bar[s]);
+        if (kc == ozc::CHUNK_KB - 1 || kb == nk - 1) mma_commit(chunk_bar);
+      }
+    }
+  } else {
+    // epilogue: warps 2..9; TMEM lane quadrant q = warp % 4, column half h
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * EPI);
+    long long ar[EPI], ai[EPI];   // exact group sums in units of 2^-21
+#pragma unroll
+    for (int j = 0; j < EPI; ++j) ar[j] = ai[j] = 0;
+    bool ok = nk > 0;
+    for (int c = 0; c < nchunks && ok; ++c) {
+      int okw = 0;
+      if (lane == 0) okw = mbar_wait(chunk_bar, (uint32_t)c & 1u, p.err, abort_flag, 3) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int set = 0; set < 2; ++set) {
+        uint32_t g0[16], g1[16], g2[16], g3[16];
+        const uint32_t sb = lane_base + (uint32_t)(set * 5 * CBN);
+        tmem_ld16_async(sb, g0);
+        tmem_ld16_async(sb + CBN, g1);
+        tmem_ld16_async(sb + 2 * CBN, g2);
+        tmem_ld16_async(sb + 3 * CBN, g3);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long long i0 = __float2int_rn(__uint_as_float(g0[j]));
+          const long long i1 = __float2int_rn(__uint_as_float(g1[j]) * 128.0f);
+          const long long i2 = __float2int_rn(__uint_as_float(g2[j]) * 16384.0f);
+          const long long i3 = __float2int_rn(__uint_as_float(g3[j]) * 2097152.0f);
+          const long long v = (i0 << 21) + (i1 << 14) + (i2 << 7) + i3;
+          if (set == 0) ar[j] += v; else ai[j] += v;
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(drained_bar);
+    }
+    if (ok) {
+      float tr[16], ti[16];
+      tmem_ld16(lane_base + 4 * CBN, tr);
+      tmem_ld16(lane_base + 9 * CBN, ti);
+      const int64_t m = (int64_t)tile_m * CBM + q * 32 + lane;
+      const int64_t n0 = (int64_t)tile_n * CBN + h * EPI;
+      if (m < p.M) {
+        const int fa = p.fA[m];
+        z64* crow = p.C + m * p.ldc;
+#pragma unroll
+        for (int j = 0; j < EPI; ++j) {
+          const int64_t n = n0 + j;
+          if (n < p.N) {
+            const int e2 = fa + p.fB[n] - 32;
+            // exact groups (units 2^-21) and the FP32 tail in units of 2^-32, one rounding
+            z64 out = zmk(i64_ldexp_rn((ar[j] << 11) + f32_fixed32(tr[j]), e2),
+                          i64_ldexp_rn((ai[j] << 11) + f32_fixed32(ti[j]), e2));
+            if (!p.plain) {
+              out = zmul(p.alpha, out);
+              if (p.beta.x != 0.0 || p.beta.y != 0.0) out = zadd(out, zmul(p.beta, crow[n]));
+            }
+            crow[n] = out;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(ozc::TMEM_COLS));
+  }
+}
+
 int64_t rup(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
-bool encode_slices(CUtensorMap* map, uint16_t* base, int64_t rows_total, int64_t Kp, int box_rows) {
+int sign_code(double c) { return c == 0.0 ? 0 : (c == 1.0 ? 1 : (c == -1.0 ? -1 : 2)); }
+
+// Tensor map over slice planes [rows_total][Kp] (bf16): boxes of box_k x box_rows, with the
+// 64-byte swizzle for 32-wide k-blocks (3M kernel) or the 32-byte one for 16-wide (one-pass kernel).
+bool encode_slices(CUtensorMap* map, uint16_t* base, int64_t rows_total, int64_t Kp, int box_rows, int box_k = BK) {
   auto enc = tma_encode_fn();
   if (!enc) return false;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
   cuuint64_t strides[1] = {(cuuint64_t)(Kp * 2)};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1u, 1u};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
+}
+
+// K up to which complex products take the one-pass kernel: there the 3M kernel's three
+// passes, each re-reading and re-writing C, cost more than its 25 % fewer MMAs save.
+constexpr int64_t kOzcMaxK = 1024;
+
+struct OzcLayout {
+  int64_t Mp, Np, Kp;
+  size_t sA, sB, eA, eB, fA, fB, total;   // byte offsets from the scratch base
+};
+
+// na: parts of A sliced (2, or 1 for a real A); B always has both.
+OzcLayout ozc_layout(int64_t M, int64_t N, int64_t K, int na) {
+  OzcLayout L;
+  L.Mp = rup(M, ozc::BM);
+  L.Np = rup(N, ozc::BN);
+  L.Kp = rup(K, 32);      // the slicing kernels work on 32 x 32 tiles
+  size_t off = 256;       // status word
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  L.sA = take((size_t)na * OZ_S * L.Mp * L.Kp * 2);
+  L.sB = take((size_t)2 * OZ_S * L.Np * L.Kp * 2);
+  L.eA = take((size_t)L.Mp * 4);
+  L.eB = take((size_t)L.Np * 4);
+  L.fA = take((size_t)L.Mp * 4);
+  L.fB = take((size_t)L.Np * 4);
+  L.total = off;
+  return L;
 }
 
 struct OzLayout {
@@ -387,7 +750,8 @@ struct OzLayout {
   size_t sA, sB, eA, eB, fA, fB, total;   // byte offsets from the scratch base
 };
 
-OzLayout oz_layout(int64_t M, int64_t N, int64_t K) {
+// pa: parts of A whose slices are held at once (1, or 3 to slice Re, Im and Re + Im in one pass)
+OzLayout oz_layout(int64_t M, int64_t N, int64_t K, int pa) {
   OzLayout L;
   L.Mp = rup(M, BM);
   L.Np = rup(N, BN);
@@ -398,11 +762,11 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t K) {
     off += (bytes + 255) & ~(size_t)255;
     return o;
   };
-  L.sA = take((size_t)OZ_S * L.Mp * L.Kp * 2);
+  L.sA = take((size_t)pa * OZ_S * L.Mp * L.Kp * 2);
   L.sB = take((size_t)OZ_S * L.Np * L.Kp * 2);
-  L.eA = take((size_t)L.Mp * 4);
+  L.eA = take((size_t)pa * L.Mp * 4);
   L.eB = take((size_t)L.Np * 4);
-  L.fA = take((size_t)L.Mp * 4);
+  L.fA = take((size_t)pa * L.Mp * 4);
   L.fB = take((size_t)L.Np * 4);
   L.total = off;
   return L;
@@ -416,8 +780,83 @@ int64_t ozgemm_tiles(int64_t M, int64_t N) { return (rup(M, BM) / BM) * (rup(N, 
 
 size_t ozgemm_scratch_bytes(int64_t M, int64_t N, int64_t K) {
   if (M <= 0 || N <= 0 || K <= 0) return 256;
-  return oz_layout(M, N, K).total;
+  if (K <= kOzcMaxK) return ozc_layout(M, N, K, 2).total;
+  return oz_layout(M, N, K, 1).total;
 }
+
+// Scratch with which a complex A is sliced once for all three products (one read of A
+// instead of three); ozgemm_ex uses that path whenever its scratch is this large.
+size_t ozgemm_scratch_bytes_fused(int64_t M, int64_t N, int64_t K) {
+  if (M <= 0 || N <= 0 || K <= 0) return 256;
+  if (K <= kOzcMaxK) return ozc_layout(M, N, K, 2).total;
+  return oz_layout(M, N, K, 3).total;
+}
+
+namespace {
+// The one-pass complex product (K <= kOzcMaxK): slices with exponents shared by Re and Im.
+agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
+                    const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc, void* scratch,
+                    size_t scratch_bytes, cudaStream_t stream) {
+  const int na = conjA == kSrcReal ? 1 : 2;
+  const OzcLayout L = ozc_layout(M, N, K, na);
+  if (scratch_bytes < L.total) {
+    agb_set_error_message("ozgemm: scratch too small", __FILE__, __LINE__);
+    return AGB_ERR_WORKSPACE;
+  }
+  AGB_ARG_CHECK(L.Mp / ozc::BM <= 65535, "ozgemm: M too large for the grid");
+  AGB_ARG_CHECK(2 * OZ_S * L.Mp < (1ll << 31) && 2 * OZ_S * L.Np < (1ll << 31),
+                "ozgemm: too many rows for a tensor map");
+  char* base = (char*)scratch;
+  uint16_t* sA = (uint16_t*)(base + L.sA);
+  uint16_t* sB = (uint16_t*)(base + L.sB);
+  int* eA = (int*)(base + L.eA);
+  int* eB = (int*)(base + L.eB);
+  int* fA = (int*)(base + L.fA);
+  int* fB = (int*)(base + L.fB);
+  CUtensorMap mA, mB;
+  if (!encode_slices(&mA, sA, na * OZ_S * L.Mp, L.Kp, ozc::BM, ozc::BK) ||
+      !encode_slices(&mB, sB, 2 * OZ_S * L.Np, L.Kp, ozc::BN, ozc::BK)) {
+    agb_set_error_message("ozgemm: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
+    return AGB_ERR_CUDA;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    AGB_CUDA_TRY(cudaFuncSetAttribute(ozc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ozc::SMEM_BYTES));
+    attr_set = true;
+  }
+  // both parts of an operand from one read, under one exponent per row (estride 0)
+  auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int np, int64_t rows_pad,
+                   int* emax, int* fexp, uint16_t* dst) -> agb_status {
+    AGB_CUDA_TRY(cudaMemsetAsync(emax, 0, (size_t)rows_pad * 4, stream));
+    const int64_t t1 = ((rows + 31) / 32) * ((K + 31) / 32);
+    const int g1 = (int)(t1 < 152 * 32 ? t1 : 152 * 32);
+    if (np == 2) oz_rowexp_kernel<2><<<g1, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, 0, emax);
+    else oz_rowexp_kernel<1><<<g1, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, 0, emax);
+    AGB_LAUNCH_CHECK();
+    const int64_t t2 = (rows_pad / 32) * (L.Kp / 32);
+    const int g2 = (int)(t2 < 152 * 32 ? t2 : 152 * 32);
+    if (np == 2)
+      oz_slice_kernel<2><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax, fexp,
+                                                 dst);
+    else
+      oz_slice_kernel<1><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax, fexp,
+                                                 dst);
+    AGB_LAUNCH_CHECK();
+    return AGB_OK;
+  };
+  AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, na, L.Mp, eA, fA, sA));
+  AGB_STATUS_TRY(slice(B, N, sBn, sBk, conjB, 2, L.Np, eB, fB, sB));
+  OzcParams p;
+  p.M = M; p.N = N; p.nkb = (int)(L.Kp / ozc::BK); p.a_parts = na; p.fA = fA; p.fB = fB; p.C = C; p.ldc = ldc;
+  p.alpha = alpha; p.beta = beta;
+  p.plain = alpha.x == 1.0 && alpha.y == 0.0 && beta.x == 0.0 && beta.y == 0.0;
+  p.err = (int*)base; p.rowsA = L.Mp; p.rowsB = L.Np;
+  const dim3 grid((unsigned)(L.Np / ozc::BN), (unsigned)(L.Mp / ozc::BM));
+  ozc_kernel<<<grid, ozc::THREADS, ozc::SMEM_BYTES, stream>>>(mA, mB, p);
+  AGB_LAUNCH_CHECK();
+  return AGB_OK;
+}
+}  // namespace
 
 // C = alpha op(A) op(B) + beta C to ~1e-12 of sum |a||b| on the bf16 tensor cores.
 // scratch: ozgemm_scratch_bytes(M, N, K), 256-byte aligned; its first int is the
@@ -430,7 +869,12 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
   AGB_ARG_CHECK(K > 0, "ozgemm: K must be positive");
   AGB_ARG_CHECK(A && B && C && scratch, "ozgemm: null pointer");
   AGB_ARG_CHECK(((uintptr_t)scratch & 255) == 0, "ozgemm: scratch must be 256-byte aligned");
-  const OzLayout L = oz_layout(M, N, K);
+  if (K <= kOzcMaxK)
+    return ozc_gemm(M, N, K, alpha, A, sAm, sAk, conjA, B, sBk, sBn, conjB, beta, C, ldc, scratch, scratch_bytes,
+                    stream);
+  const bool realA = conjA == kSrcReal, realB = conjB == kSrcReal;
+  const int pa = (!realA && scratch_bytes >= oz_layout(M, N, K, 3).total) ? 3 : 1;
+  const OzLayout L = oz_layout(M, N, K, pa);
   if (scratch_bytes < L.total) {
     agb_set_error_message("ozgemm: scratch too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;
@@ -444,8 +888,14 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
   int* eB = (int*)(base + L.eB);
   int* fA = (int*)(base + L.fA);
   int* fB = (int*)(base + L.fB);
-  CUtensorMap mA, mB;
-  if (!encode_slices(&mA, sA, OZ_S * L.Mp, L.Kp, BM) || !encode_slices(&mB, sB, OZ_S * L.Np, L.Kp, BN)) {
+  const int64_t a_part = (int64_t)OZ_S * L.Mp * L.Kp;   // elements of one part's A slices
+  CUtensorMap mA[3], mB;
+  for (int q = 0; q < pa; ++q)
+    if (!encode_slices(&mA[q], sA + q * a_part, OZ_S * L.Mp, L.Kp, BM)) {
+      agb_set_error_message("ozgemm: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
+      return AGB_ERR_CUDA;
+    }
+  if (!encode_slices(&mB, sB, OZ_S * L.Np, L.Kp, BN)) {
     agb_set_error_message("ozgemm: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
@@ -454,33 +904,49 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
     AGB_CUDA_TRY(cudaFuncSetAttribute(ozgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr_set = true;
   }
-  auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int part, int64_t rows_pad,
-                   int* emax, int* fexp, uint16_t* dst) -> agb_status {
-    AGB_CUDA_TRY(cudaMemsetAsync(emax, 0, (size_t)rows_pad * 4, stream));
-    int64_t t1 = ((rows + 31) / 32) * ((K + 31) / 32);
-    oz_rowexp_kernel<<<(int)(t1 < 152 * 32 ? t1 : 152 * 32), 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part,
-                                                                                emax);
+  // row exponents then slices of np parts (part0 ...) of an operand, one read of it each
+  auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int part0, int np,
+                   int64_t rows_pad, int* emax, int* fexp, uint16_t* dst) -> agb_status {
+    AGB_CUDA_TRY(cudaMemsetAsync(emax, 0, (size_t)np * rows_pad * 4, stream));
+    const int64_t t1 = ((rows + 31) / 32) * ((K + 31) / 32);
+    const int g1 = (int)(t1 < 152 * 32 ? t1 : 152 * 32);
+    if (np == 3) oz_rowexp_kernel<3><<<g1, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part0, rows_pad, emax);
+    else oz_rowexp_kernel<1><<<g1, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part0, rows_pad, emax);
     AGB_LAUNCH_CHECK();
-    int64_t t2 = (rows_pad / 32) * (L.Kp / 32);
-    oz_slice_kernel<<<(int)(t2 < 152 * 32 ? t2 : 152 * 32), 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part,
-                                                                              rows_pad, L.Kp, emax, fexp, dst);
+    const int64_t t2 = (rows_pad / 32) * (L.Kp / 32);
+    const int g2 = (int)(t2 < 152 * 32 ? t2 : 152 * 32);
+    if (np == 3)
+      oz_slice_kernel<3><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part0, rows_pad, L.Kp, rows_pad,
+                                                 emax, fexp, dst);
+    else
+      oz_slice_kernel<1><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, part0, rows_pad, L.Kp, rows_pad,
+                                                 emax, fexp, dst);
     AGB_LAUNCH_CHECK();
     return AGB_OK;
   };
   OzParams p;
-  p.M = M; p.N = N; p.nkb = (int)(L.Kp / BK); p.fA = fA; p.fB = fB; p.C = C; p.ldc = ldc; p.beta = beta;
+  p.M = M; p.N = N; p.nkb = (int)(L.Kp / BK); p.fB = fB; p.C = C; p.ldc = ldc; p.beta = beta;
   p.err = (int*)base; p.rowsA = L.Mp; p.rowsB = L.Np;
+  // |exact sum| < K 2^35 (1 + 2^-6) units of 2^-21: shifted by 11 it stays below 2^63 for K <= 2^16
+  p.fixed = L.Kp <= (1 << 16) ? 1 : 0;
   dim3 grid((unsigned)(L.Np / BN), (unsigned)(L.Mp / BM));
   // 3M coefficients of P1 = Re.Re, P2 = Im.Im, P3 = (Re+Im).(Re+Im)
   const z64 coef[3] = {zmk(1, -1), zmk(-1, -1), zmk(0, 1)};
   const bool use_beta = beta.x != 0.0 || beta.y != 0.0;
+  if (pa == 3) AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, 0, 3, L.Mp, eA, fA, sA));
   for (int part = 0; part < 3; ++part) {
-    if (part == 1 && (conjA == kSrcReal || conjB == kSrcReal)) continue;   // Im.Im of a real operand is zero
-    AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, part, L.Mp, eA, fA, sA));
-    AGB_STATUS_TRY(slice(B, N, sBn, sBk, conjB, part, L.Np, eB, fB, sB));
+    if (part == 1 && (realA || realB)) continue;   // Im.Im of a real operand is zero
+    int qa = 0;                                     // A slice set of this product
+    if (pa == 3) qa = part;
+    else if (!(realA && part == 2))                 // a real A's Re + Im is its Re, still in place
+      AGB_STATUS_TRY(slice(A, M, sAm, sAk, conjA, part, 1, L.Mp, eA, fA, sA));
+    AGB_STATUS_TRY(slice(B, N, sBn, sBk, conjB, part, 1, L.Np, eB, fB, sB));
+    p.fA = fA + qa * L.Mp;
     p.coef = zmul(alpha, coef[part]);
+    p.csx = sign_code(p.coef.x);
+    p.csy = sign_code(p.coef.y);
     p.mode = part > 0 ? 2 : (use_beta ? 1 : 0);
-    ozgemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA, mB, p);
+    ozgemm_kernel<<<grid, THREADS, SMEM_BYTES, stream>>>(mA[qa], mB, p);
     AGB_LAUNCH_CHECK();
   }
   return AGB_OK;

@@ -1,5 +1,7 @@
 """Ozaki-split bf16 tensor-core GEMM (agb_zgemm_oz): FP64-level accuracy against
-NumPy complex128 products, including K crossing the 512-long exact chunks,
+NumPy complex128 products on both of its kernels (K <= 1024: the one-pass 4M kernel,
+256-long exact chunks; longer K: the three-pass 3M kernel, 512-long chunks),
+including K crossing the exact chunks,
 ragged tiles, strided / conjugated operands, alpha/beta, rows of very different
 scale, integer data whose products must come out exact, and the base residual
 of the mixed solver.  Tolerance: 3e-12 of sum |a||b| per element (42-bit slices
@@ -20,15 +22,16 @@ from tests.gpu_util import crandn  # noqa: E402
 TOL = 3e-12
 
 
-def oz(A, B, alpha=1.0, beta=0.0, C=None, conjA=False, conjB=False, transA=False, transB=False):
-    """op(A) op(B) through agb_zgemm_oz; op = transpose / conjugate flags like agb_zgemm."""
+def oz(A, B, alpha=1.0, beta=0.0, C=None, conjA=False, conjB=False, transA=False, transB=False, extra=1):
+    """op(A) op(B) through agb_zgemm_oz; op = transpose / conjugate flags like agb_zgemm.
+    extra > 1 multiplies the scratch, which lets the GEMM slice A once for all products."""
     Ad, Bd = to_dev(A), to_dev(B)
     M, K = (A.shape[1], A.shape[0]) if transA else A.shape
     N = B.shape[0] if transB else B.shape[1]
     sAm, sAk = (1, M) if transA else (K, 1)
     sBk, sBn = (1, K) if transB else (N, 1)
     Cd = to_dev(C) if C is not None else torch.zeros((M, N), dtype=torch.complex128, device="cuda")
-    nb = _lib.load().agb_zgemm_oz_scratch_bytes(M, N, K)
+    nb = _lib.load().agb_zgemm_oz_scratch_bytes(M, N, K) * extra
     buf, sp, _ = workspace(nb)
     buf[:256].zero_()
     alpha, beta = complex(alpha), complex(beta)
@@ -39,7 +42,7 @@ def oz(A, B, alpha=1.0, beta=0.0, C=None, conjA=False, conjB=False, transA=False
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 32), (130, 260, 700), (300, 129, 20), (256, 384, 1500),
-                                   (5, 7, 3), (200, 160, 1025)])
+                                   (5, 7, 3), (200, 160, 1025), (129, 33, 1024), (257, 31, 257), (64, 96, 96)])
 def test_oz_gemm_accuracy(M, N, K):
     rng = np.random.default_rng(M + 7 * N + 13 * K)
     A = crandn(rng, M, K)
@@ -75,11 +78,41 @@ def test_oz_gemm_row_scales():
     assert err.max() < TOL, err.max()
 
 
-def test_oz_gemm_integer_products_exact():
+def test_oz_gemm_extreme_exponents():
+    """Row and column scales from 2^-520 to 2^505: outputs from subnormal (2^-1040) to
+    2^505 times O(1) go through the epilogue's integer conversion to FP64 and its
+    fallback for results outside the normal range."""
+    rng = np.random.default_rng(13)
+    M, N, K = 96, 48, 100
+    Au, Bu = crandn(rng, M, K), crandn(rng, K, N)
+    rs = np.array([2.0 ** -520, 1.0, 2.0 ** 505])[np.arange(M) % 3]
+    cs = np.array([2.0 ** -520, 1.0])[np.arange(N) % 2]
+    got = oz(Au * rs[:, None], Bu * cs[None, :])
+    scale = rs[:, None] * cs[None, :]
+    ref = (Au @ Bu) * scale
+    bound = (np.abs(Au) @ np.abs(Bu)) * scale
+    assert np.all(np.isfinite(got))
+    assert np.all(np.abs(got - ref) <= TOL * bound + 2.0 ** -1072)
+
+
+@pytest.mark.parametrize("conjA", [False, True])
+def test_oz_gemm_single_slicing_pass_is_identical(conjA):
+    """With room for all three parts' A slices the GEMM slices A in one pass: the same
+    slices and products, so the same bits as part-by-part slicing."""
+    rng = np.random.default_rng(17)
+    A, B, C0 = crandn(rng, 300, 1100), crandn(rng, 1100, 130), crandn(rng, 300, 130)
+    one = oz(A, B, alpha=0.3 + 1j, beta=0.5, C=C0, conjA=conjA)
+    fused = oz(A, B, alpha=0.3 + 1j, beta=0.5, C=C0, conjA=conjA, extra=4)
+    np.testing.assert_array_equal(one, fused)
+
+
+@pytest.mark.parametrize("K", [2048, 1000])
+def test_oz_gemm_integer_products_exact(K):
     """Small-integer operands have exact slices, so every partial sum is an exact
-    integer: any rounding inside the tensor-core accumulation would show."""
+    integer: any rounding inside the tensor-core accumulation would show (K = 1000:
+    four 256-long chunks of the one-pass kernel, two products per accumulator)."""
     rng = np.random.default_rng(11)
-    M, N, K = 256, 256, 2048
+    M, N = 256, 256
     A = rng.integers(-127, 128, (M, K)) + 1j * rng.integers(-127, 128, (M, K))
     B = rng.integers(-127, 128, (K, N)) + 1j * rng.integers(-127, 128, (K, N))
     got = oz(A.astype(np.complex128), B.astype(np.complex128))
