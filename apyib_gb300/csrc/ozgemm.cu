@@ -461,24 +461,66 @@ __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64
 // (the Im.Im MMAs negate A) and Im C = Re.Im + Im.Re in another.  Each set is the
 // 3M kernel's five accumulators (exact groups 0..3 and the tail); two products per
 // accumulator double the group bounds (group 3: 2 (2^14 + 2^13) units per k), so the
-// exact chunk is 256 k (< 2^24 units).  The tile is 128 x 32 outputs: 2 sets x 5 x 32
-// = 320 TMEM columns.  The epilogue turns the int64 group sums and the tail into FP64
-// with integer instructions and writes C once: no read-modify-write of C between
-// products and no FP64 arithmetic when alpha = 1 and beta = 0.  A real A (the first
-// AO->MO quarter step) has no Im slices and runs the Re.Re and Re.Im products only.
+// exact chunk is 256 k (< 2^24 units).  The tile is 128 x 48 outputs: 2 sets x 5 x 48
+// = 480 TMEM columns (the widest tile that fits; each MMA instruction then carries 1.5x
+// the work of a 32-wide one, which matters because 21 slice pairs x 4 products make
+// many small MMAs).  The epilogue turns the int64 group sums and the tail into FP64 with
+// integer instructions and writes C once: no read-modify-write of C between products and
+// no FP64 arithmetic when alpha = 1 and beta = 0.  A real A (the first AO->MO quarter
+// step) has no Im slices and runs the Re.Re and Re.Im products only.
 namespace ozc {
-constexpr int BM = 128, BN = 32, BK = 16;            // BK in bf16 elements (32-byte rows)
+constexpr int BM = 128, BN = 48, BK = 16;            // BK in bf16 elements (32-byte rows)
 constexpr int NSL = 2 * OZ_S;                         // slice tiles per operand: Re 0..5, Im 6..11
 constexpr int A_TILE = BM * BK * 2;                   // 4 KB
-constexpr int B_TILE = BN * BK * 2;                   // 1 KB
-constexpr int STAGE_BYTES = NSL * (A_TILE + B_TILE);  // 60 KB
+constexpr int B_TILE = BN * BK * 2;                   // 1.5 KB
+constexpr int STAGE_BYTES = NSL * (A_TILE + B_TILE);  // 66 KB
 constexpr int STAGES = 3;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int THREADS = 320;
-constexpr unsigned TMEM_COLS = 512;                   // Re G0..G3 T | Im G0..G3 T, 32 columns each (320 used)
+constexpr unsigned TMEM_COLS = 512;                   // Re G0..G3 T | Im G0..G3 T, 48 columns each (480 used)
 constexpr int CHUNK_KB = 16;                          // k-blocks per exact chunk (256 k)
-constexpr int EPI_COLS = BN / 2;                      // columns per epilogue warp
+constexpr int EPI_COLS = BN / 2;                      // columns per epilogue warp (three groups of 8)
+constexpr int NP_ALIGN = 96;                          // N padding: whole tiles and the slicer's 32-row tiles
 }  // namespace ozc
+
+// tcgen05.ld of 8 columns without the wait.
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+// Exact group sums g0..g3 (FP32, units 1, 2^-7, 2^-14, 2^-21) as one integer in units of 2^-21.
+__device__ __forceinline__ long long oz_groups(uint32_t g0, uint32_t g1, uint32_t g2, uint32_t g3) {
+  const long long i0 = __float2int_rn(__uint_as_float(g0));
+  const long long i1 = __float2int_rn(__uint_as_float(g1) * 128.0f);
+  const long long i2 = __float2int_rn(__uint_as_float(g2) * 16384.0f);
+  const long long i3 = __float2int_rn(__uint_as_float(g3) * 2097152.0f);
+  return (i0 << 21) + (i1 << 14) + (i2 << 7) + i3;
+}
+
+// Exact sum I (units 2^-21) plus the FP32 tail t, as an integer in units of 2^-32:
+// t 2^21 = u_hi + u_lo with u_hi = rint(t 2^21) (both exact in FP32), then u_lo 2^11 is
+// rounded once, as round(t 2^32) would be.  Needs |t| < 2^9.
+__device__ __forceinline__ long long oz_fixed32(long long I, float t) {
+  const float u = t * 2097152.0f;
+  const float uh = rintf(u);
+  return ((I + (long long)__float2int_rn(uh)) << 11) + (long long)__float2int_rn((u - uh) * 2048.0f);
+}
+
+// T * 2^e2 to the nearest double for e2 in [-1022, 960] (then every |T| < 2^63 gives a
+// normal double): the branch-free part of i64_ldexp_rn.
+__device__ __forceinline__ double i64_ldexp_normal(long long T, int e2) {
+  const unsigned long long sgn = T < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long a = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
+  const int lz = __clzll((long long)a);
+  const unsigned long long m = a << (lz & 63);
+  unsigned long long mant = m >> 11;
+  const unsigned long long rem = m & 0x7FFull;
+  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  const unsigned long long bits = (((unsigned long long)(1085 - lz + e2)) << 52) + mant;
+  return __longlong_as_double((long long)(a == 0 ? 0ull : (bits | sgn)));
+}
 
 // tcgen05 shared-memory descriptor: K-major, 32-byte swizzle, 8-row groups 256 B apart.
 __device__ __forceinline__ uint64_t make_desc_sw32(uint32_t saddr) {
@@ -628,6 +670,57 @@ ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUt
     // epilogue: warps 2..9; TMEM lane quadrant q = warp % 4, column half h
     const int q = warp & 3, h = (warp - 2) >> 2;
     const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * EPI);
+    const int64_t m = (int64_t)tile_m * CBM + q * 32 + lane;
+    const int64_t n0 = (int64_t)tile_n * CBN + h * EPI;
+    // C(m, n) from the int64 sums (units 2^-21) and the FP32 tails of the two sets
+    auto store = [&](int64_t n, long long Ir, long long Ii, float tr, float ti, int fa) {
+      const int e2 = fa + p.fB[n] - 32;
+      // exact groups and the FP32 tail in units of 2^-32, rounded once to FP64
+      const long long Tr = oz_fixed32(Ir, tr), Ti = oz_fixed32(Ii, ti);
+      z64 out;
+      if (e2 >= -1022 && e2 <= 960) out = zmk(i64_ldexp_normal(Tr, e2), i64_ldexp_normal(Ti, e2));
+      else out = zmk(i64_ldexp_rn(Tr, e2), i64_ldexp_rn(Ti, e2));
+      z64* cp = p.C + m * p.ldc + n;
+      if (!p.plain) {
+        out = zmul(p.alpha, out);
+        if (p.beta.x != 0.0 || p.beta.y != 0.0) out = zadd(out, zmul(p.beta, *cp));
+      }
+      *cp = out;
+    };
+    if (nchunks == 1) {
+      // K <= 256: one exact chunk, converted straight from TMEM, 8 columns at a time
+      int okw = 0;
+      if (lane == 0) okw = mbar_wait(chunk_bar, 0u, p.err, abort_flag, 3) ? 1 : 0;
+      if (__shfl_sync(0xffffffffu, okw, 0) != 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int fa = m < p.M ? p.fA[m] : 0;
+#pragma unroll 1
+        for (int c8 = 0; c8 < EPI / 8; ++c8) {
+          uint32_t r0[8], r1[8], r2[8], r3[8], rt[8], i0[8], i1[8], i2[8], i3[8], it[8];
+          const uint32_t sb = lane_base + (uint32_t)(c8 * 8);
+          tmem_ld8_async(sb, r0);
+          tmem_ld8_async(sb + CBN, r1);
+          tmem_ld8_async(sb + 2 * CBN, r2);
+          tmem_ld8_async(sb + 3 * CBN, r3);
+          tmem_ld8_async(sb + 4 * CBN, rt);
+          tmem_ld8_async(sb + 5 * CBN, i0);
+          tmem_ld8_async(sb + 6 * CBN, i1);
+          tmem_ld8_async(sb + 7 * CBN, i2);
+          tmem_ld8_async(sb + 8 * CBN, i3);
+          tmem_ld8_async(sb + 9 * CBN, it);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (m < p.M) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int64_t n = n0 + c8 * 8 + j;
+              if (n < p.N)
+                store(n, oz_groups(r0[j], r1[j], r2[j], r3[j]), oz_groups(i0[j], i1[j], i2[j], i3[j]),
+                      __uint_as_float(rt[j]), __uint_as_float(it[j]), fa);
+            }
+          }
+        }
+      }
+    } else {
     long long ar[EPI], ai[EPI];   // exact group sums in units of 2^-21
 #pragma unroll
     for (int j = 0; j < EPI; ++j) ar[j] = ai[j] = 0;
@@ -640,21 +733,20 @@ ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUt
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int set = 0; set < 2; ++set) {
-        uint32_t g0[16], g1[16], g2[16], g3[16];
-        const uint32_t sb = lane_base + (uint32_t)(set * 5 * CBN);
-        tmem_ld16_async(sb, g0);
-        tmem_ld16_async(sb + CBN, g1);
-        tmem_ld16_async(sb + 2 * CBN, g2);
-        tmem_ld16_async(sb + 3 * CBN, g3);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const long long i0 = __float2int_rn(__uint_as_float(g0[j]));
-          const long long i1 = __float2int_rn(__uint_as_float(g1[j]) * 128.0f);
-          const long long i2 = __float2int_rn(__uint_as_float(g2[j]) * 16384.0f);
-          const long long i3 = __float2int_rn(__uint_as_float(g3[j]) * 2097152.0f);
-          const long long v = (i0 << 21) + (i1 << 14) + (i2 << 7) + i3;
-          if (set == 0) ar[j] += v; else ai[j] += v;
+        for (int c8 = 0; c8 < EPI / 8; ++c8) {
+          uint32_t g0[8], g1[8], g2[8], g3[8];
+          const uint32_t sb = lane_base + (uint32_t)(set * 5 * CBN + c8 * 8);
+          tmem_ld8_async(sb, g0);
+          tmem_ld8_async(sb + CBN, g1);
+          tmem_ld8_async(sb + 2 * CBN, g2);
+          tmem_ld8_async(sb + 3 * CBN, g3);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const long long v = oz_groups(g0[j], g1[j], g2[j], g3[j]);
+            if (set == 0) ar[c8 * 8 + j] += v; else ai[c8 * 8 + j] += v;
+          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -662,30 +754,23 @@ ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUt
       if (lane == 0) mbar_arrive(drained_bar);
     }
     if (ok) {
-      float tr[16], ti[16];
-      tmem_ld16(lane_base + 4 * CBN, tr);
-      tmem_ld16(lane_base + 9 * CBN, ti);
-      const int64_t m = (int64_t)tile_m * CBM + q * 32 + lane;
-      const int64_t n0 = (int64_t)tile_n * CBN + h * EPI;
-      if (m < p.M) {
-        const int fa = p.fA[m];
-        z64* crow = p.C + m * p.ldc;
+      const int fa = m < p.M ? p.fA[m] : 0;
 #pragma unroll
-        for (int j = 0; j < EPI; ++j) {
-          const int64_t n = n0 + j;
-          if (n < p.N) {
-            const int e2 = fa + p.fB[n] - 32;
-            // exact groups (units 2^-21) and the FP32 tail in units of 2^-32, one rounding
-            z64 out = zmk(i64_ldexp_rn((ar[j] << 11) + f32_fixed32(tr[j]), e2),
-                          i64_ldexp_rn((ai[j] << 11) + f32_fixed32(ti[j]), e2));
-            if (!p.plain) {
-              out = zmul(p.alpha, out);
-              if (p.beta.x != 0.0 || p.beta.y != 0.0) out = zadd(out, zmul(p.beta, crow[n]));
-            }
-            crow[n] = out;
+      for (int c8 = 0; c8 < EPI / 8; ++c8) {
+        uint32_t tr[8], ti[8];
+        tmem_ld8_async(lane_base + 4 * CBN + c8 * 8, tr);
+        tmem_ld8_async(lane_base + 9 * CBN + c8 * 8, ti);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (m < p.M) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t n = n0 + c8 * 8 + j;
+            if (n < p.N)
+              store(n, ar[c8 * 8 + j], ai[c8 * 8 + j], __uint_as_float(tr[j]), __uint_as_float(ti[j]), fa);
           }
         }
       }
+    }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -727,7 +812,7 @@ struct OzcLayout {
 OzcLayout ozc_layout(int64_t M, int64_t N, int64_t K, int na) {
   OzcLayout L;
   L.Mp = rup(M, ozc::BM);
-  L.Np = rup(N, ozc::BN);
+  L.Np = rup(N, ozc::NP_ALIGN);
   L.Kp = rup(K, 32);      // the slicing kernels work on 32 x 32 tiles
   size_t off = 256;       // status word
   auto take = [&](size_t bytes) {
@@ -851,7 +936,7 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
   p.alpha = alpha; p.beta = beta;
   p.plain = alpha.x == 1.0 && alpha.y == 0.0 && beta.x == 0.0 && beta.y == 0.0;
   p.err = (int*)base; p.rowsA = L.Mp; p.rowsB = L.Np;
-  const dim3 grid((unsigned)(L.Np / ozc::BN), (unsigned)(L.Mp / ozc::BM));
+  const dim3 grid((unsigned)((N + ozc::BN - 1) / ozc::BN), (unsigned)(L.Mp / ozc::BM));
   ozc_kernel<<<grid, ozc::THREADS, ozc::SMEM_BYTES, stream>>>(mA, mB, p);
   AGB_LAUNCH_CHECK();
   return AGB_OK;

@@ -62,18 +62,20 @@ using namespace tc05;
 
 constexpr int BM = 128, BN = 256, BK = 16;   // K padding of the planes, in fp32 elements (64 bytes)
 constexpr int THREADS = 192;
-// Single-CTA tile shapes: 128 x NB outputs, NB = 256 (2 stages of 96 KB, one CTA per SM) or,
-// for outputs at most 64 wide, NB = 64 (2 stages of 48 KB, two CTAs per SM, so one CTA's
-// epilogue overlaps the other's loads): a 60-wide output then pays for 64 columns of MMA
-// work and operand traffic, not 256.
+// Single-CTA tile shapes: 128 x NB outputs, NB = 256 (2 stages of 96 KB, one CTA per SM),
+// NB = 160 for outputs 65..160 wide (2 stages of 72 KB; the AO->MO quarter steps' 150-wide
+// outputs), or, for outputs at most 64 wide, NB = 64 (2 stages of 48 KB, two CTAs per SM,
+// so one CTA's epilogue overlaps the other's loads): a narrow output then pays for the
+// MMA work and operand traffic of its own width, not of 256 columns.
 template <int NB> struct Tile {
   static constexpr int STAGES = 2;
-  static constexpr int CTAS_PER_SM = NB == 256 ? 1 : 2;
+  static constexpr int CTAS_PER_SM = NB == 64 ? 2 : 1;
   static constexpr int A_TILE_BYTES = BM * BK * 4;
   static constexpr int B_TILE_BYTES = NB * BK * 4;
   static constexpr int STAGE_BYTES = 4 * (A_TILE_BYTES + B_TILE_BYTES);
   static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-  static constexpr unsigned TMEM_COLS = 2 * NB;                // Re and Im accumulators
+  // Re and Im accumulators (2 NB columns), allocated as a power of two
+  static constexpr unsigned TMEM_COLS = 2 * NB <= 128 ? 128u : (2 * NB <= 256 ? 256u : 512u);
 };
 
 // tcgen05 shared-memory descriptor of a K-major tile with 64-byte swizzle (16 fp32 per row),
@@ -640,7 +642,7 @@ agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_r
 
 namespace {
 // Tile width of the single-CTA kernel for an N-wide output.
-int tile_n_for(int64_t N) { return N <= 64 ? 64 : BN; }
+int tile_n_for(int64_t N) { return N <= 64 ? 64 : (N <= 160 ? 160 : BN); }
 
 int choose_splits(int64_t M, int64_t N, int64_t nkb, size_t partial_cap) {
   const int nb = tile_n_for(N);
@@ -692,6 +694,8 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
                                       Tile<256>::SMEM_BYTES));
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Tile<64>::SMEM_BYTES));
+    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<160>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<160>::SMEM_BYTES));
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       P2_SMEM_BYTES));
     attr_set = true;
@@ -713,6 +717,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     tf32x3_gemm2_kernel<<<grid2, THREADS, P2_SMEM_BYTES, stream>>>(mA, mB, p);
   } else {
     if (nb == 64) tf32x3_gemm_kernel<64><<<grid, THREADS, Tile<64>::SMEM_BYTES, stream>>>(mA, mB, p);
+    else if (nb == 160) tf32x3_gemm_kernel<160><<<grid, THREADS, Tile<160>::SMEM_BYTES, stream>>>(mA, mB, p);
     else tf32x3_gemm_kernel<256><<<grid, THREADS, Tile<256>::SMEM_BYTES, stream>>>(mA, mB, p);
   }
   AGB_LAUNCH_CHECK();
