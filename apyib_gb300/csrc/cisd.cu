@@ -49,10 +49,10 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
 // AGB_PREC_OZAKI mode; smaller ones (few tiles, long K) the split-K double-float kernel.
 constexpr int64_t kOzMinTiles = 152;
 agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
-                            float* dst, cudaStream_t stream);
+                            float* dst, cudaStream_t stream, int kblk);
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
                             z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
-                            int trans_c);
+                            int trans_c, int kblkA, int kblkB);
 
 namespace {
 
@@ -226,61 +226,59 @@ __global__ void unpack_ring_kernel(const z64* __restrict__ t2p, int o, int v, in
 // The ring GEMM's A operand straight from the packed amplitudes, as the four zero-padded
 // K-major TF32 planes the tensor-core GEMM reads (re_hi, re_lo, im_hi, im_lo of
 // Tring[(i,a)][(k,c)] = t2[i,k,a,c]), for 3xTF32 residuals: no FP64 Tring is written and
-// re-read by a separate operand split.
+// re-read by a separate operand split.  One warp per row (i,a), lanes along (k,c), so the
+// plane writes are coalesced; with Fov it also forms the singles term
+// r1x[(i,a)] = sum_(k,c) t2[i,k,a,c] F_kc (apyib/ci_wfn.py:313, F_jb t2_ijab) from the values
+// it has just unpacked, in FP32 (the 3xTF32 residual's own level).
 __global__ void unpack_ring_planes_kernel(const z64* __restrict__ t2p, int o, int v, int64_t pv, int64_t rows_pad,
-                                          int64_t Kp, float* __restrict__ planes) {
-  const int64_t ov = (int64_t)o * v, plane = rows_pad * Kp;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < plane; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = e / Kp, col = e % Kp;
-    z64 val = zmk(0, 0);
-    if (row < ov && col < ov) {
-      const int i = (int)(row / v), a = (int)(row % v), k = (int)(col / v), c = (int)(col % v);
-      const int sg = sgn_pair(i, k) * sgn_pair(a, c);
-      if (sg != 0) {
-        val = t2p[pair_index(min(i, k), max(i, k), o) * pv + pair_index(min(a, c), max(a, c), v)];
-        if (sg < 0) val = zneg(val);
-      }
-    }
-    uint32_t rh, rl, ih, il;
-    split_tf32_fast((uint32_t)__double2hiint(val.x), (uint32_t)__double2loint(val.x), rh, rl);
-    split_tf32_fast((uint32_t)__double2hiint(val.y), (uint32_t)__double2loint(val.y), ih, il);
-    planes[e] = __uint_as_float(rh);
-    planes[plane + e] = __uint_as_float(rl);
-    planes[2 * plane + e] = __uint_as_float(ih);
-    planes[3 * plane + e] = __uint_as_float(il);
-  }
-}
-
-// r1[i,a] += sum_{k,c} t2[i,k,a,c] F_kc (the F_jb t2_ijab term of apyib/ci_wfn.py:313) from the
-// half-unpacked t2h[i][k][(a<c)], FP32 arithmetic for 3xTF32 residuals; one warp per (i,a),
-// the warps of one i sharing its slice of t2h in L2.
-__global__ void r1_fov_t2_kernel(const z64* __restrict__ t2h, int o, int v, int64_t pv, const z64* __restrict__ Fov,
-                                 z64* __restrict__ r1) {
+                                          int64_t Kp, const z64* __restrict__ Fov, z64* __restrict__ r1x,
+                                          float* __restrict__ planes) {
   const int lane = threadIdx.x & 31;
-  const int64_t ov = (int64_t)o * v;
+  const int64_t ov = (int64_t)o * v, plane = rows_pad * Kp;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t row = warp; row < ov; row += nwarps) {
-    const int i = (int)(row / v), a = (int)(row % v);
+  for (int64_t row = warp; row < rows_pad; row += nwarps) {
+    const bool live = row < ov;
+    const int i = live ? (int)(row / v) : 0, a = live ? (int)(row % v) : 0;
     float re = 0.f, im = 0.f;
-    for (int64_t idx = lane; idx < ov; idx += 32) {
-      const int k = (int)(idx / v), c = (int)(idx % v);
-      if (c == a) continue;
-      z64 t = t2h[((int64_t)i * o + k) * pv + pair_index(min(a, c), max(a, c), v)];
-      if (c < a) t = zneg(t);
-      const float4 tv = split_z_fast(t);
-      const float4 fv = split_z_fast(Fov[idx]);
-      re = fmaf(tv.x, fv.x, re);
-      re = fmaf(-tv.z, fv.z, re);
-      im = fmaf(tv.x, fv.z, im);
-      im = fmaf(tv.z, fv.x, im);
+    for (int64_t col = lane; col < Kp; col += 32) {
+      z64 val = zmk(0, 0);
+      const bool in = live && col < ov;
+      int k = 0, c = 0;
+      if (in) {
+        k = (int)(col / v);
+        c = (int)(col % v);
+        const int sg = sgn_pair(i, k) * sgn_pair(a, c);
+        if (sg != 0) {
+          val = t2p[pair_index(min(i, k), max(i, k), o) * pv + pair_index(min(a, c), max(a, c), v)];
+          if (sg < 0) val = zneg(val);
+        }
+      }
+      uint32_t rh, rl, ih, il;
+      split_tf32_fast((uint32_t)__double2hiint(val.x), (uint32_t)__double2loint(val.x), rh, rl);
+      split_tf32_fast((uint32_t)__double2hiint(val.y), (uint32_t)__double2loint(val.y), ih, il);
+      const int64_t e = row * Kp + col;
+      planes[e] = __uint_as_float(rh);
+      planes[plane + e] = __uint_as_float(rl);
+      planes[2 * plane + e] = __uint_as_float(ih);
+      planes[3 * plane + e] = __uint_as_float(il);
+      if (Fov && in) {
+        const float tr = __uint_as_float(rh) + __uint_as_float(rl), ti = __uint_as_float(ih) + __uint_as_float(il);
+        const float4 f = split_z_fast(Fov[col]);
+        re = fmaf(tr, f.x, re);
+        re = fmaf(-ti, f.z, re);
+        im = fmaf(tr, f.z, im);
+        im = fmaf(ti, f.x, im);
+      }
     }
+    if (Fov && live) {
 #pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      re += __shfl_xor_sync(0xffffffffu, re, off);
-      im += __shfl_xor_sync(0xffffffffu, im, off);
+      for (int off = 16; off; off >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, off);
+        im += __shfl_xor_sync(0xffffffffu, im, off);
+      }
+      if (lane == 0) r1x[row] = zmk(f2d_exact(re), f2d_exact(im));
     }
-    if (lane == 0) r1[row] = zadd(r1[row], zmk(f2d_exact(re), f2d_exact(im)));
   }
 }
 
@@ -317,9 +315,14 @@ __global__ void unpack_q_kernel(const z64* __restrict__ t2p, int64_t po, int v, 
 }
 
 // y = x (or 0) , optionally y -= E*t
-__global__ void r1_init_kernel(const z64* __restrict__ src, int64_t n, z64* __restrict__ r) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    r[e] = src ? src[e] : zmk(0, 0);
+// r = src (or 0), plus add (when given)
+__global__ void r1_init_kernel(const z64* __restrict__ src, const z64* __restrict__ add, int64_t n,
+                               z64* __restrict__ r) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    z64 x = src ? src[e] : zmk(0, 0);
+    if (add) x = zadd(x, add[e]);
+    r[e] = x;
+  }
 }
 __global__ void axpy_kernel(int64_t n, z64 alpha, const z64* __restrict__ x, z64* __restrict__ y) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
@@ -734,7 +737,7 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   P->vpairs = (int2*)take(sizeof(int2) * (pv > 0 ? pv : 1));
   P->R0p = (z64*)take(Z * po * pv);
   if (P->mp2_only) {
-    P->VT = P->WooooT = P->Wvp = P->Tring = P->X = P->PQ = P->t2h = P->t2q = P->Gq = P->H2h = nullptr;
+    P->VT = P->WooooT = P->Wvp = P->Tring = P->X = P->PQ = P->t2h = P->t2q = P->Gq = P->H2h = P->R1x = nullptr;
     P->WvovvH = P->WooovP = P->WovooP = P->WvvvoP = P->Zq = P->Yh = nullptr;
     P->gemm_scratch = take(4096);
     P->gemm_scratch_bytes = 4096;
@@ -753,6 +756,7 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   P->t2q = (z64*)take(Z * po * v * v);
   P->Gq = (z64*)take(Z * po * v * v);
   P->H2h = (z64*)take(Z * o * o * pv);
+  P->R1x = (z64*)take(Z * ov);
   if (P->singles) {
     P->WvovvH = (z64*)take(Z * v * o * pv);
     P->WooovP = (z64*)take(Z * o * po * v);
@@ -831,10 +835,13 @@ namespace {
 // GEMM on the selected backend.  conj flags are never needed on the hot path.
 // PA / PB: TF32 planes of a static operand prepared at set-up (tensor-core path only).
 // trans_c: C(m, n) lives at C[n * ldc + m]; the 3xTF32 kernel stores it so, the other
-// backends compute the same product as C^T = B^T A^T.
+// backends compute the same product as C^T = B^T A^T.  kblk: both operands' planes are
+// K-blocked (static ones prepared so at set-up; the singles GEMMs, whose operands are up to
+// 1.7M elements long in K).
 agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm,
                 int64_t sAk, const z64* B, int64_t sBk, int64_t sBn, z64 beta, z64* C, int64_t ldc,
-                cudaStream_t st, const float* PA = nullptr, const float* PB = nullptr, int trans_c = 0) {
+                cudaStream_t st, const float* PA = nullptr, const float* PB = nullptr, int trans_c = 0,
+                int kblk = 0) {
   if (prec == AGB_PREC_TF32X3) {
     if (M == 0 || N == 0) return AGB_OK;
     if (K == 0) return zgemm_ex(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, nullptr, 0, st);
@@ -842,12 +849,12 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
     size_t off = 256;
     if (!PA) {
       PA = (const float*)(base + off);
-      AGB_STATUS_TRY(tf32_prep_planes(A, M, K, sAm, sAk, 0, (float*)PA, st));
+      AGB_STATUS_TRY(tf32_prep_planes(A, M, K, sAm, sAk, 0, (float*)PA, st, kblk));
       off += align256(tf32_planes_bytes(M, K));
     }
     if (!PB) {
       PB = (const float*)(base + off);
-      AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, 0, (float*)PB, st));
+      AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, 0, (float*)PB, st, kblk));
       off += align256(tf32_planes_bytes(N, K));
     }
     if (off > P->gemm_scratch_bytes) {
@@ -855,7 +862,7 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
       return AGB_ERR_WORKSPACE;
     }
     return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
-                            P->gemm_scratch_bytes - off, st, trans_c);
+                            P->gemm_scratch_bytes - off, st, trans_c, kblk, kblk);
   }
   if (trans_c) return gemm(P, prec, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, ldc, st);
   if (prec == AGB_PREC_OZAKI && ozgemm_tiles(M, N) >= kOzMinTiles)
@@ -869,18 +876,23 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
                   P->gemm_scratch_bytes - 256, st);
 }
 
+// The singles GEMMs read K-blocked planes when every operand they take as A (v-row and
+// (j,p(ab))-row operands) has more than 64 rows, so that its planes hold whole 128-row boxes.
+int singles_kblk(const agb_cisd_plan* P) { return (P->v > 64 && (int64_t)P->o * P->pv > 64) ? 1 : 0; }
+
 // TF32 planes of every static ERI-block operand, in the orientation its GEMM reads it.
 agb_status prepare_static_planes(agb_cisd_plan* P, cudaStream_t st) {
   if (!P->mixed || P->mp2_only) return AGB_OK;
   const int64_t o = P->o, v = P->v, ov = P->ov, po = P->po, pv = P->pv;
-  AGB_STATUS_TRY(tf32_prep_planes(P->VT, ov, ov, ov, 1, 0, P->P_VT, st));
-  AGB_STATUS_TRY(tf32_prep_planes(P->Wvp, pv, pv, pv, 1, 0, P->P_Wvp, st));
-  AGB_STATUS_TRY(tf32_prep_planes(P->WooooT, po, po, po, 1, 0, P->P_Woooo, st));
+  AGB_STATUS_TRY(tf32_prep_planes(P->VT, ov, ov, ov, 1, 0, P->P_VT, st, 0));
+  AGB_STATUS_TRY(tf32_prep_planes(P->Wvp, pv, pv, pv, 1, 0, P->P_Wvp, st, 0));
+  AGB_STATUS_TRY(tf32_prep_planes(P->WooooT, po, po, po, 1, 0, P->P_Woooo, st, 0));
   if (P->singles) {
-    AGB_STATUS_TRY(tf32_prep_planes(P->WvovvH, v, o * pv, o * pv, 1, 0, P->P_Wvovv, st));
-    AGB_STATUS_TRY(tf32_prep_planes(P->WooovP, o, po * v, po * v, 1, 0, P->P_Wooov, st));
-    AGB_STATUS_TRY(tf32_prep_planes(P->WovooP, po * v, o, o, 1, 0, P->P_Wovoo, st));
-    AGB_STATUS_TRY(tf32_prep_planes(P->WvvvoP, o * pv, v, 1, o * pv, 0, P->P_Wvvvo, st));
+    const int kb = singles_kblk(P);
+    AGB_STATUS_TRY(tf32_prep_planes(P->WvovvH, v, o * pv, o * pv, 1, 0, P->P_Wvovv, st, kb));
+    AGB_STATUS_TRY(tf32_prep_planes(P->WooovP, o, po * v, po * v, 1, 0, P->P_Wooov, st, kb));
+    AGB_STATUS_TRY(tf32_prep_planes(P->WovooP, po * v, o, o, 1, 0, P->P_Wovoo, st, kb));
+    AGB_STATUS_TRY(tf32_prep_planes(P->WvvvoP, o * pv, v, 1, o * pv, 0, P->P_Wvvvo, st, kb));
   }
   return AGB_OK;
 }
@@ -1125,7 +1137,10 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
   const bool ring_planes = prec == AGB_PREC_TF32X3;
   if (ring_planes) {
     const int64_t rp = tf32_rows_pad(ov), kp = tf32_k_pad(ov);
-    unpack_ring_planes_kernel<<<grid_for(rp * kp, 256), 256, 0, st>>>(t2p, o, v, pv, rp, kp, (float*)P->Tring);
+    // one warp per plane row; with singles it also forms the F_jb t2_ijab term into R1x
+    unpack_ring_planes_kernel<<<grid_for(rp * 32, 256), 256, 0, st>>>(t2p, o, v, pv, rp, kp,
+                                                                      P->singles ? P->EW : nullptr, P->R1x,
+                                                                      (float*)P->Tring);
   } else {
     unpack_ring_kernel<<<grid_for(ov * ov, 256), 256, 0, st>>>(t2p, o, v, pv, P->Tring);
   }
@@ -1140,7 +1155,8 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
   if (P->singles) {
     // r1 = F_ai - F_ji t1_ja + F_ab t1_ib + <ja||bi> t1_jb + F_jb t2_ijab + 1/2 <aj||cb> t2_ijcb
     //      - 1/2 <kj||ib> t2_kjab - E t1                                    (apyib/ci_wfn.py:309-316)
-    r1_init_kernel<<<grid_for(n1, 256), 256, 0, st>>>((flags & AGB_RES_CONST) ? P->FvoT : nullptr, n1, r1);
+    r1_init_kernel<<<grid_for(n1, 256), 256, 0, st>>>((flags & AGB_RES_CONST) ? P->FvoT : nullptr,
+                                                      ring_planes ? P->R1x : nullptr, n1, r1);
     AGB_LAUNCH_CHECK();
     AGB_STATUS_TRY(gemm(P, prec, o, v, o, zmk(-1, 0), P->Foo, 1, o, t1, v, 1, one, r1, v, st));
     AGB_STATUS_TRY(gemm(P, prec, o, v, v, one, t1, v, 1, P->Fvv, 1, v, one, r1, v, st));
@@ -1148,30 +1164,29 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     // (~2^-44), the 3xTF32 mode an FP32 one (its GEMM terms carry FP32-level error)
     auto gemv = prec == AGB_PREC_FP64 ? zgemv : (prec == AGB_PREC_TF32X3 ? zgemv_f32 : zgemv_df);
     AGB_STATUS_TRY(gemv(ov, ov, one, P->VT, ov, t1, one, r1, st));
-    if (ring_planes) {
-      r1_fov_t2_kernel<<<grid_for(ov * 32, 256), 256, 0, st>>>(P->t2h, o, v, pv, P->EW, r1);
-      AGB_LAUNCH_CHECK();
-    } else {
+    // (3xTF32: the F_jb t2_ijab term came with the ring planes, added by r1_init)
+    if (!ring_planes) {
       AGB_STATUS_TRY(gemv(ov, ov, one, P->Tring, ov, P->EW, one, r1, st));
     }
     // The singles GEMMs run with the long or static extent as M and the o-wide one as N:
     // under 3xTF32 an o-wide N takes the 64-wide tile and the transposed store keeps the
     // output's writes coalesced (r1 and Yh are i-major, Zq a-minor).
     // r1[i][a] += sum_(j,p(cb)) <aj||cb> t2h[i][j][p(cb)]
+    const int kb = singles_kblk(P);
     AGB_STATUS_TRY(gemm(P, prec, v, o, (int64_t)o * pv, one, P->WvovvH, (int64_t)o * pv, 1, P->t2h, 1,
-                        (int64_t)o * pv, one, r1, v, st, P->P_Wvovv, nullptr, 1));
+                        (int64_t)o * pv, one, r1, v, st, P->P_Wvovv, nullptr, 1, kb));
     // r1[i][a] += sum_(p(kj),b) <kj||ib> t2q[p(kj)][b][a]
     AGB_STATUS_TRY(gemm(P, prec, v, o, po * v, one, P->t2q, 1, v, P->WooovP, 1, po * v, one, r1, v, st, nullptr,
-                        P->P_Wooov, 1));
+                        P->P_Wooov, 1, kb));
     if (flags & AGB_RES_ETERM) {
       axpy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(n1, zneg(E), t1, r1);
       AGB_LAUNCH_CHECK();
     }
     // Zq[p(ij)][b][a] = sum_k <kb||ij> t1[k,a];  Yh[i][j][p(ab)] = sum_c t1[i,c] <ab||cj>
     AGB_STATUS_TRY(gemm(P, prec, v, po * v, o, one, t1, 1, v, P->WovooP, 1, o, zero, P->Zq, v, st, nullptr,
-                        P->P_Wovoo, 1));
+                        P->P_Wovoo, 1, kb));
     AGB_STATUS_TRY(gemm(P, prec, (int64_t)o * pv, o, v, one, P->WvvvoP, 1, (int64_t)o * pv, t1, 1, v, zero, P->Yh,
-                        (int64_t)o * pv, st, P->P_Wvvvo, nullptr, 1));
+                        (int64_t)o * pv, st, P->P_Wvvvo, nullptr, 1, kb));
   }
   // ladders: PQ = sum_{k<l} <kl||ij> t2p[kl,ab] + sum_{c<d} t2p[ij,cd] <ab||cd>
   AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st, P->P_Woooo));

@@ -32,6 +32,7 @@ struct agb_cisd_plan {
   agb::z64 *Yh;                       // [i][j][p(ab)]
   agb::z64 *Gq;                       // [p(ij)][a][b]
   agb::z64 *H2h;                      // [i][j][p(ab)]
+  agb::z64 *R1x;                      // [(i,a)] sum_(k,c) t2[i,k,a,c] F_kc, from the ring-plane unpack
   // TF32 hi/lo planes of the static operands (mixed plans only)
   float *P_VT = nullptr, *P_Wvp = nullptr, *P_Woooo = nullptr, *P_Wvovv = nullptr, *P_Wooov = nullptr,
         *P_Wovoo = nullptr, *P_Wvvvo = nullptr;

@@ -120,6 +120,7 @@ struct GemmParams {
   int* err;
   int64_t rowsA, rowsB;  // padded rows per plane
   int trans_c;           // store C(m, n) at C[n * ldc + m] instead of C[m * ldc + n]
+  int kblkA, kblkB;      // operand planes K-blocked ([k/16][row][16] per plane), read through 3D maps
 };
 
 template <int NB>
@@ -182,11 +183,19 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
         if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
         uint8_t* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-        int kx = (kb0 + kb) * BK;
+        const int kx = (kb0 + kb) * BK;
         for (int pl = 0; pl < 4; ++pl) {
-          tma_load_2d(st + pl * A_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
-          tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kx,
-                      (int)(pl * p.rowsB + tile_n * NB));
+          // K-blocked planes: one contiguous box per (plane, k-block); rows past the plane read zeros
+          if (p.kblkA)
+            tma_load_3d(st + pl * A_TILE_BYTES, &mapA, &full_bar[s], 0, tile_m * BM, pl * p.nkb_total + kb0 + kb);
+          else
+            tma_load_2d(st + pl * A_TILE_BYTES, &mapA, &full_bar[s], kx, (int)(pl * p.rowsA + tile_m * BM));
+          if (p.kblkB)
+            tma_load_3d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], 0, tile_n * NB,
+                        pl * p.nkb_total + kb0 + kb);
+          else
+            tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kx,
+                        (int)(pl * p.rowsB + tile_n * NB));
         }
         issued = kb + 1;
       }
@@ -541,7 +550,7 @@ tf32x3_gemm2_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_const
 
 // planes[4][rows][Kp]: re_hi, re_lo, im_hi, im_lo of X(row, k) = src[row*s_row + k*s_k], zero padded.
 __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t K, int64_t s_row, int64_t s_k,
-                            int conj, int64_t rows_pad, int64_t Kp, float* __restrict__ planes) {
+                            int conj, int64_t rows_pad, int64_t Kp, int kblk, float* __restrict__ planes) {
   __shared__ z64 tile[32][33];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
@@ -568,7 +577,7 @@ __global__ void prep_kernel(const z64* __restrict__ src, int64_t nrows, int64_t 
       uint32_t rh, rl, ih, il;
       split_tf32_fast((uint32_t)__double2hiint(v.x), (uint32_t)__double2loint(v.x), rh, rl);
       split_tf32_fast((uint32_t)__double2hiint(v.y), (uint32_t)__double2loint(v.y), ih, il);
-      int64_t off = r * Kp + k;
+      const int64_t off = kblk ? ((k >> 4) * rows_pad + r) * 16 + (k & 15) : r * Kp + k;
       planes[off] = __uint_as_float(rh);
       planes[plane + off] = __uint_as_float(rl);
       planes[2 * plane + off] = __uint_as_float(ih);
@@ -598,6 +607,21 @@ __global__ void splitk_sum_kernel(const z64* __restrict__ partial, int splits, i
 int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() { return tma_encode_fn(); }
+
+// K-blocked planes [4][Kp/16][rows_pad][16] as a 3D tensor (16 k, rows_pad rows, 4 Kp/16 plane-k-blocks):
+// a box of 16 k x box_rows rows is one contiguous run.
+bool encode_planes_kblk(CUtensorMap* map, float* base, int64_t rows_pad, int64_t Kp, int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {16u, (cuuint64_t)rows_pad, (cuuint64_t)(4 * (Kp / 16))};
+  cuuint64_t strides[2] = {16u * sizeof(float), (cuuint64_t)rows_pad * 16u * sizeof(float)};
+  cuuint32_t box[3] = {16u, (cuuint32_t)box_rows, 1u};
+  cuuint32_t estr[3] = {1u, 1u, 1u};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
 
 bool encode_planes(CUtensorMap* map, float* base, int64_t rows_total, int64_t Kp, int box_rows, int kb) {
   auto enc = get_encode();
@@ -630,12 +654,14 @@ size_t tf32_planes_bytes(int64_t rows, int64_t K) {
 
 // Split an FP64 complex operand X(row,k) = src[row*s_row + k*s_k] into the four
 // zero-padded K-major TF32 planes the tensor-core kernel reads.
+// kblk: K-blocked layout [4][Kp/16][rows_pad][16] (for GEMMs whose K is long and whose rows,
+// Kp apart in the plain layout, would each cost the TMA a separate DRAM page per k-block).
 agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k, int conj,
-                            float* dst, cudaStream_t stream) {
+                            float* dst, cudaStream_t stream, int kblk) {
   int64_t rp = tf32_rows_pad(rows), kp = tf32_k_pad(K);
   int64_t tiles = (rp / 32) * ((kp + 31) / 32);
   int grid = (int)(tiles < 152 * 32 ? tiles : 152 * 32);
-  prep_kernel<<<grid, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, rp, kp, dst);
+  prep_kernel<<<grid, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, rp, kp, kblk, dst);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -668,9 +694,10 @@ size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K) {
 // C = alpha * A B^T + beta C on prepared planes (A: rows M, B: rows N, both K-major over K).
 // trans_c: C(m, n) lives at C[n * ldc + m] (the output written column by column, which keeps
 // the stores of an output with a short row extent coalesced).
+// kblkA / kblkB: that operand's planes are K-blocked (single-CTA kernel only).
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
                             z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
-                            int trans_c) {
+                            int trans_c, int kblkA, int kblkB) {
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
@@ -680,11 +707,13 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   int splits = partials ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
-  const bool pair = use_pair(M, N, splits) && !trans_c;
+  const bool pair = use_pair(M, N, splits) && !trans_c && !kblkA && !kblkB;
   const int nb = tile_n_for(N);
   CUtensorMap mA, mB;
-  if (!encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb) ||
-      !encode_planes(&mB, (float*)PB, 4 * Np, Kp, pair ? 128 : nb, kb)) {
+  const bool okA = kblkA ? encode_planes_kblk(&mA, (float*)PA, Mp, Kp, BM) : encode_planes(&mA, (float*)PA, 4 * Mp, Kp, BM, kb);
+  const bool okB = kblkB ? encode_planes_kblk(&mB, (float*)PB, Np, Kp, nb)
+                         : encode_planes(&mB, (float*)PB, 4 * Np, Kp, pair ? 128 : nb, kb);
+  if (!okA || !okB) {
     agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
@@ -703,7 +732,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   GemmParams p;
   p.M = M; p.N = N; p.nkb = nkb_split; p.nkb_total = (int)nkb;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = splits > 1 ? partials : nullptr; p.err = err;
-  p.rowsA = Mp; p.rowsB = Np; p.trans_c = trans_c;
+  p.rowsA = Mp; p.rowsB = Np; p.trans_c = trans_c; p.kblkA = kblkA; p.kblkB = kblkB;
   dim3 grid((unsigned)(round_up(N, nb) / nb), (unsigned)(round_up(M, BM) / BM), (unsigned)splits);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (g_timing.load(std::memory_order_relaxed)) {
@@ -758,11 +787,11 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
   char* base = (char*)scratch;
   float* PA = (float*)(base + 256);
   float* PB = (float*)(base + 256 + a_bytes);
-  AGB_STATUS_TRY(tf32_prep_planes(A, M, K, sAm, sAk, conjA, PA, stream));
-  AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream));
+  AGB_STATUS_TRY(tf32_prep_planes(A, M, K, sAm, sAk, conjA, PA, stream, 0));
+  AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream, 0));
   size_t used = 256 + a_bytes + b_bytes;
   return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + used),
-                          scratch_bytes - used, stream, 0);
+                          scratch_bytes - used, stream, 0, 0, 0);
 }
 
 }  // namespace agb
