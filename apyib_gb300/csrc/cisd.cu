@@ -299,6 +299,75 @@ __global__ void unpack_h_kernel(const z64* __restrict__ t2p, int o, int64_t pv, 
 }
 
 // t2q[p][a][b] = t2[(i<j)_p, a, b]
+// Offset of (row, k) in one TF32 plane: K-blocked [k/16][row][16] or plain [row][Kp].
+__device__ __forceinline__ int64_t plane_off(int64_t row, int64_t k, int64_t rows_pad, int64_t Kp, int kblk) {
+  return kblk ? ((k >> 4) * rows_pad + row) * 16 + (k & 15) : row * Kp + k;
+}
+// (row, k) of the plane element at offset e (the inverse of plane_off).
+__device__ __forceinline__ void plane_pos(int64_t e, int64_t rows_pad, int64_t Kp, int kblk, int64_t& row,
+                                          int64_t& k) {
+  if (kblk) {
+    const int64_t blk = e / (rows_pad * 16), rem = e % (rows_pad * 16);
+    row = rem >> 4;
+    k = blk * 16 + (rem & 15);
+  } else {
+    row = e / Kp;
+    k = e % Kp;
+  }
+}
+
+__device__ __forceinline__ void write_planes4(float* planes, int64_t plane, int64_t e, z64 val) {
+  uint32_t rh, rl, ih, il;
+  split_tf32_fast((uint32_t)__double2hiint(val.x), (uint32_t)__double2loint(val.x), rh, rl);
+  split_tf32_fast((uint32_t)__double2hiint(val.y), (uint32_t)__double2loint(val.y), ih, il);
+  planes[e] = __uint_as_float(rh);
+  planes[plane + e] = __uint_as_float(rl);
+  planes[2 * plane + e] = __uint_as_float(ih);
+  planes[3 * plane + e] = __uint_as_float(il);
+}
+
+// The TF32 planes of the singles GEMMs' amplitude operands straight from the packed
+// amplitudes (3xTF32 residuals with a diagonal Fock matrix, where no FP64 t2h / t2q is
+// needed): t2h as rows i, k = (j, p(ab)) -> t2[i,j,(a<b)]; t2q as rows a, k = (p(ij), b) ->
+// t2[i,j,b,a].  Threads run over plane offsets, so the writes are coalesced in either layout.
+__global__ void unpack_h_planes_kernel(const z64* __restrict__ t2p, int o, int64_t pv, int64_t rows_pad, int64_t Kp,
+                                       int kblk, float* __restrict__ planes) {
+  const int64_t plane = rows_pad * Kp, K = (int64_t)o * pv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < plane; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t row, k;
+    plane_pos(e, rows_pad, Kp, kblk, row, k);
+    z64 val = zmk(0, 0);
+    if (row < o && k < K) {
+      const int i = (int)row, j = (int)(k / pv);
+      const int s = sgn_pair(i, j);
+      if (s != 0) {
+        val = t2p[pair_index(min(i, j), max(i, j), o) * pv + k % pv];
+        if (s < 0) val = zneg(val);
+      }
+    }
+    write_planes4(planes, plane, e, val);
+  }
+}
+
+__global__ void unpack_q_planes_kernel(const z64* __restrict__ t2p, int64_t po, int v, int64_t pv, int64_t rows_pad,
+                                       int64_t Kp, int kblk, float* __restrict__ planes) {
+  const int64_t plane = rows_pad * Kp, K = po * v;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < plane; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t row, k;
+    plane_pos(e, rows_pad, Kp, kblk, row, k);
+    z64 val = zmk(0, 0);
+    if (row < v && k < K) {
+      const int a = (int)row, b = (int)(k % v);
+      const int s = sgn_pair(b, a);
+      if (s != 0) {
+        val = t2p[(k / v) * pv + pair_index(min(a, b), max(a, b), v)];
+        if (s < 0) val = zneg(val);
+      }
+    }
+    write_planes4(planes, plane, e, val);
+  }
+}
+
 __global__ void unpack_q_kernel(const z64* __restrict__ t2p, int64_t po, int v, int64_t pv, z64* __restrict__ out) {
   int64_t vv = (int64_t)v * v, total = po * vv;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
@@ -752,8 +821,9 @@ static void plan_layout(agb_cisd_plan* P, char* base, size_t* total) {
   P->X = (z64*)take(Z * ov * ov);
   P->PQ = (z64*)take(Z * po * pv);
   // t2h/t2q serve the singles terms and the non-diagonal Fock terms
-  P->t2h = (z64*)take(Z * o * o * pv);
-  P->t2q = (z64*)take(Z * po * v * v);
+  // (mixed plans: or the TF32 planes of the singles GEMMs' operands, written straight from t2p)
+  P->t2h = (z64*)take(P->mixed ? std::max(Z * o * o * pv, agb::tf32_planes_bytes(o, (int64_t)o * pv)) : Z * o * o * pv);
+  P->t2q = (z64*)take(P->mixed ? std::max(Z * po * v * v, agb::tf32_planes_bytes(v, po * v)) : Z * po * v * v);
   P->Gq = (z64*)take(Z * po * v * v);
   P->H2h = (z64*)take(Z * o * o * pv);
   P->R1x = (z64*)take(Z * ov);
@@ -1145,7 +1215,17 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     unpack_ring_kernel<<<grid_for(ov * ov, 256), 256, 0, st>>>(t2p, o, v, pv, P->Tring);
   }
   AGB_LAUNCH_CHECK();
-  if (need_hq) {
+  // 3xTF32 with a diagonal Fock matrix: t2h / t2q serve only the singles GEMMs, as planes
+  const bool hq_planes = ring_planes && P->singles && P->f_diag;
+  if (hq_planes) {
+    const int kb = singles_kblk(P);
+    const int64_t rh = tf32_rows_pad(o), kh = tf32_k_pad((int64_t)o * pv);
+    unpack_h_planes_kernel<<<grid_for(rh * kh, 256), 256, 0, st>>>(t2p, o, pv, rh, kh, kb, (float*)P->t2h);
+    AGB_LAUNCH_CHECK();
+    const int64_t rq = tf32_rows_pad(v), kq = tf32_k_pad(po * v);
+    unpack_q_planes_kernel<<<grid_for(rq * kq, 256), 256, 0, st>>>(t2p, po, v, pv, rq, kq, kb, (float*)P->t2q);
+    AGB_LAUNCH_CHECK();
+  } else if (need_hq) {
     unpack_h_kernel<<<grid_for((int64_t)o * o * pv, 256), 256, 0, st>>>(t2p, o, pv, P->t2h);
     AGB_LAUNCH_CHECK();
     unpack_q_kernel<<<grid_for(po * v * v, 256), 256, 0, st>>>(t2p, po, v, pv, P->t2q);
@@ -1174,10 +1254,11 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     // r1[i][a] += sum_(j,p(cb)) <aj||cb> t2h[i][j][p(cb)]
     const int kb = singles_kblk(P);
     AGB_STATUS_TRY(gemm(P, prec, v, o, (int64_t)o * pv, one, P->WvovvH, (int64_t)o * pv, 1, P->t2h, 1,
-                        (int64_t)o * pv, one, r1, v, st, P->P_Wvovv, nullptr, 1, kb));
+                        (int64_t)o * pv, one, r1, v, st, P->P_Wvovv, hq_planes ? (const float*)P->t2h : nullptr, 1,
+                        kb));
     // r1[i][a] += sum_(p(kj),b) <kj||ib> t2q[p(kj)][b][a]
-    AGB_STATUS_TRY(gemm(P, prec, v, o, po * v, one, P->t2q, 1, v, P->WooovP, 1, po * v, one, r1, v, st, nullptr,
-                        P->P_Wooov, 1, kb));
+    AGB_STATUS_TRY(gemm(P, prec, v, o, po * v, one, P->t2q, 1, v, P->WooovP, 1, po * v, one, r1, v, st,
+                        hq_planes ? (const float*)P->t2q : nullptr, P->P_Wooov, 1, kb));
     if (flags & AGB_RES_ETERM) {
       axpy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(n1, zneg(E), t1, r1);
       AGB_LAUNCH_CHECK();
