@@ -52,7 +52,7 @@ agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_r
                             float* dst, cudaStream_t stream, int kblk);
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
                             z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
-                            int trans_c, int kblkA, int kblkB);
+                            int trans_c, int kblkA, int kblkB, int c32);
 
 namespace {
 
@@ -408,6 +408,7 @@ struct AsmArgs {
   int64_t ov, po, pv;
   const int2* opairs;
   const z64 *R0p, *PQ, *X, *Zq, *Yh, *Gq, *H2h, *t2p;
+  int out32;             // PQ, X, Zq, Yh hold complex FP32 (3xTF32 residuals)
   const double* eps;     // SO energies (for the diagonal-Fock fast path)
   const z64 *Foo, *Fvv;  // diagonal-Fock fast path reads F[p,p]
   z64 E;
@@ -446,6 +447,18 @@ __device__ __forceinline__ float2 vneg(float2 a) { return make_float2(-a.x, -a.y
 __device__ __forceinline__ float2 vmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+// Element idx of a GEMM product array stored in complex FP32 (f32) or FP64.
+template <typename T> __device__ __forceinline__ T ldo(const z64* base, int64_t idx, int f32);
+template <> __device__ __forceinline__ float2 ldo<float2>(const z64* base, int64_t idx, int f32) {
+  return f32 ? ((const float2*)base)[idx] : ldz<float2>(base + idx);
+}
+template <> __device__ __forceinline__ z64 ldo<z64>(const z64* base, int64_t idx, int f32) {
+  if (f32) {
+    const float2 v = ((const float2*)base)[idx];
+    return zmk(f2d_exact(v.x), f2d_exact(v.y));
+  }
+  return base[idx];
+}
 template <typename T> __device__ __forceinline__ T zzero();
 template <> __device__ __forceinline__ z64 zzero<z64>() { return zmk(0, 0); }
 template <> __device__ __forceinline__ float2 zzero<float2>() { return make_float2(0.f, 0.f); }
@@ -474,9 +487,9 @@ __global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
     T s = zzero<T>();
     if (a < v && b < v) {
       // -X[(i,b),(j,a)] + X[(j,b),(i,a)]
-      s = vneg(ldz<T>(A.X + ((int64_t)i * v + b) * A.ov + (int64_t)j * v + a));
-      s = vadd(s, ldz<T>(A.X + ((int64_t)j * v + b) * A.ov + (int64_t)i * v + a));
-      if (A.singles) s = vsub(s, ldz<T>(A.Zq + p * vv + (int64_t)b * v + a));      // -Zq[p][b][a]
+      s = vneg(ldo<T>(A.X, ((int64_t)i * v + b) * A.ov + (int64_t)j * v + a, A.out32));
+      s = vadd(s, ldo<T>(A.X, ((int64_t)j * v + b) * A.ov + (int64_t)i * v + a, A.out32));
+      if (A.singles) s = vsub(s, ldo<T>(A.Zq, p * vv + (int64_t)b * v + a, A.out32));      // -Zq[p][b][a]
       if (!A.f_diag) s = vsub(s, ldz<T>(A.Gq + p * vv + (int64_t)b * v + a));      // -Gq[p][b][a]
     }
     tr[rb][tx] = s;
@@ -489,13 +502,13 @@ __global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
     int64_t q = pair_index(a, b, v);
     int64_t pq = p * A.pv + q;
     T s = tr[tx][ra];
-    s = vadd(s, ldz<T>(A.PQ + pq));
-    s = vadd(s, ldz<T>(A.X + ((int64_t)i * v + a) * A.ov + (int64_t)j * v + b));
-    s = vsub(s, ldz<T>(A.X + ((int64_t)j * v + a) * A.ov + (int64_t)i * v + b));
+    s = vadd(s, ldo<T>(A.PQ, pq, A.out32));
+    s = vadd(s, ldo<T>(A.X, ((int64_t)i * v + a) * A.ov + (int64_t)j * v + b, A.out32));
+    s = vsub(s, ldo<T>(A.X, ((int64_t)j * v + a) * A.ov + (int64_t)i * v + b, A.out32));
     if (A.singles) {
-      s = vadd(s, ldz<T>(A.Zq + p * vv + (int64_t)a * v + b));
-      s = vadd(s, ldz<T>(A.Yh + ((int64_t)i * A.o + j) * A.pv + q));
-      s = vsub(s, ldz<T>(A.Yh + ((int64_t)j * A.o + i) * A.pv + q));
+      s = vadd(s, ldo<T>(A.Zq, p * vv + (int64_t)a * v + b, A.out32));
+      s = vadd(s, ldo<T>(A.Yh, ((int64_t)i * A.o + j) * A.pv + q, A.out32));
+      s = vsub(s, ldo<T>(A.Yh, ((int64_t)j * A.o + i) * A.pv + q, A.out32));
     }
     T t = ldz<T>(A.t2p + pq);
     if (A.f_diag) {
@@ -717,8 +730,9 @@ __device__ __forceinline__ void df_diff(float ah, float al, float bh, float bl, 
 // s2 = 4 sum_{t2} (t_old - t_new)^2 (apyib/utils.py:138, ci_wfn.py:355,361-365).
 // t_new = (sum_j c_j) y_0 + sum_{j>0} c_j (y_j - y_0): the first product in FP64 (so a
 // copy, ny = 1 with c = 1, is exact), the differences, the small sum, the energy and the
-// squared norms in double-float on the FP32 pipe (~2^-46 of |y_j| per element), which
-// leaves ~8 FP64 operations per element (GB300's FP64 pipe bounded the FP64 version).
+// squared norms (old - t_new taken in double-float) in double-float on the FP32 pipe
+// (~2^-46 of |y_j| per element), which leaves 4 FP64 operations per element (GB300's FP64
+// pipe bounded the FP64 version).
 // t_old / t_new and any y_j may alias: each element is read before it is written.
 __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) {
   __shared__ float4 cs[kMaxVec];
@@ -734,10 +748,10 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) 
     const int64_t hi = part ? n : A.n1;
     for (int64_t k = stride_start(k0, stride, part ? A.n1 : 0); k < hi; k += stride) {
       const z64 y0 = A.ys[0][k];
-      z64 t = csum_real ? zmk(A.csum.x * y0.x, A.csum.x * y0.y) : zmul(A.csum, y0);
+      z64 t = zmk(0, 0);
+      float dr = 0.f, drc = 0.f, di = 0.f, dic = 0.f;
       if (A.ny > 1) {
         const float4 y0s = split_z_fast(y0);
-        float dr = 0.f, drc = 0.f, di = 0.f, dic = 0.f;
         for (int j = 1; j < A.ny; ++j) {
           const float4 yj = split_z_fast(A.ys[j][k]);
           float4 d;
@@ -750,6 +764,13 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) 
           df_mac(di, dic, c.x, c.y, d.z, d.w);
           df_mac(di, dic, c.z, c.w, d.x, d.y);
         }
+      }
+      // t = (sum c) y0 + the double-float sum: one FMA and one add per part on the FP64 pipe
+      if (csum_real) {
+        t.x = fma(A.csum.x, y0.x, f2d_exact(dr)) + f2d_exact(drc);
+        t.y = fma(A.csum.x, y0.y, f2d_exact(di)) + f2d_exact(dic);
+      } else {
+        t = zmul(A.csum, y0);
         t.x += df_to_double(dr, drc);
         t.y += df_to_double(di, dic);
       }
@@ -763,7 +784,11 @@ __global__ void __launch_bounds__(256) combine_kernel(CombArgs A, z64* partial) 
       df_mac(er, erc, -ts.z, -ts.w, ws.z, ws.w);
       df_mac(ei, eic, ts.x, ts.y, ws.z, ws.w);
       df_mac(ei, eic, ts.z, ts.w, ws.x, ws.y);
-      const float4 e = split_z_fast(zsub(old, t));
+      // old - t in double-float from the float pairs (absolute error ~2^-46 |t|; no FP64 subtract)
+      const float4 os = split_z_fast(old);
+      float4 e;
+      df_diff(os.x, os.y, ts.x, ts.y, e.x, e.y);
+      df_diff(os.z, os.w, ts.z, ts.w, e.z, e.w);
       // (old - t)^2, unconjugated
       df_mac(q[0], q[1], e.x, e.y, e.x, e.y);
       df_mac(q[0], q[1], -e.z, -e.w, e.z, e.w);
@@ -907,13 +932,15 @@ namespace {
 // trans_c: C(m, n) lives at C[n * ldc + m]; the 3xTF32 kernel stores it so, the other
 // backends compute the same product as C^T = B^T A^T.  kblk: both operands' planes are
 // K-blocked (static ones prepared so at set-up; the singles GEMMs, whose operands are up to
-// 1.7M elements long in K).
+// 1.7M elements long in K).  c32 (3xTF32 only): C holds complex FP32 values (the
+// products only the assembly reads, which works at FP32 level in 3xTF32 residuals).
 agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm,
                 int64_t sAk, const z64* B, int64_t sBk, int64_t sBn, z64 beta, z64* C, int64_t ldc,
                 cudaStream_t st, const float* PA = nullptr, const float* PB = nullptr, int trans_c = 0,
-                int kblk = 0) {
+                int kblk = 0, int c32 = 0) {
   if (prec == AGB_PREC_TF32X3) {
     if (M == 0 || N == 0) return AGB_OK;
+    AGB_ARG_CHECK(!(c32 && K == 0), "residual: empty contraction into an FP32 product");
     if (K == 0) return zgemm_ex(M, N, 0, zmk(0, 0), A, sAm, sAk, 0, B, sBk, sBn, 0, beta, C, ldc, nullptr, 0, st);
     char* base = (char*)P->gemm_scratch;
     size_t off = 256;
@@ -932,7 +959,7 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
       return AGB_ERR_WORKSPACE;
     }
     return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
-                            P->gemm_scratch_bytes - off, st, trans_c, kblk, kblk);
+                            P->gemm_scratch_bytes - off, st, trans_c, kblk, kblk, c32);
   }
   if (trans_c) return gemm(P, prec, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, ldc, st);
   if (prec == AGB_PREC_OZAKI && ozgemm_tiles(M, N) >= kOzMinTiles)
@@ -1203,8 +1230,10 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
   const z64 E = zmk(E_re, E_im);
   const bool need_hq = P->singles || !P->f_diag;
 
-  // 3xTF32 residuals take the ring operand as TF32 planes written straight from t2p
+  // 3xTF32 residuals take the ring operand as TF32 planes written straight from t2p, and keep
+  // the products that only the assembly reads (X, PQ, Zq, Yh) in complex FP32
   const bool ring_planes = prec == AGB_PREC_TF32X3;
+  const int out32 = ring_planes ? 1 : 0;
   if (ring_planes) {
     const int64_t rp = tf32_rows_pad(ov), kp = tf32_k_pad(ov);
     // one warp per plane row; with singles it also forms the F_jb t2_ijab term into R1x
@@ -1265,16 +1294,18 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     }
     // Zq[p(ij)][b][a] = sum_k <kb||ij> t1[k,a];  Yh[i][j][p(ab)] = sum_c t1[i,c] <ab||cj>
     AGB_STATUS_TRY(gemm(P, prec, v, po * v, o, one, t1, 1, v, P->WovooP, 1, o, zero, P->Zq, v, st, nullptr,
-                        P->P_Wovoo, 1, kb));
+                        P->P_Wovoo, 1, kb, out32));
     AGB_STATUS_TRY(gemm(P, prec, (int64_t)o * pv, o, v, one, P->WvvvoP, 1, (int64_t)o * pv, t1, 1, v, zero, P->Yh,
-                        (int64_t)o * pv, st, P->P_Wvvvo, nullptr, 1, kb));
+                        (int64_t)o * pv, st, P->P_Wvvvo, nullptr, 1, kb, out32));
   }
   // ladders: PQ = sum_{k<l} <kl||ij> t2p[kl,ab] + sum_{c<d} t2p[ij,cd] <ab||cd>
-  AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st, P->P_Woooo));
-  AGB_STATUS_TRY(gemm(P, prec, po, pv, pv, one, t2p, pv, 1, P->Wvp, 1, pv, one, P->PQ, pv, st, nullptr, P->P_Wvp));
+  AGB_STATUS_TRY(gemm(P, prec, po, pv, po, one, P->WooooT, po, 1, t2p, pv, 1, zero, P->PQ, pv, st, P->P_Woooo,
+                      nullptr, 0, 0, out32));
+  AGB_STATUS_TRY(gemm(P, prec, po, pv, pv, one, t2p, pv, 1, P->Wvp, 1, pv, one, P->PQ, pv, st, nullptr, P->P_Wvp, 0,
+                      0, out32));
   // rings: X[(i,a),(j,b)] = sum_(k,c) t2[i,k,a,c] <kb||cj>
   AGB_STATUS_TRY(gemm(P, prec, ov, ov, ov, one, P->Tring, ov, 1, P->VT, 1, ov, zero, P->X, ov, st,
-                      ring_planes ? (const float*)P->Tring : nullptr, P->P_VT));
+                      ring_planes ? (const float*)P->Tring : nullptr, P->P_VT, 0, 0, out32));
   if (!P->f_diag) {
     AGB_STATUS_TRY(gemm(P, prec, po * v, v, v, one, P->t2q, v, 1, P->Fvv, 1, v, zero, P->Gq, v, st));
     AGB_STATUS_TRY(gemm(P, prec, o, (int64_t)o * pv, o, one, P->Foo, 1, o, P->t2h, (int64_t)o * pv, 1, zero, P->H2h,
@@ -1284,6 +1315,7 @@ agb_status agb_cisd_residual(agb_cisd_plan* P, int prec, const void* tv, double 
     AsmArgs A;
     A.o = o; A.v = v; A.ov = ov; A.po = po; A.pv = pv; A.opairs = P->opairs;
     A.R0p = P->R0p; A.PQ = P->PQ; A.X = P->X; A.Zq = P->Zq; A.Yh = P->Yh; A.Gq = P->Gq; A.H2h = P->H2h;
+    A.out32 = out32;
     A.t2p = t2p; A.eps = P->eps; A.Foo = P->Foo; A.Fvv = P->Fvv; A.E = E;
     A.use_const = (flags & AGB_RES_CONST) != 0; A.use_e = (flags & AGB_RES_ETERM) != 0;
     A.singles = P->singles; A.f_diag = P->f_diag; A.r2p = r2p;

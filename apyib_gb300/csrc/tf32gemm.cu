@@ -121,6 +121,7 @@ struct GemmParams {
   int64_t rowsA, rowsB;  // padded rows per plane
   int trans_c;           // store C(m, n) at C[n * ldc + m] instead of C[m * ldc + n]
   int kblkA, kblkB;      // operand planes K-blocked ([k/16][row][16] per plane), read through 3D maps
+  int c32;               // C holds complex FP32 (float2) values: C = AB (+ C when beta = 1)
 };
 
 template <int NB>
@@ -278,6 +279,21 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
 #pragma unroll
             for (int j = 0; j < 32; ++j)
               if (n0 + j < p.N) dst[j] = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
+          } else if (p.c32) {
+            const int64_t sj = p.trans_c ? p.ldc : 1;
+            float2* dst = (float2*)p.C + (p.trans_c ? n0 * p.ldc + m : m * p.ldc + n0);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (n0 + j < p.N) {
+                float2 out = make_float2(vr[j], vi[j]);
+                if (unit_beta) {
+                  const float2 c = dst[j * sj];
+                  out.x += c.x;
+                  out.y += c.y;
+                }
+                dst[j * sj] = out;
+              }
+            }
           } else {
             // row-major C: a thread writes its row's 32 columns; transposed C: for each column
             // the warp's 32 rows are consecutive addresses
@@ -516,6 +532,20 @@ tf32x3_gemm2_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_const
 #pragma unroll
             for (int j = 0; j < 32; ++j)
               if (n0 + j < p.N) dst[j] = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
+          } else if (p.c32) {
+            float2* dst = (float2*)p.C + m * p.ldc + n0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (n0 + j < p.N) {
+                float2 out = make_float2(vr[j], vi[j]);
+                if (unit_beta) {
+                  const float2 c = dst[j];
+                  out.x += c.x;
+                  out.y += c.y;
+                }
+                dst[j] = out;
+              }
+            }
           } else {
             z64* dst = p.C + m * p.ldc + n0;
 #pragma unroll
@@ -694,17 +724,20 @@ size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K) {
 // C = alpha * A B^T + beta C on prepared planes (A: rows M, B: rows N, both K-major over K).
 // trans_c: C(m, n) lives at C[n * ldc + m] (the output written column by column, which keeps
 // the stores of an output with a short row extent coalesced).
-// kblkA / kblkB: that operand's planes are K-blocked (single-CTA kernel only).
+// kblkA / kblkB: that operand's planes are K-blocked (single-CTA kernel only).  c32: C holds
+// complex FP32 values (ldc in float2 units), alpha = 1, beta 0 or 1, no K split.
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
                             z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
-                            int trans_c, int kblkA, int kblkB) {
+                            int trans_c, int kblkA, int kblkB, int c32) {
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
   constexpr int kb = 16;
   const int64_t Mp = tf32_rows_pad(M), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K), nkb = Kp / kb;
   AGB_ARG_CHECK(Mp / BM <= 65535, "tf32_gemm_planes: grid too large");
-  int splits = partials ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
+  AGB_ARG_CHECK(!c32 || (alpha.x == 1.0 && alpha.y == 0.0 && beta.y == 0.0 && (beta.x == 0.0 || beta.x == 1.0)),
+                "tf32_gemm_planes: an FP32 output takes alpha = 1 and beta = 0 or 1");
+  int splits = (partials && !c32) ? choose_splits(M, N, Kp / BK, partial_bytes) : 1;
   int nkb_split = (int)((nkb + splits - 1) / splits);
   splits = (int)((nkb + nkb_split - 1) / nkb_split);
   const bool pair = use_pair(M, N, splits) && !trans_c && !kblkA && !kblkB;
@@ -732,7 +765,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   GemmParams p;
   p.M = M; p.N = N; p.nkb = nkb_split; p.nkb_total = (int)nkb;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = splits > 1 ? partials : nullptr; p.err = err;
-  p.rowsA = Mp; p.rowsB = Np; p.trans_c = trans_c; p.kblkA = kblkA; p.kblkB = kblkB;
+  p.rowsA = Mp; p.rowsB = Np; p.trans_c = trans_c; p.kblkA = kblkA; p.kblkB = kblkB; p.c32 = c32;
   dim3 grid((unsigned)(round_up(N, nb) / nb), (unsigned)(round_up(M, BM) / BM), (unsigned)splits);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (g_timing.load(std::memory_order_relaxed)) {
@@ -791,7 +824,7 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
   AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream, 0));
   size_t used = 256 + a_bytes + b_bytes;
   return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + used),
-                          scratch_bytes - used, stream, 0, 0, 0);
+                          scratch_bytes - used, stream, 0, 0, 0, 0);
 }
 
 }  // namespace agb
