@@ -270,7 +270,8 @@ agb_status agb_cisd_guess(agb_cisd_plan* plan, void* t, void* stream);
 /* ------------------------------------------------------------------- MP2 -- */
 
 /* MP2_SO from a built plan: t2p = <ab||ij>/D, E = sum_p <ij||ab>_p t2p
- * (apyib/mp2_wfn.py:82-85); t receives the packed vector (t1 part zero). */
+ * (apyib/mp2_wfn.py:82-85); t receives the packed vector (t1 part zero).
+ * partials: device scratch of at least agb_vec_partials_bytes(1) bytes. */
 agb_status agb_mp2_so(agb_cisd_plan* plan, void* t, void* E_out, void* partials, size_t partials_bytes,
                       void* stream);
 
