@@ -241,18 +241,26 @@ __global__ void unpack_ring_planes_kernel(const z64* __restrict__ t2p, int o, in
     const bool live = row < ov;
     const int i = live ? (int)(row / v) : 0, a = live ? (int)(row % v) : 0;
     float re = 0.f, im = 0.f;
+    // (k, c) of col, advanced by 32 per pass without divisions; pair offsets in 32-bit
+    // (o, v < 2^15 keeps p(ab) and p(ik) below 2^31)
+    int k = v > 0 ? lane / v : 0, c = v > 0 ? lane % v : 0;
     for (int64_t col = lane; col < Kp; col += 32) {
       z64 val = zmk(0, 0);
       const bool in = live && col < ov;
-      int k = 0, c = 0;
       if (in) {
-        k = (int)(col / v);
-        c = (int)(col % v);
         const int sg = sgn_pair(i, k) * sgn_pair(a, c);
         if (sg != 0) {
-          val = t2p[pair_index(min(i, k), max(i, k), o) * pv + pair_index(min(a, c), max(a, c), v)];
+          const int lo = min(i, k), hi = max(i, k), la = min(a, c), ha = max(a, c);
+          const int pik = lo * o - lo * (lo + 1) / 2 + (hi - lo - 1);
+          const int pac = la * v - la * (la + 1) / 2 + (ha - la - 1);
+          val = t2p[(int64_t)pik * pv + pac];
           if (sg < 0) val = zneg(val);
         }
+      }
+      c += 32;
+      while (v > 0 && c >= v) {
+        c -= v;
+        ++k;
       }
       uint32_t rh, rl, ih, il;
       split_tf32_fast((uint32_t)__double2hiint(val.x), (uint32_t)__double2loint(val.x), rh, rl);
@@ -427,9 +435,11 @@ __device__ __forceinline__ float f64_to_f32(double x) {
   return __fadd_rn(h, l);
 }
 template <typename T> __device__ __forceinline__ T ldz(const z64* p);
-template <> __device__ __forceinline__ z64 ldz<z64>(const z64* p) { return *p; }
+// (read-only loads: the assembly's inputs are never written while it runs, which lets the
+// compiler issue a thread's loads ahead of its stores)
+template <> __device__ __forceinline__ z64 ldz<z64>(const z64* p) { return __ldg(p); }
 template <> __device__ __forceinline__ float2 ldz<float2>(const z64* p) {
-  const z64 v = *p;
+  const z64 v = __ldg(p);
   return make_float2(f64_to_f32(v.x), f64_to_f32(v.y));
 }
 template <typename T> __device__ __forceinline__ T cz(z64 v);
@@ -450,11 +460,11 @@ __device__ __forceinline__ float2 vmul(float2 a, float2 b) {
 // Element idx of a GEMM product array stored in complex FP32 (f32) or FP64.
 template <typename T> __device__ __forceinline__ T ldo(const z64* base, int64_t idx, int f32);
 template <> __device__ __forceinline__ float2 ldo<float2>(const z64* base, int64_t idx, int f32) {
-  return f32 ? ((const float2*)base)[idx] : ldz<float2>(base + idx);
+  return f32 ? __ldg((const float2*)base + idx) : ldz<float2>(base + idx);
 }
 template <> __device__ __forceinline__ z64 ldo<z64>(const z64* base, int64_t idx, int f32) {
   if (f32) {
-    const float2 v = ((const float2*)base)[idx];
+    const float2 v = __ldg((const float2*)base + idx);
     return zmk(f2d_exact(v.x), f2d_exact(v.y));
   }
   return base[idx];
@@ -466,8 +476,10 @@ template <> __device__ __forceinline__ float2 zzero<float2>() { return make_floa
 // One CTA per (pair p(ij), upper-triangle tile of (a,b)).  Terms whose source
 // is indexed [b][a] are summed first along a (coalesced) into shared memory
 // and read transposed; the rest are read along b.
+// Four blocks per SM (at most 64 registers): the kernel is bound by load latency (ncu at
+// 40/160: long-scoreboard stalls first, 25 % of DRAM bandwidth at 3 blocks per SM).
 template <typename T>
-__global__ void __launch_bounds__(256) assemble_r2_kernel(AsmArgs A) {
+__global__ void __launch_bounds__(256, 4) assemble_r2_kernel(AsmArgs A) {
   __shared__ T tr[TS][TS + 1];
   const int ntile = (A.v + TS - 1) / TS;
   // decode tile pair (ta <= tb) from blockIdx.x
