@@ -620,13 +620,23 @@ __device__ __forceinline__ void block_reduce_store(z64 (&acc)[NV], z64* out) {
   }
 }
 
-// out[k] = sum over blocks of partial[b*nv + k] for k < count <= nv, fixed order (deterministic)
-__global__ void finish_partials_kernel(const z64* __restrict__ partial, int nblocks, int nv, int count, z64* out) {
-  int k = threadIdx.x;
+// out[k] = sum over blocks of partial[b*nv + k], one 256-thread block per slot k < count <= nv:
+// thread t sums blocks t, t + 256, ... in order, then a fixed tree (deterministic; a single
+// thread's dependent chain of nblocks loads made this tail ~90 us).
+__global__ void __launch_bounds__(256) finish_partials_kernel(const z64* __restrict__ partial, int nblocks, int nv,
+                                                              int count, z64* out) {
+  __shared__ z64 sh[256];
+  const int k = blockIdx.x, t = threadIdx.x;
   if (k >= count || k >= nv) return;
   z64 s = zmk(0, 0);
-  for (int b = 0; b < nblocks; ++b) s = zadd(s, partial[(int64_t)b * nv + k]);
-  out[k] = s;
+  for (int b = t; b < nblocks; b += 256) s = zadd(s, partial[(int64_t)b * nv + k]);
+  sh[t] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) sh[t] = zadd(sh[t], sh[t + w]);
+    __syncthreads();
+  }
+  if (t == 0) out[k] = sh[0];
 }
 
 constexpr int kRedBlocks = 152 * 4;
@@ -1386,7 +1396,7 @@ agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void
   const int nv = launch_dots(A, ny, part, st);
   AGB_LAUNCH_CHECK();
   // finish only the first ny of the nv slots (stride nv)
-  finish_partials_kernel<<<1, 32, 0, st>>>(part, kDotBlocks, nv, ny, (z64*)out);
+  finish_partials_kernel<<<ny, 256, 0, st>>>(part, kDotBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -1479,7 +1489,7 @@ agb_status agb_vec_dots_noalloc(int64_t n1, int64_t n2, double w1, double w2, co
   z64* part = (z64*)scratch;
   const int nv = launch_dots(A, ny, part, st);
   AGB_LAUNCH_CHECK();
-  finish_partials_kernel<<<1, 32, 0, st>>>(part, kDotBlocks, nv, ny, (z64*)out);
+  finish_partials_kernel<<<ny, 256, 0, st>>>(part, kDotBlocks, nv, ny, (z64*)out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -1505,7 +1515,7 @@ agb_status agb_cisd_combine(agb_cisd_plan* P, const void* const* ys, const doubl
   A.t_old = (const z64*)t_old; A.t_new = (z64*)t_new; A.ew = P->EW;
   combine_kernel<<<kRedBlocks, 256, 0, st>>>(A, (z64*)partials);
   AGB_LAUNCH_CHECK();
-  finish_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kRedBlocks, 3, 3, (z64*)out3);
+  finish_partials_kernel<<<3, 256, 0, st>>>((const z64*)partials, kRedBlocks, 3, 3, (z64*)out3);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }

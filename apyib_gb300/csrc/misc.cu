@@ -124,12 +124,20 @@ __global__ void __launch_bounds__(256) mp2_kernel(const z64* __restrict__ R0p, c
   }
 }
 
-__global__ void sum_partials_kernel(const z64* __restrict__ partial, int n, z64* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    z64 s = zmk(0, 0);
-    for (int b = 0; b < n; ++b) s = zadd(s, partial[b]);
-    *out = s;
+// *out = sum of partial[0 .. n), one 256-thread block: strided sums in order, then a fixed
+// tree (deterministic).
+__global__ void __launch_bounds__(256) sum_partials_kernel(const z64* __restrict__ partial, int n, z64* out) {
+  __shared__ z64 sh[256];
+  const int t = threadIdx.x;
+  z64 s = zmk(0, 0);
+  for (int b = t; b < n; b += 256) s = zadd(s, partial[b]);
+  sh[t] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) sh[t] = zadd(sh[t], sh[t + w]);
+    __syncthreads();
   }
+  if (t == 0) *out = sh[0];
 }
 
 // ---- real FP64 GEMM (first AO->MO quarter step: real ERIs x interleaved complex C)
@@ -626,7 +634,7 @@ agb_status agb_mp2_so(agb_cisd_plan* P, void* t, void* E_out, void* partials, si
   mp2_kernel<<<kMp2Blocks, 256, 0, st>>>(P->R0p, P->EW + P->n1, P->invD + P->n1, P->n2,
                                          (z64*)t + P->n1, (z64*)partials);
   AGB_LAUNCH_CHECK();
-  sum_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);
+  sum_partials_kernel<<<1, 256, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
@@ -837,7 +845,7 @@ extern "C" agb_status agb_mp2_spatial(const void* ERI_MO, int64_t nmo, int64_t n
   mp2_spatial_kernel<<<kMp2Blocks, 256, 0, st>>>((const z64*)ERI_MO, nmo, (int)no, (int)(nmo - no), eps, (z64*)t2,
                                                  (z64*)partials);
   AGB_LAUNCH_CHECK();
-  sum_partials_kernel<<<1, 32, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);
+  sum_partials_kernel<<<1, 256, 0, st>>>((const z64*)partials, kMp2Blocks, (z64*)E_out);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }
