@@ -12,6 +12,9 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
                         int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                         void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t cgemm_tf32x3_scratch(int64_t M, int64_t N, int64_t K);
+agb_status cgemm_tf32x3_fa(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk,
+                           int conjA, const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C,
+                           int64_t ldc, void* scratch, size_t scratch_bytes, cudaStream_t stream);
 agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
                      const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
@@ -689,9 +692,14 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
   AGB_LAUNCH_CHECK();
   // out[(rest)][q] = sum_k T[k][(rest)] Cop[k][q]
   auto step = [&](const z64* T, int64_t Mrest, int kind, const z64* Cop, z64* out) -> agb_status {
-    if (precision == AGB_PREC_TF32X3)
+    if (precision == AGB_PREC_TF32X3) {
+      // outputs up to 256 wide: the GEMM converts the FP64 intermediate itself (no operand planes)
+      if (nmo <= 256)
+        return cgemm_tf32x3_fa(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo,
+                               gs, gs_bytes, st);
       return cgemm_tf32x3(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
                           gs_bytes, st);
+    }
     if (precision == AGB_PREC_DF64)
       return dfgemm_ex(Mrest, nmo, nbf, zmk(1, 0), T, 1, Mrest, kind, Cop, nmo, 1, 0, zmk(0, 0), out, nmo, gs,
                        gs_bytes, st);

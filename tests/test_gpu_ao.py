@@ -109,3 +109,33 @@ def test_transform_precision_modes(prec, tol):
     ERI_MO = utils.compute_ERI_MO(p, wfn, C_list, precision=prec)
     scale = np.abs(g["ERI_MO"]).max()
     np.testing.assert_allclose(ERI_MO, g["ERI_MO"], atol=tol * scale)
+
+
+@pytest.mark.parametrize("n", [40, 70])
+def test_transform_tf32x3_matches_fp64_multi_tile(n):
+    """The 3xTF32 transform (the GEMMs convert the FP64 intermediate in their own
+    converter warps; nmo = 40 takes the 64-wide tile, 70 the 160-wide one, thousands of
+    128-row tiles) against the FP64 transform of the same seeded AO integrals.  Bound:
+    each quarter step carries ~2^-21 of sum |a||b| (~sqrt(n) times its result for a
+    unitary C), four steps chained: 1e-5 of the largest element."""
+    import ctypes
+
+    from apyib_gb300.device import ptr, stream_ptr, workspace
+    g = torch.Generator(device="cpu").manual_seed(n)
+    A = torch.randn(2 * n, n, n, generator=g, dtype=torch.float64)
+    A = ((A + A.transpose(1, 2)) / (2 * (2 * n * n) ** 0.5)).cuda()
+    eri = torch.einsum("Lmn,Lls->mnls", A, A).contiguous()
+    Cm = torch.linalg.qr(torch.randn(n, n, generator=g, dtype=torch.complex128))[0].cuda().contiguous()
+    out = {}
+    for prec in (_lib.PREC_FP64, _lib.PREC_TF32X3):
+        o = torch.empty(n, n, n, n, dtype=torch.complex128, device="cuda")
+        nb = _lib.load().agb_ao2mo_scratch_bytes(n, n, prec)
+        buf, sp, _ = workspace(nb)
+        _lib.call("agb_ao2mo", ptr(eri), n, ptr(Cm), n, ptr(o), ctypes.c_void_p(sp), ctypes.c_size_t(nb), prec,
+                  stream_ptr())
+        torch.cuda.synchronize()
+        out[prec] = o
+        del buf
+    scale = out[_lib.PREC_FP64].abs().max().item()
+    err = (out[_lib.PREC_TF32X3] - out[_lib.PREC_FP64]).abs().max().item() / scale
+    assert err < 1e-5, err
