@@ -55,11 +55,12 @@ def tf32_gemm(A, B, alpha=1.0, beta=0.0, C=None, transB=False):
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 16), (1, 1, 1), (200, 300, 77), (60, 240, 6000), (513, 129, 1000),
                                    (2000, 60, 240), (240, 60, 60000), (300, 64, 500), (100, 65, 100), (33, 17, 100),
-                                   (64, 64, 64)])
+                                   (64, 64, 64), (1100, 1030, 500), (1024, 2049, 64)])
 def test_tf32x3_gemm_accuracy(M, N, K):
     """3xTF32 complex GEMM: error ~1e-6 relative to sum|a||b| (FP32-level).  N <= 64 takes
     the 64-wide tile (split over K for (240, 60, 60000)); M <= 64 an A operand whose
-    64-row planes the 128-row tile reads past."""
+    64-row planes the 128-row tile reads past; both extents >= 1024 the CTA-pair kernel
+    (ragged pair tiles in (1100, 1030, 500))."""
     rng = np.random.default_rng(M + N + K)
     A = crandn(rng, M, K)
     B = crandn(rng, K, N)
