@@ -391,7 +391,10 @@ __device__ __forceinline__ uint16_t oz_digit_bf16(long long d, float scale) {
 // Slices [OZ_S][rows_pad][Kp] (bf16, K-major, zero padded) and row scale exponents f_r of
 // NP parts from one read of the source: part q's slices start at slices + q * OZ_S * rows_pad * Kp,
 // its exponents at emax / fexp + q * estride (estride 0: one exponent shared by the parts).
-template <int NP>
+// KBLK: each slice plane is laid out [Kp / 16][rows_pad][16] instead, the two 16-byte halves
+// of a row's 32 bytes swapped on rows r with (r >> 2) & 1 (the MMA's 32-byte swizzle), so a
+// block of rows of one 16-k block is one contiguous, ready-to-use run of shared memory.
+template <int NP, bool KBLK = false>
 __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
                                 int conj, int part0, int64_t rows_pad, int64_t Kp, int64_t estride,
                                 const int* __restrict__ emax, int* __restrict__ fexp, uint16_t* __restrict__ slices) {
@@ -436,7 +439,9 @@ __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64
           X -= d[s] << sh;
         }
         d[OZ_S - 1] = X;
-        uint16_t* dst = slices + (int64_t)q * OZ_S * plane + r * Kp + k;
+        const int64_t within = KBLK ? ((k >> 4) * rows_pad + r) * 16 + ((((k >> 3) & 1) ^ ((r >> 2) & 1)) << 3) + (k & 7)
+                                    : r * Kp + k;
+        uint16_t* dst = slices + (int64_t)q * OZ_S * plane + within;
         float sc = 1.0f;
 #pragma unroll
         for (int s = 0; s < OZ_S; ++s) {
@@ -477,7 +482,6 @@ constexpr int THREADS = 320;
 constexpr unsigned TMEM_COLS = 512;                   // Re G0..G3 T | Im G0..G3 T, 48 columns each (480 used)
 constexpr int CHUNK_KB = 16;                          // k-blocks per exact chunk (256 k)
 constexpr int EPI_COLS = BN / 2;                      // columns per epilogue warp (three groups of 8)
-constexpr int NP_ALIGN = 96;                          // N padding: whole tiles and the slicer's 32-row tiles
 }  // namespace ozc
 
 // tcgen05.ld of 8 columns without the wait.
@@ -530,9 +534,10 @@ __device__ __forceinline__ uint64_t make_desc_sw32(uint32_t saddr) {
   return d;
 }
 
-// kind::f16 instruction descriptor: D = F32, A = B = BF16, K-major both, N = 32, M = 128, optional -A.
-__host__ __device__ constexpr uint32_t make_idesc_ozc(bool negA) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(ozc::BN >> 3) << 17) |
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, K-major both, M = 128, N = n (a
+// multiple of 16, at most ozc::BN), optional -A.
+__host__ __device__ constexpr uint32_t make_idesc_ozc(bool negA, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(ozc::BM >> 4) << 24);
 }
 
@@ -540,6 +545,11 @@ struct OzcParams {
   int64_t M, N;
   int nkb;                   // k-blocks of ozc::BK
   int a_parts;               // 2, or 1 for a real A (no Im slices)
+  int W;                     // column tile width: a multiple of 16, at most ozc::BN
+  int ntn;                   // column tiles
+  int64_t ntiles;            // row tiles x column tiles
+  const uint16_t* sA;        // A slices [a_parts * 6][nkb][rowsA][16], each 32-byte row swizzled
+  const uint16_t* sB;        // B slices [12][nkb][rowsB][16]
   const int* fA;             // per-row scale exponents of A (shared by Re and Im)
   const int* fB;             // per-column scale exponents of B
   z64* C;
@@ -550,8 +560,26 @@ struct OzcParams {
   int64_t rowsA, rowsB;      // padded rows per slice plane
 };
 
-__global__ void __launch_bounds__(ozc::THREADS, 1)
-ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, OzcParams p) {
+// MMA columns of column tile tn: W, or the rest of N rounded up to the MMA's 16.
+__device__ __forceinline__ int ozc_tile_width(int64_t N, int W, int tn) {
+  const int64_t rest = N - (int64_t)tn * W;
+  return rest >= W ? W : (int)((rest + 15) & ~(int64_t)15);
+}
+
+// Persistent: each CTA takes tiles blockIdx.x, + gridDim.x, ... (the column tiles of a row
+// tile adjacent, so the CTAs running at once share their A slices through L2).  Warp 0
+// copies k-blocks of slices (contiguous runs, one bulk copy per plane) into a ring of
+// stages that runs across tiles; warp 1 issues the MMAs; warps 2..9 read the accumulators
+// into registers, release TMEM to the next tile's MMAs and only then convert and store,
+// so a tile's epilogue overlaps the next tile's MMAs.
+//
+// A tile of width wn keeps its ten accumulators wn columns apart in TMEM and its B slice
+// tiles wn rows apart in the stage, so the exact groups sa..3 and the tail of one A slice
+// sa are one MMA against B slices 0..4-sa side by side (N = (5 - sa) wn), and the g = 5
+// pair (sa, 5 - sa) a second one into the tail: 11 MMAs per product instead of one per
+// slice pair (21).  Each MMA reads its A slice from shared memory once; the narrow ones
+// cost about as much as the wide ones, so fewer, wider MMAs are faster.
+__global__ void __launch_bounds__(ozc::THREADS, 1) ozc_kernel(OzcParams p) {
   constexpr int STAGES = ozc::STAGES, STAGE_BYTES = ozc::STAGE_BYTES, A_TILE = ozc::A_TILE, B_TILE = ozc::B_TILE;
   constexpr int CBM = ozc::BM, CBN = ozc::BN, CBK = ozc::BK, NSL = ozc::NSL, EPI = ozc::EPI_COLS;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -559,21 +587,16 @@ ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUt
   uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty_bar = full_bar + STAGES;
   uint64_t* chunk_bar = empty_bar + STAGES;   // MMA -> epilogue: the chunk's MMAs completed
-  uint64_t* drained_bar = chunk_bar + 1;      // epilogue -> MMA: exact accumulators read (8 warps)
-  uint32_t* tmem_slot = (uint32_t*)(drained_bar + 1);
+  uint64_t* drained_bar = chunk_bar + 1;      // epilogue -> MMA: the chunk's accumulators read (8 warps)
+  uint64_t* done_bar = drained_bar + 1;       // MMA issuer, on abort: its MMAs completed
+  uint32_t* tmem_slot = (uint32_t*)(done_bar + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntn = gridDim.x, ntm = gridDim.y;
-  const int lin = blockIdx.y * ntn + blockIdx.x;
-  const int gsz = kGroupM * ntn;
-  const int first_m = (lin / gsz) * kGroupM;
-  const int gm = min(ntm - first_m, kGroupM);
-  const int tile_m = first_m + (lin % gsz) % gm;
-  const int tile_n = (lin % gsz) / gm;
   const int nk = p.nkb;
   const int nchunks = (nk + ozc::CHUNK_KB - 1) / ozc::CHUNK_KB;
   const int na = p.a_parts;
+  const int64_t tile0 = blockIdx.x, tstep = gridDim.x;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -582,6 +605,7 @@ ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUt
     }
     mbar_init(chunk_bar, 1);
     mbar_init(drained_bar, 8);
+    mbar_init(done_bar, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -598,176 +622,197 @@ ozc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUt
 
   if (warp == 0) {
     if (lane == 0) {
-      const uint32_t bytes = (uint32_t)(na * OZ_S * A_TILE + NSL * B_TILE);
-      int issued = 0;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-        if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
-        uint8_t* st = smem + s * STAGE_BYTES;
-        mbar_expect_tx(&full_bar[s], bytes);
-        const int kx = kb * CBK;
-        for (int q = 0; q < na * OZ_S; ++q)
-          tma_load_2d(st + q * A_TILE, &mapA, &full_bar[s], kx, (int)(q * p.rowsA + tile_m * CBM));
-        for (int q = 0; q < NSL; ++q)
-          tma_load_2d(st + NSL * A_TILE + q * B_TILE, &mapB, &full_bar[s], kx, (int)(q * p.rowsB + tile_n * CBN));
-        issued = kb + 1;
+      long long issued = 0;   // k-blocks whose copies were issued (the stage ring runs across tiles)
+      bool ok = true;
+      for (int64_t t = tile0; t < p.ntiles && ok; t += tstep) {
+        const int64_t tm = t / p.ntn;
+        const int tn = (int)(t % p.ntn);
+        const uint32_t bbytes = (uint32_t)ozc_tile_width(p.N, p.W, tn) * CBK * 2;
+        const uint32_t bytes = (uint32_t)(na * OZ_S * A_TILE) + (uint32_t)NSL * bbytes;
+        const uint16_t* a0 = p.sA + tm * CBM * CBK;
+        const uint16_t* b0 = p.sB + (int64_t)tn * p.W * CBK;
+        for (int kb = 0; kb < nk; ++kb) {
+          const int s = (int)(issued % STAGES);
+          const uint32_t ph = (uint32_t)(issued / STAGES) & 1u;
+          if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) {
+            ok = false;
+            break;
+          }
+          uint8_t* st = smem + s * STAGE_BYTES;
+          mbar_expect_tx(&full_bar[s], bytes);
+          for (int q = 0; q < na * OZ_S; ++q)
+            bulk_load(st + q * A_TILE, a0 + ((int64_t)q * nk + kb) * p.rowsA * CBK, (uint32_t)A_TILE, &full_bar[s]);
+          // B slice tiles of this tile's width, packed wn rows apart
+          for (int q = 0; q < NSL; ++q)
+            bulk_load(st + NSL * A_TILE + q * bbytes, b0 + ((int64_t)q * nk + kb) * p.rowsB * CBK, bbytes,
+                      &full_bar[s]);
+          ++issued;
+        }
       }
-      if (*abort_flag) {
-        for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb) {
+      if (!ok) {
+        // let the copies in flight land before the CTA exits
+        for (long long i = (issued > STAGES ? issued - STAGES : 0); i < issued; ++i) {
           long long t0 = clock64();
-          while (!mbar_try_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u) &&
-                 clock64() - t0 < kWaitCycles) {
+          while (!mbar_try_wait(&full_bar[i % STAGES], (uint32_t)(i / STAGES) & 1u) && clock64() - t0 < kWaitCycles) {
           }
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t id_pos = make_idesc_ozc(false), id_neg = make_idesc_ozc(true);
-      for (int kb = 0; kb < nk; ++kb) {
-        const int kc = kb % ozc::CHUNK_KB, chunk = kb / ozc::CHUNK_KB;
-        if (kc == 0 && chunk > 0) {
-          // the epilogue must have read the previous chunk's exact accumulators
-          if (!mbar_wait(drained_bar, (uint32_t)(chunk - 1) & 1u, p.err, abort_flag, 4)) break;
+      long long used = 0;   // k-blocks consumed
+      long long chunks = 0;  // chunks committed
+      bool ok = true;
+      for (int64_t t = tile0; t < p.ntiles && ok; t += tstep) {
+        const int wn = ozc_tile_width(p.N, p.W, (int)(t % p.ntn));
+        for (int kb = 0; kb < nk; ++kb, ++used) {
+          const int kc = kb % ozc::CHUNK_KB;
+          if (kc == 0 && chunks > 0) {
+            // the epilogue must have read the previous chunk's accumulators (this tile's or the last one's)
+            if (!mbar_wait(drained_bar, (uint32_t)(chunks - 1) & 1u, p.err, abort_flag, 4)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          }
+          const int s = (int)(used % STAGES);
+          const uint32_t ph = (uint32_t)(used / STAGES) & 1u;
+          if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) {
+            ok = false;
+            break;
+          }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        }
-        const int s = kb % STAGES;
-        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-        if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint64_t a0 = make_desc_sw32(smem_u32(smem + s * STAGE_BYTES));
-        const uint64_t b0 = make_desc_sw32(smem_u32(smem + s * STAGE_BYTES + NSL * A_TILE));
-        // products (A part, B part, accumulator set, -A): Re.Re, Im.Im -> Re; Re.Im, Im.Re -> Im
+          const uint64_t a0 = make_desc_sw32(smem_u32(smem + s * STAGE_BYTES));
+          const uint64_t b0 = make_desc_sw32(smem_u32(smem + s * STAGE_BYTES + NSL * A_TILE));
+          // products (A part, B part, accumulator set, -A): Re.Re, Im.Im -> Re; Re.Im, Im.Re -> Im
 #pragma unroll
-        for (int pr = 0; pr < 4; ++pr) {
-          const int aq = (pr == 1 || pr == 3) ? 1 : 0, bq = (pr == 1 || pr == 2) ? 1 : 0;
-          const int set = pr >= 2 ? 1 : 0;
-          if (aq == 1 && na == 1) continue;                 // a real A has no Im part
-          const uint32_t idesc = pr == 1 ? id_neg : id_pos;
+          for (int pr = 0; pr < 4; ++pr) {
+            const int aq = (pr == 1 || pr == 3) ? 1 : 0, bq = (pr == 1 || pr == 2) ? 1 : 0;
+            const int set = pr >= 2 ? 1 : 0;
+            if (aq == 1 && na == 1) continue;                 // a real A has no Im part
+            const bool neg = pr == 1;
+            // the set's first product opens the exact groups at each chunk and the tail once per tile
+            const bool opener = pr == 0 || pr == 2;
+            const uint32_t acc0 = tmem_base + (uint32_t)(set * 5 * wn);
 #pragma unroll
-          for (int sa = 0; sa < OZ_S; ++sa) {
-#pragma unroll
-            for (int tb = 0; tb + sa < OZ_S; ++tb) {
-              const int g = sa + tb;
-              const int d = g < 4 ? g : 4;
+            for (int sa = 0; sa < OZ_S; ++sa) {
               const uint64_t a = a0 + (uint64_t)(((aq * OZ_S + sa) * A_TILE) >> 4);
-              const uint64_t b = b0 + (uint64_t)(((bq * OZ_S + tb) * B_TILE) >> 4);
-              // the set's first product opens each exact group per chunk and the tail once
-              const bool first = (pr == 0 || pr == 2) && sa == 0 && ((g < 4 && kc == 0) || (g == 4 && kb == 0));
-              mma_bf16(tmem_base + (uint32_t)((set * 5 + d) * CBN), a, b, idesc, first ? 0u : 1u);
+              const uint64_t bs = b0 + (uint64_t)(((bq * OZ_S) * wn * CBK * 2) >> 4);   // B slice 0 of part bq
+              if (sa < OZ_S - 1) {
+                // groups sa..3 and the tail: B slices 0..4-sa
+                const int run = OZ_S - 1 - sa;
+                if (opener && sa == 0 && kc == 0 && kb > 0) {
+                  // a later chunk: the exact groups restart, the tail carries on
+                  mma_bf16(acc0, a, bs, make_idesc_ozc(neg, 4 * wn), 0u);
+                  mma_bf16(acc0 + (uint32_t)(4 * wn), a, bs + (uint64_t)((4 * wn * CBK * 2) >> 4),
+                           make_idesc_ozc(neg, wn), 1u);
+                } else {
+                  mma_bf16(acc0 + (uint32_t)(sa * wn), a, bs, make_idesc_ozc(neg, run * wn),
+                           (opener && sa == 0 && kc == 0) ? 0u : 1u);
+                }
+              }
+              // the g = 5 pair (sa, 5 - sa) into the tail
+              mma_bf16(acc0 + (uint32_t)(4 * wn), a, bs + (uint64_t)(((OZ_S - 1 - sa) * wn * CBK * 2) >> 4),
+                       make_idesc_ozc(neg, wn), 1u);
             }
           }
+          mma_commit(&empty_bar[s]);
+          if (kc == ozc::CHUNK_KB - 1 || kb == nk - 1) {
+            mma_commit(chunk_bar);
+            ++chunks;
+          }
         }
-        mma_commit(&empty_bar[s]);
-        if (kc == ozc::CHUNK_KB - 1 || kb == nk - 1) mma_commit(chunk_bar);
+      }
+      if (!ok) {
+        // the MMAs issued so far complete before TMEM is freed
+        mma_commit(done_bar);
+        long long t0 = clock64();
+        while (!mbar_try_wait(done_bar, 0u) && clock64() - t0 < kWaitCycles) {
+        }
       }
     }
   } else {
     // epilogue: warps 2..9; TMEM lane quadrant q = warp % 4, column half h
     const int q = warp & 3, h = (warp - 2) >> 2;
     const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * EPI);
-    const int64_t m = (int64_t)tile_m * CBM + q * 32 + lane;
-    const int64_t n0 = (int64_t)tile_n * CBN + h * EPI;
-    // C(m, n) from the int64 sums (units 2^-21) and the FP32 tails of the two sets
-    auto store = [&](int64_t n, long long Ir, long long Ii, float tr, float ti, int fa) {
-      const int e2 = fa + p.fB[n] - 32;
-      // exact groups and the FP32 tail in units of 2^-32, rounded once to FP64
-      const long long Tr = oz_fixed32(Ir, tr), Ti = oz_fixed32(Ii, ti);
-      z64 out;
-      if (e2 >= -1022 && e2 <= 960) out = zmk(i64_ldexp_normal(Tr, e2), i64_ldexp_normal(Ti, e2));
-      else out = zmk(i64_ldexp_rn(Tr, e2), i64_ldexp_rn(Ti, e2));
-      z64* cp = p.C + m * p.ldc + n;
-      if (!p.plain) {
-        out = zmul(p.alpha, out);
-        if (p.beta.x != 0.0 || p.beta.y != 0.0) out = zadd(out, zmul(p.beta, *cp));
-      }
-      *cp = out;
-    };
-    if (nchunks == 1) {
-      // K <= 256: one exact chunk, converted straight from TMEM, 8 columns at a time
-      int okw = 0;
-      if (lane == 0) okw = mbar_wait(chunk_bar, 0u, p.err, abort_flag, 3) ? 1 : 0;
-      if (__shfl_sync(0xffffffffu, okw, 0) != 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int fa = m < p.M ? p.fA[m] : 0;
-#pragma unroll 1
-        for (int c8 = 0; c8 < EPI / 8; ++c8) {
-          uint32_t r0[8], r1[8], r2[8], r3[8], rt[8], i0[8], i1[8], i2[8], i3[8], it[8];
-          const uint32_t sb = lane_base + (uint32_t)(c8 * 8);
-          tmem_ld8_async(sb, r0);
-          tmem_ld8_async(sb + CBN, r1);
-          tmem_ld8_async(sb + 2 * CBN, r2);
-          tmem_ld8_async(sb + 3 * CBN, r3);
-          tmem_ld8_async(sb + 4 * CBN, rt);
-          tmem_ld8_async(sb + 5 * CBN, i0);
-          tmem_ld8_async(sb + 6 * CBN, i1);
-          tmem_ld8_async(sb + 7 * CBN, i2);
-          tmem_ld8_async(sb + 8 * CBN, i3);
-          tmem_ld8_async(sb + 9 * CBN, it);
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-          if (m < p.M) {
+    long long chunks = 0;
+    bool ok = nk > 0;
+    for (int64_t t = tile0; t < p.ntiles && ok; t += tstep) {
+      const int64_t tm = t / p.ntn;
+      const int tn = (int)(t % p.ntn);
+      const int wn = ozc_tile_width(p.N, p.W, tn);
+      const int64_t m = tm * CBM + q * 32 + lane;
+      const int64_t n0 = (int64_t)tn * p.W + h * EPI;
+      const bool cols = h * EPI < wn;   // warp-uniform: this half of the tile holds columns of C
+      // exact group sums (units 2^-21); after the last chunk, with the tails, in units of 2^-32
+      long long ar[EPI], ai[EPI];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int64_t n = n0 + c8 * 8 + j;
-              if (n < p.N)
-                store(n, oz_groups(r0[j], r1[j], r2[j], r3[j]), oz_groups(i0[j], i1[j], i2[j], i3[j]),
-                      __uint_as_float(rt[j]), __uint_as_float(it[j]), fa);
+      for (int j = 0; j < EPI; ++j) ar[j] = ai[j] = 0;
+      for (int c = 0; c < nchunks; ++c, ++chunks) {
+        int okw = 0;
+        if (lane == 0) okw = mbar_wait(chunk_bar, (uint32_t)chunks & 1u, p.err, abort_flag, 3) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (cols) {
+#pragma unroll
+          for (int set = 0; set < 2; ++set) {
+#pragma unroll
+            for (int c8 = 0; c8 < EPI / 8; ++c8) {
+              uint32_t g0[8], g1[8], g2[8], g3[8];
+              const uint32_t sb = lane_base + (uint32_t)(set * 5 * wn + c8 * 8);
+              tmem_ld8_async(sb, g0);
+              tmem_ld8_async(sb + wn, g1);
+              tmem_ld8_async(sb + 2 * wn, g2);
+              tmem_ld8_async(sb + 3 * wn, g3);
+              asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const long long v = oz_groups(g0[j], g1[j], g2[j], g3[j]);
+                if (set == 0) ar[c8 * 8 + j] += v; else ai[c8 * 8 + j] += v;
+              }
+            }
+          }
+          if (c == nchunks - 1) {
+#pragma unroll
+            for (int c8 = 0; c8 < EPI / 8; ++c8) {
+              uint32_t tr[8], ti[8];
+              tmem_ld8_async(lane_base + 4 * wn + c8 * 8, tr);
+              tmem_ld8_async(lane_base + 9 * wn + c8 * 8, ti);
+              asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                ar[c8 * 8 + j] = oz_fixed32(ar[c8 * 8 + j], __uint_as_float(tr[j]));
+                ai[c8 * 8 + j] = oz_fixed32(ai[c8 * 8 + j], __uint_as_float(ti[j]));
+              }
             }
           }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(drained_bar);
       }
-    } else {
-    long long ar[EPI], ai[EPI];   // exact group sums in units of 2^-21
-#pragma unroll
-    for (int j = 0; j < EPI; ++j) ar[j] = ai[j] = 0;
-    bool ok = nk > 0;
-    for (int c = 0; c < nchunks && ok; ++c) {
-      int okw = 0;
-      if (lane == 0) okw = mbar_wait(chunk_bar, (uint32_t)c & 1u, p.err, abort_flag, 3) ? 1 : 0;
-      ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
       if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // TMEM is free for the next tile: convert (exact sums + tail, units 2^-32, rounded once to FP64) and store
+      if (cols && m < p.M) {
+        const int fa = p.fA[m];
+        z64* crow = p.C + m * p.ldc;
 #pragma unroll
-      for (int set = 0; set < 2; ++set) {
-#pragma unroll
-        for (int c8 = 0; c8 < EPI / 8; ++c8) {
-          uint32_t g0[8], g1[8], g2[8], g3[8];
-          const uint32_t sb = lane_base + (uint32_t)(set * 5 * CBN + c8 * 8);
-          tmem_ld8_async(sb, g0);
-          tmem_ld8_async(sb + CBN, g1);
-          tmem_ld8_async(sb + 2 * CBN, g2);
-          tmem_ld8_async(sb + 3 * CBN, g3);
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const long long v = oz_groups(g0[j], g1[j], g2[j], g3[j]);
-            if (set == 0) ar[c8 * 8 + j] += v; else ai[c8 * 8 + j] += v;
+        for (int j = 0; j < EPI; ++j) {
+          const int64_t n = n0 + j;
+          if (h * EPI + j < wn && n < p.N) {
+            const int e2 = fa + p.fB[n] - 32;
+            z64 out;
+            if (e2 >= -1022 && e2 <= 960) out = zmk(i64_ldexp_normal(ar[j], e2), i64_ldexp_normal(ai[j], e2));
+            else out = zmk(i64_ldexp_rn(ar[j], e2), i64_ldexp_rn(ai[j], e2));
+            if (!p.plain) {
+              out = zmul(p.alpha, out);
+              if (p.beta.x != 0.0 || p.beta.y != 0.0) out = zadd(out, zmul(p.beta, crow[n]));
+            }
+            crow[n] = out;
           }
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(drained_bar);
-    }
-    if (ok) {
-      const int fa = m < p.M ? p.fA[m] : 0;
-#pragma unroll
-      for (int c8 = 0; c8 < EPI / 8; ++c8) {
-        uint32_t tr[8], ti[8];
-        tmem_ld8_async(lane_base + 4 * CBN + c8 * 8, tr);
-        tmem_ld8_async(lane_base + 9 * CBN + c8 * 8, ti);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (m < p.M) {
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int64_t n = n0 + c8 * 8 + j;
-            if (n < p.N)
-              store(n, ar[c8 * 8 + j], ai[c8 * 8 + j], __uint_as_float(tr[j]), __uint_as_float(ti[j]), fa);
-          }
-        }
-      }
-    }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -781,18 +826,18 @@ int64_t rup(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 int sign_code(double c) { return c == 0.0 ? 0 : (c == 1.0 ? 1 : (c == -1.0 ? -1 : 2)); }
 
-// Tensor map over slice planes [rows_total][Kp] (bf16): boxes of box_k x box_rows, with the
-// 64-byte swizzle for 32-wide k-blocks (3M kernel) or the 32-byte one for 16-wide (one-pass kernel).
-bool encode_slices(CUtensorMap* map, uint16_t* base, int64_t rows_total, int64_t Kp, int box_rows, int box_k = BK) {
+// Tensor map over slice planes [rows_total][Kp] (bf16) for the 3M kernel: boxes of BK x
+// box_rows with the 64-byte swizzle.
+bool encode_slices(CUtensorMap* map, uint16_t* base, int64_t rows_total, int64_t Kp, int box_rows) {
   auto enc = tma_encode_fn();
   if (!enc) return false;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
   cuuint64_t strides[1] = {(cuuint64_t)(Kp * 2)};
-  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1u, 1u};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
@@ -809,7 +854,7 @@ struct OzcLayout {
 OzcLayout ozc_layout(int64_t M, int64_t N, int64_t K, int na) {
   OzcLayout L;
   L.Mp = rup(M, ozc::BM);
-  L.Np = rup(N, ozc::NP_ALIGN);
+  L.Np = rup(rup(N, ozc::BN), 32);   // whole 48-wide column tiles, in the slicer's 32-row tiles
   L.Kp = rup(K, 32);      // the slicing kernels work on 32 x 32 tiles
   size_t off = 256;       // status word
   auto take = [&](size_t bytes) {
@@ -885,9 +930,6 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
     agb_set_error_message("ozgemm: scratch too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;
   }
-  AGB_ARG_CHECK(L.Mp / ozc::BM <= 65535, "ozgemm: M too large for the grid");
-  AGB_ARG_CHECK(2 * OZ_S * L.Mp < (1ll << 31) && 2 * OZ_S * L.Np < (1ll << 31),
-                "ozgemm: too many rows for a tensor map");
   char* base = (char*)scratch;
   uint16_t* sA = (uint16_t*)(base + L.sA);
   uint16_t* sB = (uint16_t*)(base + L.sB);
@@ -895,17 +937,6 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
   int* eB = (int*)(base + L.eB);
   int* fA = (int*)(base + L.fA);
   int* fB = (int*)(base + L.fB);
-  CUtensorMap mA, mB;
-  if (!encode_slices(&mA, sA, na * OZ_S * L.Mp, L.Kp, ozc::BM, ozc::BK) ||
-      !encode_slices(&mB, sB, 2 * OZ_S * L.Np, L.Kp, ozc::BN, ozc::BK)) {
-    agb_set_error_message("ozgemm: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
-    return AGB_ERR_CUDA;
-  }
-  static bool attr_set = false;
-  if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(ozc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ozc::SMEM_BYTES));
-    attr_set = true;
-  }
   // both parts of an operand from one read, under one exponent per row (estride 0)
   auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int np, int64_t rows_pad,
                    int* emax, int* fexp, uint16_t* dst) -> agb_status {
@@ -918,11 +949,11 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
     const int64_t t2 = (rows_pad / 32) * (L.Kp / 32);
     const int g2 = (int)(t2 < 152 * 32 ? t2 : 152 * 32);
     if (np == 2)
-      oz_slice_kernel<2><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax, fexp,
-                                                 dst);
+      oz_slice_kernel<2, true><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax,
+                                                       fexp, dst);
     else
-      oz_slice_kernel<1><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax, fexp,
-                                                 dst);
+      oz_slice_kernel<1, true><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax,
+                                                       fexp, dst);
     AGB_LAUNCH_CHECK();
     return AGB_OK;
   };
@@ -933,8 +964,17 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
   p.alpha = alpha; p.beta = beta;
   p.plain = alpha.x == 1.0 && alpha.y == 0.0 && beta.x == 0.0 && beta.y == 0.0;
   p.err = (int*)base; p.rowsA = L.Mp; p.rowsB = L.Np;
-  const dim3 grid((unsigned)((N + ozc::BN - 1) / ozc::BN), (unsigned)(L.Mp / ozc::BM));
-  ozc_kernel<<<grid, ozc::THREADS, ozc::SMEM_BYTES, stream>>>(mA, mB, p);
+  p.sA = sA; p.sB = sB;
+  // ceil(N / 48) column tiles of equal width W (a multiple of 16; the last may be narrower)
+  p.ntn = (int)((N + ozc::BN - 1) / ozc::BN);
+  p.W = (int)rup((N + p.ntn - 1) / p.ntn, 16);
+  p.ntiles = (L.Mp / ozc::BM) * p.ntn;
+  AGB_CUDA_TRY(cudaFuncSetAttribute(ozc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ozc::SMEM_BYTES));
+  int dev = 0, nsm = 0;
+  AGB_CUDA_TRY(cudaGetDevice(&dev));
+  AGB_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t grid = p.ntiles < nsm ? p.ntiles : nsm;   // one persistent CTA per SM
+  ozc_kernel<<<(unsigned)grid, ozc::THREADS, ozc::SMEM_BYTES, stream>>>(p);
   AGB_LAUNCH_CHECK();
   return AGB_OK;
 }

@@ -42,7 +42,10 @@ def oz(A, B, alpha=1.0, beta=0.0, C=None, conjA=False, conjB=False, transA=False
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 32), (130, 260, 700), (300, 129, 20), (256, 384, 1500),
-                                   (5, 7, 3), (200, 160, 1025), (129, 33, 1024), (257, 31, 257), (64, 96, 96)])
+                                   (5, 7, 3), (200, 160, 1025), (129, 33, 1024), (257, 31, 257), (64, 96, 96),
+                                   # several tiles per persistent CTA; last column tiles 16 or 32 wide;
+                                   # one to four 256-long chunks per tile
+                                   (20000, 150, 150), (3000, 100, 300), (2000, 20, 520), (1500, 64, 1024)])
 def test_oz_gemm_accuracy(M, N, K):
     rng = np.random.default_rng(M + 7 * N + 13 * K)
     A = crandn(rng, M, K)
