@@ -388,6 +388,35 @@ __device__ __forceinline__ uint16_t oz_digit_bf16(long long d, float scale) {
   return (uint16_t)(__float_as_uint(__fmul_rn(f, scale)) >> 16);
 }
 
+// The OZ_S bf16 slices of v under the row's biased exponent eb (0: a zero row): v 2^-f,
+// f = eb - 1023 + 1 - 7, rounded to the nearest integer X (|X| <= 2^42), split into
+// balanced base-2^7 digits d_s; slice s is d_s 2^-7s, exact in bf16.
+__device__ __forceinline__ void oz_digits(double v, int eb, uint16_t (&out)[OZ_S]) {
+  const uint32_t hw = (uint32_t)__double2hiint(v), lw = (uint32_t)__double2loint(v);
+  const int ex = (int)((hw >> 20) & 0x7ffu);
+  long long X = 0;
+  const int shift = 11 + (eb - ex);
+  if (ex > 0 && eb > 0 && shift < 64) {
+    const unsigned long long M = ((unsigned long long)(hw & 0xfffffu) << 32 | lw) | (1ull << 52);
+    X = (long long)((M + (1ull << (shift - 1))) >> shift);   // nearest (|X| <= 2^42 keeps |d_0| <= 128)
+    if (hw >> 31) X = -X;
+  }
+  long long d[OZ_S];
+#pragma unroll
+  for (int s = 0; s < OZ_S - 1; ++s) {
+    const int sh = 35 - 7 * s;
+    d[s] = (X + (1ll << (sh - 1))) >> sh;
+    X -= d[s] << sh;
+  }
+  d[OZ_S - 1] = X;
+  float sc = 1.0f;
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) {
+    out[s] = oz_digit_bf16(d[s], sc);
+    sc *= 0.0078125f;   // 2^-7
+  }
+}
+
 // Slices [OZ_S][rows_pad][Kp] (bf16, K-major, zero padded) and row scale exponents f_r of
 // NP parts from one read of the source: part q's slices start at slices + q * OZ_S * rows_pad * Kp,
 // its exponents at emax / fexp + q * estride (estride 0: one exponent shared by the parts).
@@ -420,34 +449,13 @@ __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64
       for (int q = 0; q < NP; ++q) {
         const int eb = r < rows ? emax[q * estride + r] : 0;
         if (k0 == 0 && tx == 0 && r < rows_pad) fexp[q * estride + r] = eb > 0 ? eb - 1023 + 1 - 7 : 0;
-        const double v = oz_part(vz, part0 + q);
-        const uint32_t hw = (uint32_t)__double2hiint(v), lw = (uint32_t)__double2loint(v);
-        const int ex = (int)((hw >> 20) & 0x7ffu);
-        long long X = 0;
-        const int shift = 11 + (eb - ex);
-        if (ex > 0 && eb > 0 && shift < 64) {
-          const unsigned long long M = ((unsigned long long)(hw & 0xfffffu) << 32 | lw) | (1ull << 52);
-          X = (long long)((M + (1ull << (shift - 1))) >> shift);   // nearest (|X| <= 2^42 keeps |d_0| <= 128)
-          if (hw >> 31) X = -X;
-        }
-        // balanced base-2^7 digits of X (|X| < 2^42)
-        long long d[OZ_S];
-#pragma unroll
-        for (int s = 0; s < OZ_S - 1; ++s) {
-          const int sh = 35 - 7 * s;
-          d[s] = (X + (1ll << (sh - 1))) >> sh;
-          X -= d[s] << sh;
-        }
-        d[OZ_S - 1] = X;
+        uint16_t dg[OZ_S];
+        oz_digits(oz_part(vz, part0 + q), eb, dg);
         const int64_t within = KBLK ? ((k >> 4) * rows_pad + r) * 16 + ((((k >> 3) & 1) ^ ((r >> 2) & 1)) << 3) + (k & 7)
                                     : r * Kp + k;
         uint16_t* dst = slices + (int64_t)q * OZ_S * plane + within;
-        float sc = 1.0f;
 #pragma unroll
-        for (int s = 0; s < OZ_S; ++s) {
-          dst[s * plane] = oz_digit_bf16(d[s], sc);
-          sc *= 0.0078125f;   // 2^-7
-        }
+        for (int s = 0; s < OZ_S; ++s) dst[s * plane] = dg[s];
       }
     }
     __syncthreads();
@@ -459,17 +467,16 @@ __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64
 //
 // Rows of A and columns of B are sliced with one exponent shared by their Re and Im
 // parts, so the four real products Re.Re, Im.Im, Re.Im and Im.Re are sums in the same
-// fixed-point units: Re C = Re.Re - Im.Im accumulates in one set of TMEM columns
-// (the Im.Im MMAs negate A) and Im C = Re.Im + Im.Re in another.  Each set is the
-// 3M kernel's five accumulators (exact groups 0..3 and the tail); two products per
-// accumulator double the group bounds (group 3: 2 (2^14 + 2^13) units per k), so the
-// exact chunk is 256 k (< 2^24 units).  The tile is 128 x 48 outputs: 2 sets x 5 x 48
-// = 480 TMEM columns (the widest tile that fits; each MMA instruction then carries 1.5x
-// the work of a 32-wide one, which matters because 21 slice pairs x 4 products make
-// many small MMAs).  The epilogue turns the int64 group sums and the tail into FP64 with
-// integer instructions and writes C once: no read-modify-write of C between products and
-// no FP64 arithmetic when alpha = 1 and beta = 0.  A real A (the first AO->MO quarter
-// step) has no Im slices and runs the Re.Re and Re.Im products only.
+// fixed-point units: Re C = Re.Re - Im.Im accumulates in one set of TMEM columns (the
+// Im.Im MMAs negate A) and Im C = Re.Im + Im.Re in another.  Each set is the 3M kernel's
+// five accumulators (exact groups 0..3 and the tail); two products per accumulator
+// double the group bounds (group 3: 2 (2^14 + 2^13) units per k), so the exact chunk is
+// 256 k (< 2^24 units).  The tile is 128 x 48 outputs: 2 sets x 5 x 48 = 480 TMEM
+// columns, the widest tile that fits.  The epilogue turns the int64 group sums and the
+// tail into FP64 with integer instructions and writes C once: no read-modify-write of C
+// between products and no FP64 arithmetic when alpha = 1 and beta = 0.  A real A (the
+// first AO->MO quarter step) has no Im slices and runs the Re.Re and Re.Im products
+// only.
 namespace ozc {
 constexpr int BM = 128, BN = 48, BK = 16;            // BK in bf16 elements (32-byte rows)
 constexpr int NSL = 2 * OZ_S;                         // slice tiles per operand: Re 0..5, Im 6..11

@@ -109,6 +109,19 @@ def test_oz_gemm_single_slicing_pass_is_identical(conjA):
     np.testing.assert_array_equal(one, fused)
 
 
+@pytest.mark.parametrize("M,N,K", [(3000, 150, 150), (700, 40, 600)])
+def test_oz_gemm_transposed_operands_are_identical(M, N, K):
+    """Short K: operands read along k or along rows (the slicer's two transposed tile loads)
+    give the same slices in the K-blocked layout, so the same bits."""
+    rng = np.random.default_rng(19)
+    A, B = crandn(rng, M, K), crandn(rng, K, N)
+    kfast = oz(A, B.T.copy(), transB=True)                    # A: k-fast rows; B: k-fast columns
+    rowfast = oz(A.T.copy(), B, transA=True)                  # A: adjacent rows; B: adjacent columns
+    np.testing.assert_array_equal(kfast, rowfast)
+    err = np.abs(rowfast - A @ B) / (np.abs(A) @ np.abs(B))
+    assert err.max() < TOL, err.max()
+
+
 @pytest.mark.parametrize("K", [2048, 1000])
 def test_oz_gemm_integer_products_exact(K):
     """Small-integer operands have exact slices, so every partial sum is an exact
