@@ -485,10 +485,10 @@ constexpr int B_TILE = BN * BK * 2;                   // 1.5 KB
 constexpr int STAGE_BYTES = NSL * (A_TILE + B_TILE);  // 66 KB
 constexpr int STAGES = 3;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int THREADS = 320;
+constexpr int THREADS = 448;                          // load warp, MMA warp, 12 epilogue warps
 constexpr unsigned TMEM_COLS = 512;                   // Re G0..G3 T | Im G0..G3 T, 48 columns each (480 used)
 constexpr int CHUNK_KB = 16;                          // k-blocks per exact chunk (256 k)
-constexpr int EPI_COLS = BN / 2;                      // columns per epilogue warp (three groups of 8)
+constexpr int EPI_COLS = BN / 3;                      // columns per epilogue warp (two groups of 8)
 }  // namespace ozc
 
 // tcgen05.ld of 8 columns without the wait.
@@ -576,7 +576,7 @@ __device__ __forceinline__ int ozc_tile_width(int64_t N, int W, int tn) {
 // Persistent: each CTA takes tiles blockIdx.x, + gridDim.x, ... (the column tiles of a row
 // tile adjacent, so the CTAs running at once share their A slices through L2).  Warp 0
 // copies k-blocks of slices (contiguous runs, one bulk copy per plane) into a ring of
-// stages that runs across tiles; warp 1 issues the MMAs; warps 2..9 read the accumulators
+// stages that runs across tiles; warp 1 issues the MMAs; warps 2..13 read the accumulators
 // into registers, release TMEM to the next tile's MMAs and only then convert and store,
 // so a tile's epilogue overlaps the next tile's MMAs.
 //
@@ -594,7 +594,7 @@ __global__ void __launch_bounds__(ozc::THREADS, 1) ozc_kernel(OzcParams p) {
   uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty_bar = full_bar + STAGES;
   uint64_t* chunk_bar = empty_bar + STAGES;   // MMA -> epilogue: the chunk's MMAs completed
-  uint64_t* drained_bar = chunk_bar + 1;      // epilogue -> MMA: the chunk's accumulators read (8 warps)
+  uint64_t* drained_bar = chunk_bar + 1;      // epilogue -> MMA: the chunk's accumulators read (12 warps)
   uint64_t* done_bar = drained_bar + 1;       // MMA issuer, on abort: its MMAs completed
   uint32_t* tmem_slot = (uint32_t*)(done_bar + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
@@ -611,7 +611,7 @@ __global__ void __launch_bounds__(ozc::THREADS, 1) ozc_kernel(OzcParams p) {
       mbar_init(&empty_bar[s], 1);
     }
     mbar_init(chunk_bar, 1);
-    mbar_init(drained_bar, 8);
+    mbar_init(drained_bar, 12);
     mbar_init(done_bar, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(ozc::THREADS, 1) ozc_kernel(OzcParams p) {
       }
     }
   } else {
-    // epilogue: warps 2..9; TMEM lane quadrant q = warp % 4, column half h
+    // epilogue: warps 2..13; TMEM lane quadrant q = warp % 4, column third h
     const int q = warp & 3, h = (warp - 2) >> 2;
     const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * EPI);
     long long chunks = 0;
@@ -750,7 +750,17 @@ __global__ void __launch_bounds__(ozc::THREADS, 1) ozc_kernel(OzcParams p) {
       const int wn = ozc_tile_width(p.N, p.W, tn);
       const int64_t m = tm * CBM + q * 32 + lane;
       const int64_t n0 = (int64_t)tn * p.W + h * EPI;
-      const bool cols = h * EPI < wn;   // warp-uniform: this half of the tile holds columns of C
+      const bool cols = h * EPI < wn;   // warp-uniform: this third of the tile holds columns of C
+      // the row's and the columns' scale exponents, read while the tile's MMAs run
+      int fa = 0, fb[EPI];
+#pragma unroll
+      for (int j = 0; j < EPI; ++j) fb[j] = 0;
+      if (cols && m < p.M) {
+        fa = __ldg(p.fA + m);
+#pragma unroll
+        for (int j = 0; j < EPI; ++j)
+          if (h * EPI + j < wn && n0 + j < p.N) fb[j] = __ldg(p.fB + n0 + j);
+      }
       // exact group sums (units 2^-21); after the last chunk, with the tails, in units of 2^-32
       long long ar[EPI], ai[EPI];
 #pragma unroll
@@ -802,13 +812,12 @@ __global__ void __launch_bounds__(ozc::THREADS, 1) ozc_kernel(OzcParams p) {
       if (!ok) break;
       // TMEM is free for the next tile: convert (exact sums + tail, units 2^-32, rounded once to FP64) and store
       if (cols && m < p.M) {
-        const int fa = p.fA[m];
         z64* crow = p.C + m * p.ldc;
 #pragma unroll
         for (int j = 0; j < EPI; ++j) {
           const int64_t n = n0 + j;
           if (h * EPI + j < wn && n < p.N) {
-            const int e2 = fa + p.fB[n] - 32;
+            const int e2 = fa + fb[j] - 32;
             z64 out;
             if (e2 >= -1022 && e2 <= 960) out = zmk(i64_ldexp_normal(ar[j], e2), i64_ldexp_normal(ai[j], e2));
             else out = zmk(i64_ldexp_rn(ar[j], e2), i64_ldexp_rn(ai[j], e2));
