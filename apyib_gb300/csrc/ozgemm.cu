@@ -420,10 +420,7 @@ __device__ __forceinline__ void oz_digits(double v, int eb, uint16_t (&out)[OZ_S
 // Slices [OZ_S][rows_pad][Kp] (bf16, K-major, zero padded) and row scale exponents f_r of
 // NP parts from one read of the source: part q's slices start at slices + q * OZ_S * rows_pad * Kp,
 // its exponents at emax / fexp + q * estride (estride 0: one exponent shared by the parts).
-// KBLK: each slice plane is laid out [Kp / 16][rows_pad][16] instead, the two 16-byte halves
-// of a row's 32 bytes swapped on rows r with (r >> 2) & 1 (the MMA's 32-byte swizzle), so a
-// block of rows of one 16-k block is one contiguous, ready-to-use run of shared memory.
-template <int NP, bool KBLK = false>
+template <int NP>
 __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64_t K, int64_t s_row, int64_t s_k,
                                 int conj, int part0, int64_t rows_pad, int64_t Kp, int64_t estride,
                                 const int* __restrict__ emax, int* __restrict__ fexp, uint16_t* __restrict__ slices) {
@@ -451,11 +448,66 @@ __global__ void oz_slice_kernel(const z64* __restrict__ src, int64_t rows, int64
         if (k0 == 0 && tx == 0 && r < rows_pad) fexp[q * estride + r] = eb > 0 ? eb - 1023 + 1 - 7 : 0;
         uint16_t dg[OZ_S];
         oz_digits(oz_part(vz, part0 + q), eb, dg);
-        const int64_t within = KBLK ? ((k >> 4) * rows_pad + r) * 16 + ((((k >> 3) & 1) ^ ((r >> 2) & 1)) << 3) + (k & 7)
-                                    : r * Kp + k;
-        uint16_t* dst = slices + (int64_t)q * OZ_S * plane + within;
+        uint16_t* dst = slices + (int64_t)q * OZ_S * plane + r * Kp + k;
 #pragma unroll
         for (int s = 0; s < OZ_S; ++s) dst[s * plane] = dg[s];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Slices of NP parts in the one-pass kernel's layout: each plane [Kp / 16][rows_pad][16],
+// the two 16-byte halves of a row's 32 bytes swapped on rows r with (r >> 2) & 1 (the MMA's
+// 32-byte swizzle), so a block of rows of one 16-k block is one contiguous run that lands in
+// shared memory ready to use.  64-row x 32-k tiles are staged in shared memory (read along
+// k or along rows, whichever is contiguous); each thread then converts 8 consecutive k of
+// one row and writes them to each plane as one 16-byte store, a warp covering 16 rows x 32
+// bytes of one k-block (512 contiguous bytes per plane).
+template <int NP>
+__global__ void __launch_bounds__(256) oz_slice_kblk_kernel(const z64* __restrict__ src, int64_t rows, int64_t K,
+                                                            int64_t s_row, int64_t s_k, int conj, int part0,
+                                                            int64_t rows_pad, int64_t Kp, int64_t estride,
+                                                            const int* __restrict__ emax, int* __restrict__ fexp,
+                                                            uint16_t* __restrict__ slices) {
+  __shared__ z64 tile[64][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
+  const int64_t tiles_k = Kp / 32, tiles = ((rows_pad + 63) / 64) * tiles_k;
+  const int64_t plane = rows_pad * Kp;
+  // conversion task of this thread: row rl of the tile, 8-k chunk c (warps 0..3 the first
+  // k-block of the tile, 4..7 the second; a lane pair shares a row)
+  const int rl = (ty & 3) * 16 + (tx >> 1), c = ((ty >> 2) << 1) | (tx & 1);
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_k) * 64, k0 = (t % tiles_k) * 32;
+    for (int i = ty; i < 64; i += 8) {
+      int rr, kk;
+      if (kfast) { rr = i; kk = tx; } else { rr = tx + ((i >> 5) << 5); kk = i & 31; }
+      const int64_t r = r0 + rr, k = k0 + kk;
+      tile[rr][kk] = (r < rows && k < K) ? oz_load(src, r * s_row + k * s_k, conj) : zmk(0.0, 0.0);
+    }
+    __syncthreads();
+    const int64_t r = r0 + rl;
+    if (r < rows_pad) {
+      const int64_t kb = (k0 >> 4) + (c >> 1);
+      const int64_t off = (kb * rows_pad + r) * 16 + (((c & 1) ^ (int)((r >> 2) & 1)) << 3);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const int eb = r < rows ? emax[q * estride + r] : 0;
+        if (k0 == 0 && c == 0) fexp[q * estride + r] = eb > 0 ? eb - 1023 + 1 - 7 : 0;
+        uint32_t w[OZ_S][4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          uint16_t lo[OZ_S], hi[OZ_S];
+          oz_digits(oz_part(tile[rl][c * 8 + j], part0 + q), eb, lo);
+          oz_digits(oz_part(tile[rl][c * 8 + j + 1], part0 + q), eb, hi);
+#pragma unroll
+          for (int s2 = 0; s2 < OZ_S; ++s2) w[s2][j >> 1] = (uint32_t)lo[s2] | ((uint32_t)hi[s2] << 16);
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < OZ_S; ++s2)
+          *(uint4*)(slices + (int64_t)(q * OZ_S + s2) * plane + off) = make_uint4(w[s2][0], w[s2][1], w[s2][2],
+                                                                                  w[s2][3]);
       }
     }
     __syncthreads();
@@ -962,14 +1014,14 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
     if (np == 2) oz_rowexp_kernel<2><<<g1, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, 0, emax);
     else oz_rowexp_kernel<1><<<g1, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, 0, emax);
     AGB_LAUNCH_CHECK();
-    const int64_t t2 = (rows_pad / 32) * (L.Kp / 32);
-    const int g2 = (int)(t2 < 152 * 32 ? t2 : 152 * 32);
+    const int64_t t2 = ((rows_pad + 63) / 64) * (L.Kp / 32);
+    const int g2 = (int)(t2 < 152 * 16 ? t2 : 152 * 16);
     if (np == 2)
-      oz_slice_kernel<2, true><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax,
-                                                       fexp, dst);
+      oz_slice_kblk_kernel<2><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax,
+                                                      fexp, dst);
     else
-      oz_slice_kernel<1, true><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax,
-                                                       fexp, dst);
+      oz_slice_kblk_kernel<1><<<g2, 256, 0, stream>>>(src, rows, K, s_row, s_k, conj, 0, rows_pad, L.Kp, 0, emax,
+                                                      fexp, dst);
     AGB_LAUNCH_CHECK();
     return AGB_OK;
   };
