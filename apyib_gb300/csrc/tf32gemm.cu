@@ -326,15 +326,22 @@ tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
 // The single-CTA GEMM with A converted from FP64 inside the kernel (the AO->MO quarter
 // steps, whose A is the FP64 intermediate read column by column).  A separate operand split
 // reads the intermediate and writes its TF32 planes (8.7 GB per quarter step at nbf = 150),
-// which the GEMM then reads back; here four converter warps load each 128-row x 16-k block
+// which the GEMM then reads back; here eight converter warps load each 128-row x 16-k block
 // of A straight from FP64 (coalesced along M), split it into the four planes and store them
 // into the stage in the MMA's 64-byte-swizzled K-major layout, then signal the stage.  B
-// (the small coefficient matrix) arrives by TMA from its planes as before.  Warps: 0 B loads,
-// 1 MMAs, 2-5 epilogue, 6-13 converters (thread c: row c % 128, k-half c / 128 of each
-// 16-wide block).  Three stages where they fit (64- and 160-wide tiles), so the converters
-// run ahead of the MMAs.
-constexpr int FA_THREADS = 448;
-constexpr int FA_CONV = 256;
+// (the small coefficient matrix) arrives by TMA from its planes as before.  N fits one
+// column tile, so a tile is a 128-row band of C.
+//
+// Persistent: each CTA takes bands blockIdx.x, + gridDim.x, ...; the converters and the B
+// loads run through a ring of stages that continues across bands, so the next band's
+// operands are converted while this band's epilogue drains TMEM and stores.  A band's
+// MMAs wait only until the previous band's accumulators have been read.  Warps: 0 B loads,
+// 1 MMAs, 2-9 epilogue (TMEM lane quadrant warp % 4, column half), 10-17 converters
+// (thread c: row c % 128, k-half c / 128 of each 16-wide block).  Three stages where they
+// fit (64- and 160-wide tiles).
+constexpr int FA_EPI_WARPS = 8;
+constexpr int FA_THREADS = 64 + 32 * FA_EPI_WARPS + 256;   // B loads, MMAs, epilogue, converters
+constexpr int FA_CONV0 = 64 + 32 * FA_EPI_WARPS;            // first converter thread
 template <int NB> struct FaTile {
   static constexpr int STAGES = NB == 256 ? 2 : 3;
   static constexpr int SMEM_BYTES = STAGES * Tile<NB>::STAGE_BYTES + 1024 + 256;
@@ -346,6 +353,7 @@ struct FaParams {
   int64_t sAm, sAk;
   int conjA;
   int nkb;               // 16-wide k-blocks
+  int64_t ntiles;        // 128-row bands
   z64 alpha, beta;
   z64* C;
   int64_t ldc;
@@ -365,26 +373,31 @@ tf32x3_gemm_fa_kernel(const __grid_constant__ CUtensorMap mapB, FaParams p) {
   constexpr int STAGES = FaTile<NB>::STAGES, STAGE_BYTES = Tile<NB>::STAGE_BYTES;
   constexpr int A_TILE_BYTES = Tile<NB>::A_TILE_BYTES, B_TILE_BYTES = Tile<NB>::B_TILE_BYTES;
   constexpr unsigned NCOLS = Tile<NB>::TMEM_COLS;
+  constexpr int HALF = NB / 2;               // columns per epilogue warp
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full_bar = (uint64_t*)(smem + STAGES * STAGE_BYTES);
   uint64_t* empty_bar = full_bar + STAGES;
-  uint64_t* tmem_bar = empty_bar + STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(tmem_bar + 1);
+  uint64_t* tmem_full = empty_bar + STAGES;   // MMA -> epilogue: the band's MMAs completed
+  uint64_t* tmem_empty = tmem_full + 1;       // epilogue -> MMA: the band's accumulators read (8 warps)
+  uint64_t* done_bar = tmem_empty + 1;        // MMA issuer, on abort: its MMAs completed
+  uint32_t* tmem_slot = (uint32_t*)(done_bar + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
   volatile int* conv_ok = abort_flag + 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile_n = blockIdx.x, tile_m = blockIdx.y;
   const int nk = p.nkb;
   const bool real_a = p.conjA == kSrcReal;   // no Im planes: six of the twelve MMAs, half the stores
+  const int64_t tile0 = blockIdx.x, tstep = gridDim.x;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full_bar[s], 2);      // B's expect_tx arrival + the converters' arrival
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(tmem_bar, 1);
+    mbar_init(tmem_full, 1);
+    mbar_init(tmem_empty, FA_EPI_WARPS);
+    mbar_init(done_bar, 1);
     *abort_flag = 0;
     *conv_ok = 1;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -402,24 +415,28 @@ tf32x3_gemm_fa_kernel(const __grid_constant__ CUtensorMap mapB, FaParams p) {
 
   if (warp == 0) {
     if (lane == 0) {
-      // B planes by TMA
-      int issued = 0;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-        if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) break;
-        uint8_t* st = smem + s * STAGE_BYTES;
-        mbar_expect_tx(&full_bar[s], 4 * B_TILE_BYTES);
-        for (int pl = 0; pl < 4; ++pl)
-          tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kb * BK,
-                      (int)(pl * p.rowsB + tile_n * NB));
-        issued = kb + 1;
+      // B planes by TMA, stage by stage across bands
+      long long issued = 0;
+      bool ok = true;
+      for (int64_t t = tile0; t < p.ntiles && ok; t += tstep) {
+        for (int kb = 0; kb < nk; ++kb) {
+          const int s = (int)(issued % STAGES);
+          const uint32_t ph = (uint32_t)(issued / STAGES) & 1u;
+          if (!mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 1)) {
+            ok = false;
+            break;
+          }
+          uint8_t* st = smem + s * STAGE_BYTES;
+          mbar_expect_tx(&full_bar[s], 4 * B_TILE_BYTES);
+          for (int pl = 0; pl < 4; ++pl)
+            tma_load_2d(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES, &mapB, &full_bar[s], kb * BK, (int)(pl * p.rowsB));
+          ++issued;
+        }
       }
-      if (*abort_flag) {
-        for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb) {
+      if (!ok) {
+        for (long long i = (issued > STAGES ? issued - STAGES : 0); i < issued; ++i) {
           long long t0 = clock64();
-          while (!mbar_try_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u) &&
-                 clock64() - t0 < kWaitCycles) {
+          while (!mbar_try_wait(&full_bar[i % STAGES], (uint32_t)(i / STAGES) & 1u) && clock64() - t0 < kWaitCycles) {
           }
         }
       }
@@ -428,124 +445,161 @@ tf32x3_gemm_fa_kernel(const __grid_constant__ CUtensorMap mapB, FaParams p) {
     if (lane == 0) {
       const uint32_t id_pos = make_idesc<NB>(false), id_neg = make_idesc<NB>(true);
       const uint32_t d_re = tmem_base, d_im = tmem_base + NB;
+      long long used = 0, bands = 0;
       bool ok = true;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-        if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) { ok = false; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-#pragma unroll
-        for (int ks = 0; ks < BK / 8; ++ks) {
-          uint64_t a[4], b[4];
-#pragma unroll
-          for (int pl = 0; pl < 4; ++pl) {
-            a[pl] = make_desc_sw64(st + pl * A_TILE_BYTES + ks * 32);
-            b[pl] = make_desc_sw64(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
+      for (int64_t t = tile0; t < p.ntiles && ok; t += tstep) {
+        if (bands > 0) {
+          // the epilogue must have read the previous band's accumulators
+          if (!mbar_wait(tmem_empty, (uint32_t)(bands - 1) & 1u, p.err, abort_flag, 4)) {
+            ok = false;
+            break;
           }
-          uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-          mma_tf32(d_re, a[1], b[0], id_pos, acc0);
-          mma_tf32(d_re, a[0], b[1], id_pos, 1u);
-          mma_tf32(d_re, a[0], b[0], id_pos, 1u);
-          if (!real_a) {
-            mma_tf32(d_re, a[3], b[2], id_neg, 1u);
-            mma_tf32(d_re, a[2], b[3], id_neg, 1u);
-            mma_tf32(d_re, a[2], b[2], id_neg, 1u);
-          }
-          mma_tf32(d_im, a[1], b[2], id_pos, acc0);
-          mma_tf32(d_im, a[0], b[3], id_pos, 1u);
-          mma_tf32(d_im, a[0], b[2], id_pos, 1u);
-          if (!real_a) {
-            mma_tf32(d_im, a[3], b[0], id_pos, 1u);
-            mma_tf32(d_im, a[2], b[1], id_pos, 1u);
-            mma_tf32(d_im, a[2], b[0], id_pos, 1u);
-          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         }
-        mma_commit(&empty_bar[s]);
+        for (int kb = 0; kb < nk; ++kb, ++used) {
+          const int s = (int)(used % STAGES);
+          const uint32_t ph = (uint32_t)(used / STAGES) & 1u;
+          if (!mbar_wait(&full_bar[s], ph, p.err, abort_flag, 2)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < BK / 8; ++ks) {
+            uint64_t a[4], b[4];
+#pragma unroll
+            for (int pl = 0; pl < 4; ++pl) {
+              a[pl] = make_desc_sw64(st + pl * A_TILE_BYTES + ks * 32);
+              b[pl] = make_desc_sw64(st + 4 * A_TILE_BYTES + pl * B_TILE_BYTES + ks * 32);
+            }
+            uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
+            mma_tf32(d_re, a[1], b[0], id_pos, acc0);
+            mma_tf32(d_re, a[0], b[1], id_pos, 1u);
+            mma_tf32(d_re, a[0], b[0], id_pos, 1u);
+            if (!real_a) {
+              mma_tf32(d_re, a[3], b[2], id_neg, 1u);
+              mma_tf32(d_re, a[2], b[3], id_neg, 1u);
+              mma_tf32(d_re, a[2], b[2], id_neg, 1u);
+            }
+            mma_tf32(d_im, a[1], b[2], id_pos, acc0);
+            mma_tf32(d_im, a[0], b[3], id_pos, 1u);
+            mma_tf32(d_im, a[0], b[2], id_pos, 1u);
+            if (!real_a) {
+              mma_tf32(d_im, a[3], b[0], id_pos, 1u);
+              mma_tf32(d_im, a[2], b[1], id_pos, 1u);
+              mma_tf32(d_im, a[2], b[0], id_pos, 1u);
+            }
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        if (!ok) break;
+        mma_commit(tmem_full);
+        ++bands;
       }
-      if (ok) mma_commit(tmem_bar);
+      if (!ok) {
+        // the MMAs issued so far complete before TMEM is freed
+        mma_commit(done_bar);
+        long long t0 = clock64();
+        while (!mbar_try_wait(done_bar, 0u) && clock64() - t0 < kWaitCycles) {
+        }
+      }
     }
-  } else if (warp >= 6) {
-    // converters: thread c owns row c % 128 of the tile and half (8 k) of each k-block
-    const int c = threadIdx.x - 192;
+  } else if (threadIdx.x >= FA_CONV0) {
+    // converters: thread c owns row c % 128 of the band and half (8 k) of each k-block
+    const int c = threadIdx.x - FA_CONV0;
     const int row = c & 127, kh = c >> 7;
-    const int64_t m = (int64_t)tile_m * BM + row;
-    const bool live = m < p.M;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (c == 0) *conv_ok = mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 5) ? 1 : 0;
-      asm volatile("bar.sync 1, 256;" ::: "memory");   // the eight converter warps; c == 0's wait is bounded
-      if (!*conv_ok) break;
-      z64 v[BK / 2];
+    long long it = 0;
+    bool ok = true;
+    for (int64_t t = tile0; t < p.ntiles && ok; t += tstep) {
+      const int64_t m = t * BM + row;
+      const bool live = m < p.M;
+      for (int kb = 0; kb < nk; ++kb, ++it) {
+        const int s = (int)(it % STAGES);
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+        if (c == 0) *conv_ok = mbar_wait(&empty_bar[s], ph ^ 1u, p.err, abort_flag, 5) ? 1 : 0;
+        asm volatile("bar.sync 1, 256;" ::: "memory");   // the eight converter warps; c == 0's wait is bounded
+        if (!*conv_ok) {
+          ok = false;
+          break;
+        }
+        z64 v[BK / 2];
 #pragma unroll
-      for (int kk = 0; kk < BK / 2; ++kk) {
-        const int64_t k = (int64_t)kb * BK + kh * (BK / 2) + kk;
-        v[kk] = zmk(0, 0);
-        if (live && k < p.K) {
-          if (p.conjA == kSrcReal) {
-            v[kk].x = ((const double*)p.A)[m * p.sAm + k * p.sAk];
-          } else {
-            v[kk] = p.A[m * p.sAm + k * p.sAk];
-            if (p.conjA == 1) v[kk].y = -v[kk].y;
+        for (int kk = 0; kk < BK / 2; ++kk) {
+          const int64_t k = (int64_t)kb * BK + kh * (BK / 2) + kk;
+          v[kk] = zmk(0, 0);
+          if (live && k < p.K) {
+            if (p.conjA == kSrcReal) {
+              v[kk].x = ((const double*)p.A)[m * p.sAm + k * p.sAk];
+            } else {
+              v[kk] = p.A[m * p.sAm + k * p.sAk];
+              if (p.conjA == 1) v[kk].y = -v[kk].y;
+            }
           }
         }
-      }
-      uint8_t* st = smem + s * STAGE_BYTES;
+        uint8_t* st = smem + s * STAGE_BYTES;
 #pragma unroll
-      for (int cl = 0; cl < BK / 8; ++cl) {
-        const int ch = kh * (BK / 8) + cl;          // 16-byte chunk of the row
-        float4 rh, rl, ih, il;
-        float* prh = &rh.x;
-        float* prl = &rl.x;
-        float* pih = &ih.x;
-        float* pil = &il.x;
+        for (int cl = 0; cl < BK / 8; ++cl) {
+          const int ch = kh * (BK / 8) + cl;          // 16-byte chunk of the row
+          float4 rh, rl, ih, il;
+          float* prh = &rh.x;
+          float* prl = &rl.x;
+          float* pih = &ih.x;
+          float* pil = &il.x;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          uint32_t a0, a1, b0, b1;
-          const z64 x = v[4 * cl + u];
-          split_tf32_fast((uint32_t)__double2hiint(x.x), (uint32_t)__double2loint(x.x), a0, a1);
-          split_tf32_fast((uint32_t)__double2hiint(x.y), (uint32_t)__double2loint(x.y), b0, b1);
-          prh[u] = __uint_as_float(a0);
-          prl[u] = __uint_as_float(a1);
-          pih[u] = __uint_as_float(b0);
-          pil[u] = __uint_as_float(b1);
+          for (int u = 0; u < 4; ++u) {
+            uint32_t a0, a1, b0, b1;
+            const z64 x = v[4 * cl + u];
+            split_tf32_fast((uint32_t)__double2hiint(x.x), (uint32_t)__double2loint(x.x), a0, a1);
+            split_tf32_fast((uint32_t)__double2hiint(x.y), (uint32_t)__double2loint(x.y), b0, b1);
+            prh[u] = __uint_as_float(a0);
+            prl[u] = __uint_as_float(a1);
+            pih[u] = __uint_as_float(b0);
+            pil[u] = __uint_as_float(b1);
+          }
+          const uint32_t off = sw64_chunk_off(row, ch);
+          *(float4*)(st + off) = rh;
+          *(float4*)(st + A_TILE_BYTES + off) = rl;
+          if (!real_a) {
+            *(float4*)(st + 2 * A_TILE_BYTES + off) = ih;
+            *(float4*)(st + 3 * A_TILE_BYTES + off) = il;
+          }
         }
-        const uint32_t off = sw64_chunk_off(row, ch);
-        *(float4*)(st + off) = rh;
-        *(float4*)(st + A_TILE_BYTES + off) = rl;
-        if (!real_a) {
-          *(float4*)(st + 2 * A_TILE_BYTES + off) = ih;
-          *(float4*)(st + 3 * A_TILE_BYTES + off) = il;
-        }
+        // the generic-proxy stores must be visible to the tensor core's (async-proxy) reads
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        if (c == 0) mbar_arrive(&full_bar[s]);
       }
-      // the generic-proxy stores must be visible to the tensor core's (async-proxy) reads
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      if (c == 0) mbar_arrive(&full_bar[s]);
     }
   } else {
-    // epilogue warps 2..5: TMEM lane quadrant q = warp % 4
-    const int q = warp & 3;
-    const int64_t m = (int64_t)tile_m * BM + q * 32 + lane;
-    int okw = 0;
-    if (lane == 0) okw = mbar_wait(tmem_bar, 0, p.err, abort_flag, 3) ? 1 : 0;
-    const bool ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok && nk > 0) {
-      const bool use_beta = (p.beta.x != 0.0 || p.beta.y != 0.0);
-      const bool unit_alpha = p.alpha.x == 1.0 && p.alpha.y == 0.0;
+    // epilogue warps 2..9: TMEM lane quadrant q = warp % 4, column half h
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const bool use_beta = (p.beta.x != 0.0 || p.beta.y != 0.0);
+    const bool unit_alpha = p.alpha.x == 1.0 && p.alpha.y == 0.0;
+    long long bands = 0;
+    for (int64_t t = tile0; t < p.ntiles; t += tstep, ++bands) {
+      int okw = 0;
+      if (lane == 0) okw = mbar_wait(tmem_full, (uint32_t)bands & 1u, p.err, abort_flag, 3) ? 1 : 0;
+      if (__shfl_sync(0xffffffffu, okw, 0) == 0) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int64_t m = t * BM + q * 32 + lane;
 #pragma unroll 1
-      for (int cc = 0; cc < NB / 32; ++cc) {
-        float vr[32], vi[32];
-        uint32_t tl = tmem_base + ((uint32_t)(q * 32) << 16) + cc * 32;
-        tmem_ld32(tl, vr);
-        tmem_ld32(tl + NB, vi);
+      for (int cc = 0; cc < HALF / 16; ++cc) {
+        float vr[16], vi[16];
+        const uint32_t tl = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * HALF + cc * 16);
+        tmem_ld16(tl, vr);
+        tmem_ld16(tl + NB, vi);
+        if (cc == HALF / 16 - 1) {
+          // the band's accumulators are in registers: the next band's MMAs may start
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(tmem_empty);
+        }
         if (m < p.M) {
-          const int64_t n0 = (int64_t)tile_n * NB + cc * 32;
+          const int64_t n0 = (int64_t)h * HALF + cc * 16;
           z64* dst = p.C + m * p.ldc + n0;
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
+          for (int j = 0; j < 16; ++j) {
             if (n0 + j < p.N) {
               z64 out = zmk(f2d_exact(vr[j]), f2d_exact(vi[j]));
               if (!unit_alpha) out = zmul(p.alpha, out);
@@ -1044,7 +1098,6 @@ agb_status cgemm_tf32x3_fa(int64_t M, int64_t N, int64_t K, z64 alpha, const z64
     return AGB_ERR_WORKSPACE;
   }
   const int64_t Mp = round_up(M, BM), Np = tf32_rows_pad(N), Kp = tf32_k_pad(K);
-  AGB_ARG_CHECK(Mp / BM <= 65535, "cgemm_tf32x3_fa: M too large for the grid");
   char* base = (char*)scratch;
   float* PB = (float*)(base + 256);
   AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream, 0));
@@ -1054,20 +1107,20 @@ agb_status cgemm_tf32x3_fa(int64_t M, int64_t N, int64_t K, z64 alpha, const z64
     agb_set_error_message("cgemm_tf32x3_fa: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
-  static bool attr_set = false;
-  if (!attr_set) {
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_fa_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      FaTile<64>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_fa_kernel<160>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      FaTile<160>::SMEM_BYTES));
-    AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_fa_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      FaTile<256>::SMEM_BYTES));
-    attr_set = true;
-  }
+  AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_fa_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    FaTile<64>::SMEM_BYTES));
+  AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_fa_kernel<160>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    FaTile<160>::SMEM_BYTES));
+  AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_fa_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    FaTile<256>::SMEM_BYTES));
   FaParams p;
   p.M = M; p.N = N; p.K = K; p.A = A; p.sAm = sAm; p.sAk = sAk; p.conjA = conjA; p.nkb = (int)(Kp / BK);
+  p.ntiles = Mp / BM;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.err = (int*)base; p.rowsB = Np;
-  const dim3 grid((unsigned)((N + nb - 1) / nb), (unsigned)(Mp / BM));
+  int dev = 0, nsm = 0;
+  AGB_CUDA_TRY(cudaGetDevice(&dev));
+  AGB_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const unsigned grid = (unsigned)(p.ntiles < nsm ? p.ntiles : nsm);   // one persistent CTA per SM
   if (nb == 64) tf32x3_gemm_fa_kernel<64><<<grid, FA_THREADS, FaTile<64>::SMEM_BYTES, stream>>>(mB, p);
   else if (nb == 160) tf32x3_gemm_fa_kernel<160><<<grid, FA_THREADS, FaTile<160>::SMEM_BYTES, stream>>>(mB, p);
   else tf32x3_gemm_fa_kernel<256><<<grid, FA_THREADS, FaTile<256>::SMEM_BYTES, stream>>>(mB, p);
