@@ -514,6 +514,90 @@ __global__ void __launch_bounds__(256) oz_slice_kblk_kernel(const z64* __restric
   }
 }
 
+// K (padded) up to which the one-pass kernel's operands are sliced in one read: 32 whole
+// rows fit in shared memory (32 x 193 x 16 bytes at most).
+constexpr int64_t kOzFusedMaxK = 192;
+
+// Row exponents and slices of NP parts in one read of the source, for short K, in the
+// layout of oz_slice_kblk_kernel: a block stages 32 whole rows (all Kp k) in shared memory,
+// takes each row's largest exponent over its parts (one exponent shared by them; the row
+// scale f_r goes to fexp), then converts 8 consecutive k of a row per thread and writes
+// each plane with one 16-byte store.  Against a separate exponent pass this saves one
+// read of the operand.
+template <int NP>
+__global__ void __launch_bounds__(256) oz_slice_fused_kernel(const z64* __restrict__ src, int64_t rows, int64_t K,
+                                                             int64_t s_row, int64_t s_k, int conj, int64_t rows_pad,
+                                                             int64_t Kp, int* __restrict__ fexp,
+                                                             uint16_t* __restrict__ slices) {
+  extern __shared__ __align__(16) uint8_t fused_smem[];
+  z64* rowbuf = (z64*)fused_smem;                       // [32][Kp + 1]
+  __shared__ int rexp[32];
+  const int kp = (int)Kp, ld = kp + 1;
+  const bool kfast = (s_k == 1) || (s_row != 1 && s_k <= s_row);
+  const int64_t blocks = rows_pad / 32, plane = rows_pad * Kp;
+  const int ntask = 32 * (kp / 8);                       // (row, 8-k chunk) pairs of a block
+  for (int64_t b = blockIdx.x; b < blocks; b += gridDim.x) {
+    const int64_t r0 = b * 32;
+    for (int idx = threadIdx.x; idx < 32 * kp; idx += 256) {
+      int rr, kk;
+      if (kfast) {
+        rr = idx / kp;
+        kk = idx - rr * kp;
+      } else {
+        kk = idx >> 5;
+        rr = idx & 31;
+      }
+      const int64_t r = r0 + rr;
+      rowbuf[rr * ld + kk] = (r < rows && kk < K) ? oz_load(src, r * s_row + kk * s_k, conj) : zmk(0.0, 0.0);
+    }
+    __syncthreads();
+    {
+      // largest biased exponent of each row over its parts: 8 lanes per row
+      const int rr = threadIdx.x >> 3, part = threadIdx.x & 7;
+      int e = 0;
+      for (int kk = part; kk < kp; kk += 8) {
+        const z64 v = rowbuf[rr * ld + kk];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) e = max(e, oz_bexp(oz_part(v, q)));
+      }
+      e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+      e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+      e = max(e, __shfl_xor_sync(0xffffffffu, e, 4));
+      if (part == 0) {
+        rexp[rr] = r0 + rr < rows ? e : 0;
+        fexp[r0 + rr] = (r0 + rr < rows && e > 0) ? e - 1023 + 1 - 7 : 0;
+      }
+    }
+    __syncthreads();
+    // task t: k-block t / 64, row (t % 64) / 2, 8-k half t % 2 of the block, so a warp
+    // writes 16 rows x 32 bytes of one k-block per plane
+    for (int t = threadIdx.x; t < ntask; t += 256) {
+      const int kb = t >> 6, rr = (t & 63) >> 1, hh = t & 1;
+      const int64_t r = r0 + rr;
+      const int eb = rexp[rr];
+      const int64_t off = ((int64_t)kb * rows_pad + r) * 16 + ((hh ^ (int)((r >> 2) & 1)) << 3);
+      const z64* x = rowbuf + rr * ld + kb * 16 + hh * 8;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        uint32_t w[OZ_S][4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          uint16_t lo[OZ_S], hi[OZ_S];
+          oz_digits(oz_part(x[j], q), eb, lo);
+          oz_digits(oz_part(x[j + 1], q), eb, hi);
+#pragma unroll
+          for (int s2 = 0; s2 < OZ_S; ++s2) w[s2][j >> 1] = (uint32_t)lo[s2] | ((uint32_t)hi[s2] << 16);
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < OZ_S; ++s2)
+          *(uint4*)(slices + (int64_t)(q * OZ_S + s2) * plane + off) = make_uint4(w[s2][0], w[s2][1], w[s2][2],
+                                                                                  w[s2][3]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // One-pass complex Ozaki GEMM for short K (4M, Re and Im accumulated side by side).
 //
@@ -1008,6 +1092,24 @@ agb_status ozc_gemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, in
   // both parts of an operand from one read, under one exponent per row (estride 0)
   auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int np, int64_t rows_pad,
                    int* emax, int* fexp, uint16_t* dst) -> agb_status {
+    if (L.Kp <= kOzFusedMaxK) {
+      // one read: exponents and slices of 32 whole rows per block
+      const size_t sh = (size_t)32 * (L.Kp + 1) * sizeof(z64);
+      const int per_sm = (int)((227 * 1024) / (sh + 1024));
+      const int64_t blocks = rows_pad / 32, cap = (int64_t)152 * (per_sm > 0 ? per_sm : 1);
+      const int g = (int)(blocks < cap ? blocks : cap);
+      if (np == 2) {
+        AGB_CUDA_TRY(cudaFuncSetAttribute(oz_slice_fused_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)sh));
+        oz_slice_fused_kernel<2><<<g, 256, sh, stream>>>(src, rows, K, s_row, s_k, conj, rows_pad, L.Kp, fexp, dst);
+      } else {
+        AGB_CUDA_TRY(cudaFuncSetAttribute(oz_slice_fused_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)sh));
+        oz_slice_fused_kernel<1><<<g, 256, sh, stream>>>(src, rows, K, s_row, s_k, conj, rows_pad, L.Kp, fexp, dst);
+      }
+      AGB_LAUNCH_CHECK();
+      return AGB_OK;
+    }
     AGB_CUDA_TRY(cudaMemsetAsync(emax, 0, (size_t)rows_pad * 4, stream));
     const int64_t t1 = ((rows + 31) / 32) * ((K + 31) / 32);
     const int g1 = (int)(t1 < 152 * 32 ? t1 : 152 * 32);
