@@ -77,8 +77,8 @@ SIGNATURES = {
     "agb_zgemm_batched": (_int, [_i64, _i64, _i64, _i64, _d, _d, _vp, _i64, _i64, _i64, _int, _vp, _i64, _i64, _i64,
                                  _int, _d, _d, _vp, _i64, _i64, _vp]),
     "agb_zdet_inv_batched": (_int, [_i64, _int, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _vp]),
-    "agb_gemm_timing_enable": (None, [_int]),
-    "agb_gemm_timing_collect": (_int, [_d, _c.POINTER(_int), _c.POINTER(_d), _c.POINTER(_d)]),
+    "agb_cisd_plan_gemm_timing": (_int, [_vp, _int]),
+    "agb_cisd_plan_gemm_timing_collect": (_int, [_vp, _d, _c.POINTER(_int), _c.POINTER(_d), _c.POINTER(_d)]),
     "agb_compute_f_so": (_int, [_vp, _i64, _vp, _vp]),
     "agb_compute_eri_so": (_int, [_vp, _i64, _i64, _i64, _i64, _vp, _vp]),
     "agb_cisd_plan_create": (_int, [_int, _int, _int, _c.POINTER(_vp)]),

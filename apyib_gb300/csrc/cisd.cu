@@ -52,7 +52,7 @@ agb_status tf32_prep_planes(const z64* src, int64_t rows, int64_t K, int64_t s_r
                             float* dst, cudaStream_t stream, int kblk);
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
                             z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
-                            int trans_c, int kblkA, int kblkB, int c32);
+                            int trans_c, int kblkA, int kblkB, int c32, GemmTimingLog* timing);
 
 namespace {
 
@@ -981,7 +981,8 @@ agb_status gemm(agb_cisd_plan* P, int prec, int64_t M, int64_t N, int64_t K, z64
       return AGB_ERR_WORKSPACE;
     }
     return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + off),
-                            P->gemm_scratch_bytes - off, st, trans_c, kblk, kblk, c32);
+                            P->gemm_scratch_bytes - off, st, trans_c, kblk, kblk, c32,
+                            P->gemm_timing ? &P->gemm_timing_log : nullptr);
   }
   if (trans_c) return gemm(P, prec, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, ldc, st);
   if (prec == AGB_PREC_OZAKI && ozgemm_tiles(M, N) >= kOzMinTiles)
@@ -1077,8 +1078,48 @@ agb_status agb_cisd_plan_create(int o, int v, int flags, agb_cisd_plan** plan) {
 }
 
 agb_status agb_cisd_plan_destroy(agb_cisd_plan* plan) {
+  if (plan)
+    for (auto& r : plan->gemm_timing_log) {
+      cudaEventDestroy(r.e0);
+      cudaEventDestroy(r.e1);
+    }
   delete plan;
   return AGB_OK;
+}
+
+agb_status agb_cisd_plan_gemm_timing(agb_cisd_plan* plan, int on) {
+  AGB_ARG_CHECK(plan != nullptr, "gemm_timing: null plan");
+  plan->gemm_timing = on != 0;
+  return AGB_OK;
+}
+
+agb_status agb_cisd_plan_gemm_timing_collect(agb_cisd_plan* plan, double min_mnk, int* launches, double* ms,
+                                             double* flops) {
+  AGB_ARG_CHECK(plan != nullptr, "gemm_timing_collect: null plan");
+  int n = 0;
+  double tms = 0, tfl = 0;
+  agb_status st = AGB_OK;
+  for (auto& r : plan->gemm_timing_log) {
+    if (st == AGB_OK && cudaEventSynchronize(r.e1) == cudaSuccess) {
+      if ((double)r.M * (double)r.N * (double)r.K >= min_mnk) {
+        float e = 0;
+        if (cudaEventElapsedTime(&e, r.e0, r.e1) != cudaSuccess) st = AGB_ERR_CUDA;
+        ++n;
+        tms += e;
+        tfl += r.flops;
+      }
+    } else if (st == AGB_OK) {
+      agb_set_error_message("gemm_timing_collect: event synchronisation failed", __FILE__, __LINE__);
+      st = AGB_ERR_CUDA;
+    }
+    cudaEventDestroy(r.e0);
+    cudaEventDestroy(r.e1);
+  }
+  plan->gemm_timing_log.clear();
+  if (launches) *launches = n;
+  if (ms) *ms = tms;
+  if (flops) *flops = tfl;
+  return st;
 }
 
 agb_status agb_cisd_plan_workspace_bytes(const agb_cisd_plan* plan, size_t* bytes) {

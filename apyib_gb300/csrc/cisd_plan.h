@@ -38,4 +38,7 @@ struct agb_cisd_plan {
         *P_Wovoo = nullptr, *P_Wvvvo = nullptr;
   void* gemm_scratch;                 // 3xTF32 operand planes
   size_t gemm_scratch_bytes;
+  // benchmark instrumentation: events around this plan's tcgen05 GEMM launches while on
+  bool gemm_timing = false;
+  agb::GemmTimingLog gemm_timing_log;
 };

@@ -4,11 +4,22 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <vector>
+
 #include "../../include/apyib_gb300.h"
 
 namespace agb {
 
 typedef double2 z64;   // complex double, interleaved (re, im)
+
+// Benchmark instrumentation a plan keeps for itself: CUDA events bracketing each of its
+// tcgen05 GEMM launches on the launch stream, with the launch's shape.
+struct GemmTimingRec {
+  cudaEvent_t e0, e1;
+  double flops;          // 8 M N K
+  int64_t M, N, K;
+};
+typedef std::vector<GemmTimingRec> GemmTimingLog;
 
 // Operand-conjugation flag of the internal split kernels: 0 as stored, 1 conjugated,
 // kSrcReal the operand is a real FP64 array (same strides, in doubles; imaginary part zero).

@@ -17,10 +17,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
-#include <atomic>
 #include <cstdlib>
-#include <mutex>
-#include <vector>
 
 #include "common.cuh"
 #include "dfloat.cuh"
@@ -41,17 +38,6 @@ PFN_cuTensorMapEncodeTiled_v12000 tma_encode_fn() {
   }
   return fn;
 }
-
-// Optional per-launch timing of the tensor-core kernel (CUDA events recorded on
-// the launch stream around the GEMM kernel alone; diagnostics for benchmarks).
-struct TimingRec {
-  cudaEvent_t e0, e1;
-  double flops;
-  int64_t M, N, K;
-};
-static std::atomic<int> g_timing{0};
-static std::mutex g_timing_mu;
-static std::vector<TimingRec> g_timing_recs;
 
 agb_status zgemm(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, int64_t sAm, int64_t sAk, int conjA,
                  const z64* B, int64_t sBk, int64_t sBn, int conjB, z64 beta, z64* C, int64_t ldc,
@@ -1009,10 +995,11 @@ size_t tf32_partials_bytes(int64_t M, int64_t N, int64_t K) {
 // trans_c: C(m, n) lives at C[n * ldc + m] (the output written column by column, which keeps
 // the stores of an output with a short row extent coalesced).
 // kblkA / kblkB: that operand's planes are K-blocked (single-CTA kernel only).  c32: C holds
-// complex FP32 values (ldc in float2 units), alpha = 1, beta 0 or 1, no K split.
+// complex FP32 values (ldc in float2 units), alpha = 1, beta 0 or 1, no K split.  timing:
+// when not null, CUDA events around the GEMM kernel are appended to it (the caller's log).
 agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const float* PA, const float* PB, z64 beta,
                             z64* C, int64_t ldc, int* err, z64* partials, size_t partial_bytes, cudaStream_t stream,
-                            int trans_c, int kblkA, int kblkB, int c32) {
+                            int trans_c, int kblkA, int kblkB, int c32, GemmTimingLog* timing) {
   AGB_ARG_CHECK(M >= 0 && N >= 0 && K > 0, "tf32_gemm_planes: bad size");
   if (M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(PA && PB && C && err, "tf32_gemm_planes: null pointer");
@@ -1052,7 +1039,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   p.rowsA = Mp; p.rowsB = Np; p.trans_c = trans_c; p.kblkA = kblkA; p.kblkB = kblkB; p.c32 = c32;
   dim3 grid((unsigned)(round_up(N, nb) / nb), (unsigned)(round_up(M, BM) / BM), (unsigned)splits);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  if (g_timing.load(std::memory_order_relaxed)) {
+  if (timing) {
     AGB_CUDA_TRY(cudaEventCreate(&ev0));
     AGB_CUDA_TRY(cudaEventCreate(&ev1));
     AGB_CUDA_TRY(cudaEventRecord(ev0, stream));
@@ -1069,8 +1056,7 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
   AGB_LAUNCH_CHECK();
   if (ev0) {
     AGB_CUDA_TRY(cudaEventRecord(ev1, stream));
-    std::lock_guard<std::mutex> lk(g_timing_mu);
-    g_timing_recs.push_back(TimingRec{ev0, ev1, 8.0 * (double)M * (double)N * (double)K, M, N, K});
+    timing->push_back(GemmTimingRec{ev0, ev1, 8.0 * (double)M * (double)N * (double)K, M, N, K});
   }
   if (splits > 1) {
     splitk_sum_kernel<<<grid_for(M * N, 256), 256, 0, stream>>>(partials, splits, M, N, alpha, beta, C, ldc,
@@ -1156,7 +1142,7 @@ agb_status cgemm_tf32x3(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A
   AGB_STATUS_TRY(tf32_prep_planes(B, N, K, sBn, sBk, conjB, PB, stream, 0));
   size_t used = 256 + a_bytes + b_bytes;
   return tf32_gemm_planes(M, N, K, alpha, PA, PB, beta, C, ldc, (int*)base, (z64*)(base + used),
-                          scratch_bytes - used, stream, 0, 0, 0, 0);
+                          scratch_bytes - used, stream, 0, 0, 0, 0, nullptr);
 }
 
 }  // namespace agb
@@ -1175,33 +1161,6 @@ agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, do
                            scratch, scratch_bytes, (cudaStream_t)stream);
 }
 
-void agb_gemm_timing_enable(int on) { agb::g_timing.store(on ? 1 : 0); }
-
-/* Synchronises the recorded events and reports, for tcgen05 GEMM launches whose
- * M*N*K >= min_mnk: launch count, summed kernel milliseconds and summed algorithmic
- * flops (8*M*N*K); then clears the records. */
-agb_status agb_gemm_timing_collect(double min_mnk, int* launches, double* ms, double* flops) {
-  std::lock_guard<std::mutex> lk(agb::g_timing_mu);
-  int n = 0;
-  double tms = 0, tfl = 0;
-  for (auto& r : agb::g_timing_recs) {
-    AGB_CUDA_TRY(cudaEventSynchronize(r.e1));
-    if ((double)r.M * (double)r.N * (double)r.K >= min_mnk) {
-      float e = 0;
-      AGB_CUDA_TRY(cudaEventElapsedTime(&e, r.e0, r.e1));
-      ++n;
-      tms += e;
-      tfl += r.flops;
-    }
-    cudaEventDestroy(r.e0);
-    cudaEventDestroy(r.e1);
-  }
-  agb::g_timing_recs.clear();
-  if (launches) *launches = n;
-  if (ms) *ms = tms;
-  if (flops) *flops = tfl;
-  return AGB_OK;
-}
 
 /* Reads and clears the error word a 3xTF32 GEMM keeps at the start of its scratch
  * (non-zero: a bounded wait inside the kernel ran out). Synchronises the stream. */

@@ -798,7 +798,7 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    lib.agb_gemm_timing_enable(1)
+    _lib.call("agb_cisd_plan_gemm_timing", plan._h, 1)
     n0 = lib.agb_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
@@ -807,11 +807,12 @@ def main():
     ev1.record()
     torch.cuda.synchronize()
     launches = lib.agb_launch_count() - n0
-    lib.agb_gemm_timing_enable(0)
+    _lib.call("agb_cisd_plan_gemm_timing", plan._h, 0)
     nl, kms, kfl = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
     pq = (o * (o - 1) // 2) * (v * (v - 1) // 2) ** 2       # vvvv ladder M*N*K
     ring = float(o * v) ** 3
-    _lib.call("agb_gemm_timing_collect", min(pq, ring) * 0.99, ctypes.byref(nl), ctypes.byref(kms), ctypes.byref(kfl))
+    _lib.call("agb_cisd_plan_gemm_timing_collect", plan._h, min(pq, ring) * 0.99, ctypes.byref(nl), ctypes.byref(kms),
+              ctypes.byref(kfl))
     plan.check_status()
     dev_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist)
     clocks = sampler.stop()

@@ -139,12 +139,6 @@ agb_status agb_zgemm_batched(int64_t batch, int64_t M, int64_t N, int64_t K, dou
 agb_status agb_zdet_inv_batched(int64_t batch, int n, const void* A, int64_t lda, int64_t sAb, void* Ainv,
                                 int64_t ldi, int64_t sIb, void* det, int* info, void* stream);
 
-/* Benchmark instrumentation (no reference counterpart): when enabled, every
- * tcgen05 GEMM launch is bracketed by CUDA events on its stream;
- * agb_gemm_timing_collect reports launches, kernel milliseconds and
- * algorithmic flops (8*M*N*K) of launches with M*N*K >= min_mnk, then clears. */
-void agb_gemm_timing_enable(int on);
-agb_status agb_gemm_timing_collect(double min_mnk, int* launches, double* ms, double* flops);
 
 /* Reads and clears the status word a 3xTF32 GEMM keeps in the first bytes of its
  * scratch (zero it once before first use): AGB_ERR_TIMEOUT if a bounded
@@ -177,6 +171,14 @@ agb_status agb_cisd_plan_workspace_bytes(const agb_cisd_plan* plan, size_t* byte
 agb_status agb_cisd_plan_set_workspace(agb_cisd_plan* plan, void* workspace, size_t bytes);
 /* Sizes of the packed amplitude vector [t1 (o*v) | t2 (o(o-1)/2 * v(v-1)/2)]. */
 agb_status agb_cisd_plan_sizes(const agb_cisd_plan* plan, int64_t* n1, int64_t* n2);
+/* Benchmark instrumentation kept by the plan (no reference counterpart): while on, each
+ * tcgen05 GEMM launch of the plan's residuals is bracketed by CUDA events on its stream.
+ * _collect synchronises the recorded events, reports the launch count, summed kernel
+ * milliseconds and algorithmic flops (8*M*N*K) of the launches with M*N*K >= min_mnk,
+ * and clears the record.  Like every plan call, not for concurrent use on one plan. */
+agb_status agb_cisd_plan_gemm_timing(agb_cisd_plan* plan, int on);
+agb_status agb_cisd_plan_gemm_timing_collect(agb_cisd_plan* plan, double min_mnk, int* launches, double* ms,
+                                             double* flops);
 
 /* Fock matrix (full spin-orbital F_SO, nso x nso) and SO orbital energies
  * eps_so (nso doubles, occupied first) used for the denominators

@@ -169,3 +169,38 @@ def test_tf32x3_residual_tracks_fp64(o, v, offdiag):
         ref = r64[part]
         err = (r32[part] - ref).abs().max().item() / ref.abs().max().item()
         assert err < 2e-5, err
+
+
+def test_plan_gemm_timing_is_per_plan():
+    """The GEMM timing log belongs to the plan that switched it on: a 3xTF32 residual
+    records its tcgen05 launches there and nowhere else, and collecting clears it."""
+    import ctypes
+    o, v = 20, 80
+    prob = synthetic.so_factors(o, v, seed=3)
+    eps_so = np.concatenate([np.repeat(prob.eps_o, 2), np.repeat(prob.eps_v, 2)])
+    plans = []
+    for _ in range(2):
+        plan = CISDPlan(o, v, mixed=True)
+        plan.set_fock(torch.as_tensor(prob.fock_so()), eps_so)
+        plan.blocks_from_factors(torch.as_tensor(prob.B))
+        plans.append(plan)
+    timed, other = plans
+    _lib.call("agb_cisd_plan_gemm_timing", timed._h, 1)
+    t = timed.guess()
+    E0, _, _ = timed.combine([t], [1.0], t, t)
+    timed.residual(t, E0, _lib.PREC_TF32X3)
+    other.residual(t, E0, _lib.PREC_TF32X3)
+    _lib.call("agb_cisd_plan_gemm_timing", timed._h, 0)
+
+    def collect(plan):
+        n, ms, fl = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        _lib.call("agb_cisd_plan_gemm_timing_collect", plan._h, 0.0, ctypes.byref(n), ctypes.byref(ms),
+                  ctypes.byref(fl))
+        return n.value, ms.value, fl.value
+
+    n, ms, fl = collect(timed)
+    assert n > 0 and ms > 0.0 and fl >= 8.0 * (o * v) ** 3       # at least the ring product
+    assert collect(timed) == (0, 0.0, 0.0)                       # cleared
+    assert collect(other) == (0, 0.0, 0.0)                       # never switched on
+    for plan in plans:
+        plan.check_status()
