@@ -10,6 +10,10 @@
  * <pq||rs> = (pr|qs) - (ps|qr).  No entry point allocates device memory
  * except agb_cisd_plan_create (host memory for the plan object only);
  * device workspace is sized by the library and owned by the caller.
+ * Mutable state lives in the caller's plan and workspace; what the library keeps
+ * for the whole process is the last error message (one per host thread), an atomic
+ * count of kernel launches (agb_launch_count, diagnostics) and the small device
+ * array of agb_vec_dots_noalloc (see there).  A plan is used by one caller at a time.
  *
  * Reference cross-walk (apyib project paths):
  *   agb_zgemm / agb_cgemm_tf32x3   opt_einsum contractions of apyib/ci_wfn.py:309-334
