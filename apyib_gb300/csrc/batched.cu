@@ -212,12 +212,12 @@ agb_status agb_zdet_inv_batched(int64_t batch, int n, const void* A, int64_t lda
   AGB_ARG_CHECK(A && Ainv && det, "zdet_inv_batched: null pointer");
   AGB_ARG_CHECK(batch <= 2147483647LL && lda >= n && ldi >= n, "zdet_inv_batched: bad batch or leading dimension");
   const size_t smem = sizeof(z64) * (size_t)n * n + sizeof(int) * (size_t)n;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::atomic<uint64_t> attr_done{0};
+  AGB_STATUS_TRY(once_per_device(attr_done, [&]() -> agb_status {
     AGB_CUDA_TRY(cudaFuncSetAttribute(det_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(sizeof(z64) * kDetInvMaxN * kDetInvMaxN + sizeof(int) * kDetInvMaxN)));
-    attr_set = true;
-  }
+    return AGB_OK;
+  }));
   det_inv_kernel<<<(unsigned)batch, 256, smem, (cudaStream_t)stream>>>(n, (const z64*)A, lda, sAb, (z64*)Ainv, ldi, sIb,
                                                                        (z64*)det, info);
   AGB_LAUNCH_CHECK();

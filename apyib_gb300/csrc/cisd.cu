@@ -1469,21 +1469,26 @@ typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
 // the thread yet (the runtime binds the device's primary context at its first call that
 // needs one, e.g. cudaGetSymbolAddress) or the driver cannot tell.
 bool current_context_id(unsigned long long* id) {
-  static PfnCtxGetCurrent get_cur = nullptr;
-  static PfnCtxGetId get_id = nullptr;
-  static bool looked_up = false;
-  if (!looked_up) {
+  struct Fns {
+    PfnCtxGetCurrent get_cur = nullptr;
+    PfnCtxGetId get_id = nullptr;
+  };
+  // looked up once, by the first caller (a function-local static is initialised exactly once)
+  static const Fns fns = [] {
+    Fns r;
     cudaDriverEntryPointQueryResult q;
     void* f = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      get_cur = (PfnCtxGetCurrent)f;
+      r.get_cur = (PfnCtxGetCurrent)f;
     f = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      get_id = (PfnCtxGetId)f;
-    looked_up = true;
-  }
+      r.get_id = (PfnCtxGetId)f;
+    return r;
+  }();
+  const PfnCtxGetCurrent get_cur = fns.get_cur;
+  const PfnCtxGetId get_id = fns.get_id;
   if (!get_cur || !get_id) return false;
   CUcontext ctx = nullptr;
   if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;

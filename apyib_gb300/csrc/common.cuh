@@ -4,6 +4,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <vector>
 
 #include "../../include/apyib_gb300.h"
@@ -99,6 +100,21 @@ inline int grid_for(int64_t n, int threads, int64_t cap = 152LL * 64) {
       return AGB_ERR_ARG;                                         \
     }                                                             \
   } while (0)
+
+namespace agb {
+// Runs setup() once per device (CUDA keeps kernel attributes per device): `done` holds one
+// bit per device ordinal; a setup that fails, or a device past ordinal 63, is tried again
+// on the next call.
+template <class F>
+agb_status once_per_device(std::atomic<uint64_t>& done, F setup) {
+  int dev = -1;
+  const uint64_t bit = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return AGB_OK;
+  const agb_status st = setup();
+  if (st == AGB_OK && bit) done.fetch_or(bit, std::memory_order_release);
+  return st;
+}
+}  // namespace agb
 
 void agb_set_error_message(const char* msg, const char* file, int line);
 // Process-wide count of kernels this library has launched (diagnostics only).

@@ -293,11 +293,11 @@ agb_status dfgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
     AGB_LAUNCH_CHECK();
     launch_split(B, N, sBn, sBk, conjB, B4, B2);
     AGB_LAUNCH_CHECK();
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint64_t> attr_done{0};
+    AGB_STATUS_TRY(once_per_device(attr_done, [&]() -> agb_status {
       AGB_CUDA_TRY(cudaFuncSetAttribute(dfgemm3m_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DF3_SMEM));
-      attr = true;
-    }
+      return AGB_OK;
+    }));
     int sp = zgemm_splits(M, N, Kp, rest_bytes);
     int64_t kc = Kp;
     if (sp > 1) {

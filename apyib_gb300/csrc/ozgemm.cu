@@ -1191,11 +1191,11 @@ agb_status ozgemm_ex(int64_t M, int64_t N, int64_t K, z64 alpha, const z64* A, i
     agb_set_error_message("ozgemm: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::atomic<uint64_t> attr_done{0};
+  AGB_STATUS_TRY(once_per_device(attr_done, [&]() -> agb_status {
     AGB_CUDA_TRY(cudaFuncSetAttribute(ozgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set = true;
-  }
+    return AGB_OK;
+  }));
   // row exponents then slices of np parts (part0 ...) of an operand, one read of it each
   auto slice = [&](const z64* src, int64_t rows, int64_t s_row, int64_t s_k, int conj, int part0, int np,
                    int64_t rows_pad, int* emax, int* fexp, uint16_t* dst) -> agb_status {

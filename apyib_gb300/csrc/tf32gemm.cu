@@ -1021,8 +1021,8 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
     agb_set_error_message("tf32_gemm_planes: cuTensorMapEncodeTiled failed", __FILE__, __LINE__);
     return AGB_ERR_CUDA;
   }
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::atomic<uint64_t> attr_done{0};
+  AGB_STATUS_TRY(once_per_device(attr_done, [&]() -> agb_status {
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Tile<256>::SMEM_BYTES));
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1031,8 +1031,8 @@ agb_status tf32_gemm_planes(int64_t M, int64_t N, int64_t K, z64 alpha, const fl
                                       Tile<160>::SMEM_BYTES));
     AGB_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       P2_SMEM_BYTES));
-    attr_set = true;
-  }
+    return AGB_OK;
+  }));
   GemmParams p;
   p.M = M; p.N = N; p.nkb = nkb_split; p.nkb_total = (int)nkb;
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.partial = splits > 1 ? partials : nullptr; p.err = err;

@@ -12,8 +12,9 @@
  * device workspace is sized by the library and owned by the caller.
  * Mutable state lives in the caller's plan and workspace; what the library keeps
  * for the whole process is the last error message (one per host thread), an atomic
- * count of kernel launches (agb_launch_count, diagnostics) and the small device
- * array of agb_vec_dots_noalloc (see there).  A plan is used by one caller at a time.
+ * count of kernel launches (agb_launch_count, diagnostics), which kernels' attributes
+ * were already set on which device, and the small device array of
+ * agb_vec_dots_noalloc (see there).  A plan is used by one caller at a time.
  *
  * Reference cross-walk (apyib project paths):
  *   agb_zgemm / agb_cgemm_tf32x3   opt_einsum contractions of apyib/ci_wfn.py:309-334
