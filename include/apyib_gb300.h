@@ -107,8 +107,10 @@ agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double alpha_re, d
  * each row of A and column of B is scaled by a power of two and cut into six
  * 7-bit digits stored as bf16 slices; the 21 slice products that carry 42 bits
  * run as tcgen05 kind::f16 MMAs whose low-order group sums stay exact in FP32
- * over 512-long K chunks and are drained into int64; complex products use three
- * real products.  scratch: agb_zgemm_oz_scratch_bytes(M, N, K), 256-byte aligned,
+ * over K chunks and are drained into int64.  K <= 1024: one pass over Re and Im
+ * (four real products sharing one exponent per row, 256-long chunks, C written
+ * once); longer K: three real products (3M, 512-long chunks).  scratch:
+ * agb_zgemm_oz_scratch_bytes(M, N, K), 256-byte aligned,
  * its first word the kernel's error word (agb_scratch_status).  Exponents of
  * A and B entries must stay within 2^+-500 of one another's row scales. */
 size_t agb_zgemm_oz_scratch_bytes(int64_t M, int64_t N, int64_t K);
