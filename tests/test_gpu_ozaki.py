@@ -45,7 +45,9 @@ def oz(A, B, alpha=1.0, beta=0.0, C=None, conjA=False, conjB=False, transA=False
                                    (5, 7, 3), (200, 160, 1025), (129, 33, 1024), (257, 31, 257), (64, 96, 96),
                                    # several tiles per persistent CTA; last column tiles 16 or 32 wide;
                                    # one to four 256-long chunks per tile
-                                   (20000, 150, 150), (3000, 100, 300), (2000, 20, 520), (1500, 64, 1024)])
+                                   (20000, 150, 150), (3000, 100, 300), (2000, 20, 520), (1500, 64, 1024),
+                                   # the largest K sliced in one read (32 rows x 192 k staged) and the next
+                                   (3000, 70, 192), (3000, 70, 193)])
 def test_oz_gemm_accuracy(M, N, K):
     rng = np.random.default_rng(M + 7 * N + 13 * K)
     A = crandn(rng, M, K)
