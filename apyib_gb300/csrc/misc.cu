@@ -569,6 +569,14 @@ __global__ void __launch_bounds__(512) jk_sym64_kernel(const double* __restrict_
   }
 }
 }  // namespace
+
+// Complex elements each of the transform's two intermediates must hold: the first
+// quarter step writes nbf^3 nmo of them, the second nbf^2 nmo^2, the third nbf nmo^3
+// (into the first buffer again); the fourth writes the caller's output.
+int64_t ao2mo_intermediate_elems(int64_t nbf, int64_t nmo) {
+  const int64_t q1 = nbf * nbf * nbf * nmo, q2 = nbf * nbf * nmo * nmo, q3 = nbf * nmo * nmo * nmo;
+  return q1 > q2 ? (q1 > q3 ? q1 : q3) : (q2 > q3 ? q2 : q3);
+}
 }  // namespace agb
 
 using namespace agb;
@@ -643,10 +651,7 @@ agb_status agb_mp2_so(agb_cisd_plan* P, void* t, void* E_out, void* partials, si
 }
 
 size_t agb_ao2mo_scratch_bytes(int64_t nbf, int64_t nmo, int precision) {
-  int64_t big = nbf * nbf * nbf * nmo;
-  int64_t mid = nbf * nbf * nmo * nmo;
-  int64_t a = big > mid ? big : mid;
-  size_t s = sizeof(z64) * (size_t)a;
+  size_t s = sizeof(z64) * (size_t)agb::ao2mo_intermediate_elems(nbf, nmo);
   s = (s + 255) & ~(size_t)255;
   size_t gs = (size_t)64 << 20;
   // the four quarter steps: rows (n l s), (l s p), (s p q), (p q r); N = nmo, K = nbf
@@ -677,8 +682,7 @@ agb_status agb_ao2mo(const double* ERI_AO, int64_t nbf, const void* C, int64_t n
     return AGB_ERR_WORKSPACE;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  int64_t big = nbf * nbf * nbf * nmo, mid = nbf * nbf * nmo * nmo;
-  size_t s = sizeof(z64) * (size_t)(big > mid ? big : mid);
+  size_t s = sizeof(z64) * (size_t)ao2mo_intermediate_elems(nbf, nmo);
   s = (s + 255) & ~(size_t)255;
   char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
   z64* Y1 = (z64*)base;

@@ -139,3 +139,33 @@ def test_transform_tf32x3_matches_fp64_multi_tile(n):
     scale = out[_lib.PREC_FP64].abs().max().item()
     err = (out[_lib.PREC_TF32X3] - out[_lib.PREC_FP64]).abs().max().item() / scale
     assert err < 1e-5, err
+
+
+def test_transform_tf32x3_256_wide_tile():
+    """nmo = 168 (> 160) puts every quarter step of the 3xTF32 transform on the converter
+    GEMM's 256-wide tile (Re and Im accumulators filling TMEM's 512 columns, two stages);
+    nbf = 20 keeps K and the intermediates small (the output is 168^4 complex, 12.7 GB).
+    Against the Ozaki transform (FP64-accurate; the FP64 GEMM's grid does not reach
+    168^3 rows), bound as in the multi-tile test: 1e-5 of the largest element."""
+    import ctypes
+
+    from apyib_gb300.device import ptr, stream_ptr, workspace
+    nbf, nmo = 20, 168
+    g = torch.Generator(device="cpu").manual_seed(7)
+    A = torch.randn(2 * nbf, nbf, nbf, generator=g, dtype=torch.float64)
+    A = ((A + A.transpose(1, 2)) / (2 * (2 * nbf * nbf) ** 0.5)).cuda()
+    eri = torch.einsum("Lmn,Lls->mnls", A, A).contiguous()
+    Cm = (torch.randn(nbf, nmo, generator=g, dtype=torch.complex128) / nbf ** 0.5).cuda().contiguous()
+    out = {}
+    for prec in (_lib.PREC_OZAKI, _lib.PREC_TF32X3):
+        o = torch.empty(nmo, nmo, nmo, nmo, dtype=torch.complex128, device="cuda")
+        nb = _lib.load().agb_ao2mo_scratch_bytes(nbf, nmo, prec)
+        buf, sp, _ = workspace(nb)
+        _lib.call("agb_ao2mo", ptr(eri), nbf, ptr(Cm), nmo, ptr(o), ctypes.c_void_p(sp), ctypes.c_size_t(nb), prec,
+                  stream_ptr())
+        torch.cuda.synchronize()
+        out[prec] = o
+        del buf
+    scale = out[_lib.PREC_OZAKI].abs().max().item()
+    err = (out[_lib.PREC_TF32X3] - out[_lib.PREC_OZAKI]).abs().max().item() / scale
+    assert err < 1e-5, err
