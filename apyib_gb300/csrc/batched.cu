@@ -191,6 +191,7 @@ agb_status agb_zgemm_batched(int64_t batch, int64_t M, int64_t N, int64_t K, dou
   AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "zgemm_batched: conj flags must be 0 or 1");
   if (batch == 0 || M == 0 || N == 0) return AGB_OK;
   AGB_ARG_CHECK(A && B && C, "zgemm_batched: null pointer");
+  AGB_ARG_CHECK(M <= 1 || ldc >= N, "zgemm_batched: ldc must be at least N (C is row-major)");
   AGB_ARG_CHECK((M + TB - 1) / TB <= 65535 && (N + TB - 1) / TB <= 2147483647LL, "zgemm_batched: M too large");
   BGemmArgs p{M, N, K, zmk(alpha_re, alpha_im), zmk(beta_re, beta_im), (const z64*)A, sAm, sAk, sAb, conjA,
               (const z64*)B, sBk, sBn, sBb, conjB, (z64*)C, ldc, sCb, 0};

@@ -1424,7 +1424,7 @@ size_t agb_vec_partials_bytes(int ny) {
 
 agb_status agb_vec_dots(int64_t n1, int64_t n2, double w1, double w2, const void* x, const void* const* ys, int ny,
                         void* out, void* partials, size_t partials_bytes, void* stream) {
-  AGB_ARG_CHECK(x && ys && out && ny >= 1 && ny <= kMaxVec, "vec_dots: bad argument");
+  AGB_ARG_CHECK(x && ys && out && n1 >= 0 && n2 >= 0 && ny >= 1 && ny <= kMaxVec, "vec_dots: bad argument");
   if (!partials || partials_bytes < agb_vec_partials_bytes(ny)) {
     agb_set_error_message("vec_dots: partials buffer too small", __FILE__, __LINE__);
     return AGB_ERR_WORKSPACE;

@@ -351,6 +351,7 @@ extern "C" agb_status agb_zgemm_df64_ex(int64_t M, int64_t N, int64_t K, double 
                                         int64_t sBk, int64_t sBn, int conjB, double beta_re, double beta_im, void* C,
                                         int64_t ldc, void* scratch, size_t scratch_bytes, void* stream) {
   AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  AGB_ARG_CHECK(M <= 1 || N <= 0 || ldc >= N, "gemm: ldc must be at least N (C is row-major)");
   return agb::dfgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                         (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, scratch,
                         scratch_bytes, (cudaStream_t)stream);
@@ -360,6 +361,7 @@ extern "C" agb_status agb_zgemm_df64(int64_t M, int64_t N, int64_t K, double alp
                                      int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,
                                      int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* stream) {
   AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  AGB_ARG_CHECK(M <= 1 || N <= 0 || ldc >= N, "gemm: ldc must be at least N (C is row-major)");
   return agb::dfgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                         (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc, nullptr, 0,
                         (cudaStream_t)stream);

@@ -1156,6 +1156,7 @@ agb_status agb_cgemm_tf32x3(int64_t M, int64_t N, int64_t K, double alpha_re, do
                             double beta_re, double beta_im, void* C, int64_t ldc, void* scratch, size_t scratch_bytes,
                             void* stream) {
   AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  AGB_ARG_CHECK(M <= 1 || N <= 0 || ldc >= N, "gemm: ldc must be at least N (C is row-major)");
   return agb::cgemm_tf32x3(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                            (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
                            scratch, scratch_bytes, (cudaStream_t)stream);

@@ -307,6 +307,7 @@ extern "C" agb_status agb_zgemm(int64_t M, int64_t N, int64_t K, double alpha_re
                                 int64_t sAm, int64_t sAk, int conjA, const void* B, int64_t sBk, int64_t sBn,
                                 int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* stream) {
   AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  AGB_ARG_CHECK(M <= 1 || N <= 0 || ldc >= N, "gemm: ldc must be at least N (C is row-major)");
   return agb::zgemm(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                     (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,
                     (cudaStream_t)stream);
@@ -323,6 +324,7 @@ extern "C" agb_status agb_zgemm_ex(int64_t M, int64_t N, int64_t K, double alpha
                                    int conjB, double beta_re, double beta_im, void* C, int64_t ldc, void* scratch,
                                    size_t scratch_bytes, void* stream) {
   AGB_ARG_CHECK((conjA == 0 || conjA == 1) && (conjB == 0 || conjB == 1), "gemm: conj flags must be 0 or 1");
+  AGB_ARG_CHECK(M <= 1 || N <= 0 || ldc >= N, "gemm: ldc must be at least N (C is row-major)");
   AGB_ARG_CHECK(scratch != nullptr || scratch_bytes == 0, "gemm: scratch is NULL with a nonzero size");
   return agb::zgemm_ex(M, N, K, agb::zmk(alpha_re, alpha_im), (const agb::z64*)A, sAm, sAk, conjA,
                        (const agb::z64*)B, sBk, sBn, conjB, agb::zmk(beta_re, beta_im), (agb::z64*)C, ldc,

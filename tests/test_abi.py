@@ -57,3 +57,18 @@ def test_bad_arguments_are_rejected():
         _lib.call("agb_cisd_plan_create", 3, 4, 0, ctypes.byref(h))   # odd o
     with pytest.raises(_lib.AGBError):
         _lib.call("agb_cisd_plan_set_workspace", ctypes.c_void_p(0), ctypes.c_void_p(0), 0)
+
+
+@pytest.mark.parametrize("entry,extra", [("agb_zgemm", []), ("agb_zgemm_df64", []),
+                                         ("agb_zgemm_ex", [ctypes.c_void_p(0), ctypes.c_size_t(0)]),
+                                         ("agb_zgemm_df64_ex", [ctypes.c_void_p(0), ctypes.c_size_t(0)]),
+                                         ("agb_zgemm_oz", [ctypes.c_void_p(0), ctypes.c_size_t(0)]),
+                                         ("agb_cgemm_tf32x3", [ctypes.c_void_p(0), ctypes.c_size_t(0)])])
+def test_gemm_rejects_short_leading_dimension(entry, extra):
+    """A row-major C needs ldc >= N (fewer would overlap its rows and write past the
+    buffer): every GEMM entry point refuses it before touching the device."""
+    fake = ctypes.c_void_p(4096)          # never dereferenced: the call returns first
+    M, N, K = 8, 6, 4
+    with pytest.raises(_lib.AGBError, match="ldc"):
+        _lib.call(entry, M, N, K, 1.0, 0.0, fake, K, 1, 0, fake, N, 1, 0, 0.0, 0.0, fake, N - 1, *extra,
+                  ctypes.c_void_p(0))
