@@ -18,11 +18,14 @@
 // tensor core accumulates in FP32 with truncation (round toward zero), so only
 // this small tail may round: group 3 kept in the tail gave 8x the error.
 //
-// Complex operands use three real products (3M): P1 = Re.Re, P2 = Im.Im,
-// P3 = (Re+Im).(Re+Im); C = alpha (P1 - P2 + i (P3 - P1 - P2)) + beta C, each
-// product's epilogue adding alpha * (1 - i, -1 - i, i)[part] * P into C.
+// Long K (> 1024): complex operands use three real products (3M): P1 = Re.Re,
+// P2 = Im.Im, P3 = (Re+Im).(Re+Im); C = alpha (P1 - P2 + i (P3 - P1 - P2)) + beta C,
+// each product's epilogue adding alpha * (1 - i, -1 - i, i)[part] * P into C.
+// Short K (<= 1024, e.g. every AO->MO quarter step): the one-pass kernel (ozc_kernel,
+// below) shares one exponent between a row's Re and Im parts, accumulates Re C and
+// Im C side by side from the four real products and writes C once.
 //
-// Tiles: one CTA per 128x96 output tile (five 96-column accumulators fill 480 of
+// Tiles of the 3M kernel: one CTA per 128x96 output tile (five 96-column accumulators fill 480 of
 // TMEM's 512 columns), 2-stage TMA pipeline of 6 A (128 x 32 bf16) and 6 B
 // (96 x 32 bf16) slice tiles, 64-byte swizzle, 84 KB per stage; warp 0 loads,
 // warp 1 issues the MMAs from one thread, warps 2-9 drain TMEM (two warps per
