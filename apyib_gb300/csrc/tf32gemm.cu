@@ -12,8 +12,10 @@
 // 256 x 256 tiles, 3 stages); the rest on single CTAs (128 x 256 tiles, or a tile
 // and K split): warp 0 issues TMA loads, warp 1 issues the MMAs from one thread,
 // warps 2-5 drain the two TMEM accumulators (Re in columns 0-255, Im in 256-511)
-// and write FP64 results.  Every mbarrier wait is bounded; on timeout the kernel
-// records an error word and returns after releasing TMEM.
+// and write FP64 results.  Outputs up to 256 wide whose A is an FP64 intermediate (the
+// AO->MO quarter steps) take a persistent kernel whose converter warps split A into
+// the planes in shared memory themselves.  Every mbarrier wait is bounded; on timeout
+// the kernel records an error word and returns after releasing TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
